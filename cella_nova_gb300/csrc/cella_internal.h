@@ -1,0 +1,81 @@
+// cella_internal.h — types shared by the host orchestrator and the kernels.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace cg {
+
+constexpr int kMaxC = 16;   // compute_1024.wgsl:307 holds at most 16 channels
+constexpr int kMaxK = 64;
+constexpr int kMinLogN = 4;
+constexpr int kMaxLogN = 11;
+
+// Kernels grouped by the channel they read (conv pass) and by the channel
+// they feed (growth pass), each group in increasing k.
+struct KernelGroups {
+    int in_count[kMaxC], in_start[kMaxC];
+    int out_count[kMaxC], out_start[kMaxC];
+    int in_idx[kMaxK];    // kernels sorted by c0
+    int out_idx[kMaxK];   // kernels sorted by c1
+};
+
+// Growth parameters per kernel (growth.rs:46-75): mu, 1/sigma^2, weight.
+struct GrowthParams {
+    float mu[kMaxK];
+    float inv_s2[kMaxK];
+    float w[kMaxK];
+};
+
+// Everything one step's launches need.  Planar layouts, all device pointers:
+//   x_in, x_out : [C][n][n] f32 state (ping-pong)
+//   rowspec     : [C][n/2][n] complex — row spectra, transposed (kx-major)
+//   kspec       : [K][n/2+1][n] complex — Hermitian part of each kernel
+//                 spectrum scaled by 1/(2 n^2), kx-major; column 0 holds
+//                 (K(.,0)+K(.,n/2))/2, column n/2 holds (K(.,0)-K(.,n/2))/2
+//   U           : [K][n/2][n] complex — column-inverted products, kx-major
+//   A           : [C][n][n] f32 — exp(temp * weighted growth)
+//   tw          : [n] complex — W_n^m
+struct StepArgs {
+    int C, K;
+    float temp;
+    const float* x_in;
+    float* x_out;
+    float2* rowspec;
+    const float2* kspec;
+    float2* U;
+    float* A;
+    const float2* tw;
+    float* udbg;   // optional [K][n][n] f32: Re(conv) before the 1/n^2 scale
+    KernelGroups groups;
+    GrowthParams gp;
+};
+
+// Phase bits for launch_step (timed_iterate splits the step into phases).
+enum : int {
+    kPhaseRowFwd = 1,
+    kPhaseColConv = 2,
+    kPhaseGrowth = 4,
+    kPhaseDiffusion = 8,
+    kPhaseAll = 15,
+};
+
+// Per grid size (LOGN = 6..11), defined in kernels_l*.cu.
+typedef cudaError_t (*launch_step_fn)(const StepArgs&, int phases, cudaStream_t);
+typedef cudaError_t (*pack_kernel_fn)(const float2* full, float2* out, cudaStream_t);
+typedef cudaError_t (*prepare_fn)();
+
+struct SizeOps {
+    launch_step_fn step;
+    pack_kernel_fn pack;
+    prepare_fn prepare;
+};
+
+const SizeOps* size_ops(int logn);
+
+// Size-independent kernels (kernels_common.cu).
+cudaError_t launch_f64_to_f32(const double* in, float* out, size_t count, cudaStream_t s);
+cudaError_t launch_mass_f64(const float* x, int C, size_t px, double* partial, int nblocks,
+                            double* out, cudaStream_t s);
+constexpr int kMassBlocks = 296;   // 2 per SM on a 148/152-SM part
+
+}  // namespace cg

@@ -1,0 +1,172 @@
+// fft.cuh — shared-memory batched FFT building blocks for sm_103a.
+//
+// The reference transforms each row or column of the grid with a radix-2 DIT
+// FFT in WGSL (ml-rs/shaders/compute_1024.wgsl:38-218): a bit-reversal LUT
+// on load, eight radix-2 stages in workgroup memory and two or three in
+// registers, twiddles from an f32-angle host table (convolution.rs:19-30).
+// This file does the same transform differently: a mixed-radix Stockham
+// auto-sort FFT (radix 16 passes, then one radix 2/4/8 pass), natural order
+// in and out, every pass a register-resident DFT-R between two shared-memory
+// exchanges, twiddles from a table of W_N^m rounded once from double.
+//
+// A CTA transforms S independent sequences of length L at once.  Each pass
+// is written against load / store functors so that the first pass can read
+// global memory (or pre-process while loading) and the last pass can write
+// global memory (or feed an epilogue) without an extra shared-memory trip.
+#pragma once
+#include <cuda_runtime.h>
+
+namespace cg {
+
+// Shared-memory index padding: one spare float2 per 16, which keeps the
+// strided stores of every pass free of bank conflicts within a half-warp.
+__device__ __forceinline__ int pidx(int i) { return i + (i >> 4); }
+__host__ __device__ constexpr int padded_len(int n) { return n + n / 16; }
+
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+    return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+// a * conj(b)
+__device__ __forceinline__ float2 cmulc(float2 a, float2 b) {
+    return make_float2(a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y);
+}
+__device__ __forceinline__ float2 cconj(float2 a) { return make_float2(a.x, -a.y); }
+
+// cos(2*pi*q/16) and sin(2*pi*q/16), q = 0..15 (exact constants to float).
+__device__ __forceinline__ constexpr float cos16(int q) {
+    return q == 0 ? 1.0f : q == 1 ? 0.92387953251128674f : q == 2 ? 0.70710678118654752f
+         : q == 3 ? 0.38268343236508977f : q == 4 ? 0.0f : q == 5 ? -0.38268343236508977f
+         : q == 6 ? -0.70710678118654752f : q == 7 ? -0.92387953251128674f : q == 8 ? -1.0f
+         : q == 9 ? -0.92387953251128674f : q == 10 ? -0.70710678118654752f
+         : q == 11 ? -0.38268343236508977f : q == 12 ? 0.0f : q == 13 ? 0.38268343236508977f
+         : q == 14 ? 0.70710678118654752f : 0.92387953251128674f;
+}
+__device__ __forceinline__ constexpr float sin16(int q) { return cos16((q + 12) & 15); }
+
+// a * exp(-+2*pi*i*q16/16): forward uses the minus sign, inverse the plus.
+// Called with compile-time q16 after unrolling, so the branches fold.
+template <bool INV>
+__device__ __forceinline__ float2 rot16(float2 a, int q16) {
+    if (q16 == 0) return a;
+    if (q16 == 4) return INV ? make_float2(-a.y, a.x) : make_float2(a.y, -a.x);
+    if (q16 == 8) return make_float2(-a.x, -a.y);
+    if (q16 == 12) return INV ? make_float2(a.y, -a.x) : make_float2(-a.y, a.x);
+    const float c = cos16(q16), s = sin16(q16);
+    return INV ? make_float2(a.x * c - a.y * s, a.y * c + a.x * s)
+               : make_float2(a.x * c + a.y * s, a.y * c - a.x * s);
+}
+
+// In-register DFT of size R (1, 2, 4, 8, 16), natural order in and out.
+template <int R, bool INV>
+struct Dft {
+    __device__ __forceinline__ static void run(float2* v) {
+        float2 e[R / 2], o[R / 2];
+#pragma unroll
+        for (int i = 0; i < R / 2; ++i) { e[i] = v[2 * i]; o[i] = v[2 * i + 1]; }
+        Dft<R / 2, INV>::run(e);
+        Dft<R / 2, INV>::run(o);
+#pragma unroll
+        for (int q = 0; q < R / 2; ++q) {
+            const float2 t = rot16<INV>(o[q], q * (16 / R));
+            v[q] = cadd(e[q], t);
+            v[q + R / 2] = csub(e[q], t);
+        }
+    }
+};
+template <bool INV>
+struct Dft<2, INV> {
+    __device__ __forceinline__ static void run(float2* v) {
+        const float2 a = v[0], b = v[1];
+        v[0] = cadd(a, b);
+        v[1] = csub(a, b);
+    }
+};
+template <bool INV>
+struct Dft<1, INV> {
+    __device__ __forceinline__ static void run(float2*) {}
+};
+
+// Radix of the pass that starts at sub-transform size NS.
+template <int L, int NS>
+struct PassRadix {
+    static constexpr int R = (L / NS >= 16) ? 16 : (L / NS);
+};
+
+// Radix of the last pass of a length-L transform.
+__host__ __device__ constexpr int last_radix(int L) {
+    int ns = 1, r = 1;
+    while (ns < L) {
+        r = (L / ns >= 16) ? 16 : L / ns;
+        ns *= r;
+    }
+    return r;
+}
+
+// One Stockham pass (radix R, sub-transform size NS) over S sequences of
+// length L, with T threads.  Work item `item` = (sequence s, butterfly j);
+// thread t owns items t, t+T, ...  It loads v[r] = x[j + r*L/R], applies
+// W_{NS*R}^{r*(j mod NS)}, runs DFT-R and stores v[q] at
+// (j div NS)*NS*R + (j mod NS) + q*NS.  All loads finish (barrier) before any
+// store, so in-place passes are safe; a second barrier closes the pass.
+//   twN : W_N^m = exp(-2*pi*i*m/N), m in [0, N); TWS = N / L.
+//   ld(s, i)                -> float2
+//   st(s, i, v, it, q)      (it, q) name the register slot that held v.
+template <int L, int R, int NS, bool INV, int T, int S, int TWS, class LD, class ST>
+__device__ __forceinline__ void stockham_pass(LD& ld, ST& st, const float2* __restrict__ twN) {
+    constexpr int J = L / R;
+    constexpr int ITEMS = S * J;
+    constexpr int IPT = (ITEMS + T - 1) / T;
+    float2 v[IPT][R];
+#pragma unroll
+    for (int it = 0; it < IPT; ++it) {
+        const int item = threadIdx.x + it * T;
+        if (ITEMS % T == 0 || item < ITEMS) {
+            const int s = item / J, j = item % J;
+#pragma unroll
+            for (int r = 0; r < R; ++r) v[it][r] = ld(s, j + r * J);
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int it = 0; it < IPT; ++it) {
+        const int item = threadIdx.x + it * T;
+        if (ITEMS % T == 0 || item < ITEMS) {
+            const int s = item / J, j = item % J;
+            const int k = j % NS;
+            if (NS > 1) {
+#pragma unroll
+                for (int r = 1; r < R; ++r) {
+                    float2 w = __ldg(&twN[r * k * (L / (NS * R)) * TWS]);
+                    if (INV) w.y = -w.y;
+                    v[it][r] = cmul(v[it][r], w);
+                }
+            }
+            Dft<R, INV>::run(v[it]);
+            const int d = (j / NS) * NS * R + k;
+#pragma unroll
+            for (int r = 0; r < R; ++r) st(s, d + r * NS, v[it][r], it, r);
+        }
+    }
+    __syncthreads();
+}
+
+// Full length-L transform: first pass reads through `ld`, middle passes use
+// shared memory through smld/smst, the last pass writes through `stl`.
+template <int L, int NS, bool INV, int T, int S, int TWS>
+struct FftPasses {
+    template <class LD, class SMLD, class SMST, class STL>
+    __device__ __forceinline__ static void run(LD& ld, SMLD& smld, SMST& smst, STL& stl,
+                                               const float2* __restrict__ twN) {
+        constexpr int R = PassRadix<L, NS>::R;
+        if constexpr (NS * R == L) {
+            stockham_pass<L, R, NS, INV, T, S, TWS>(ld, stl, twN);
+        } else {
+            stockham_pass<L, R, NS, INV, T, S, TWS>(ld, smst, twN);
+            FftPasses<L, NS * R, INV, T, S, TWS>::run(smld, smld, smst, stl, twN);
+        }
+    }
+};
+
+}  // namespace cg

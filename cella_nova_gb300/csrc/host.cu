@@ -1,0 +1,484 @@
+// host.cu — the GpuMaceLenia orchestrator (ml-rs/orchestrator/mod.rs) in C++
+// behind the C ABI of include/cella_gpu.h.
+//
+// Buffers (mod.rs:109-122 allocates channel, new_channel, affinity, z,
+// kernel, conv, render) become: two state planes used in turn (no
+// new_channel -> channel copy, mod.rs:377-383), row spectra, packed kernel
+// half spectra, column-inverted products and the affinity exponential.  The
+// Z buffer and the render buffer do not exist: Z lives in shared memory and
+// rendering is not part of the step.  A step is two CUDA graphs, one per
+// ping-pong parity, captured once at creation.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "cella_gpu.h"
+#include "cella_internal.h"
+
+namespace cg {
+extern const SizeOps size_ops_l4, size_ops_l5, size_ops_l6, size_ops_l7, size_ops_l8, size_ops_l9, size_ops_l10,
+    size_ops_l11;
+
+const SizeOps* size_ops(int logn) {
+    switch (logn) {
+        case 4: return &size_ops_l4;
+        case 5: return &size_ops_l5;
+        case 6: return &size_ops_l6;
+        case 7: return &size_ops_l7;
+        case 8: return &size_ops_l8;
+        case 9: return &size_ops_l9;
+        case 10: return &size_ops_l10;
+        case 11: return &size_ops_l11;
+        default: return nullptr;
+    }
+}
+
+thread_local std::string g_last_error;
+
+int fail(int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what) {
+    if (e == cudaErrorMemoryAllocation)
+        return fail(CG_ERR_OOM, "%s: %s", what, cudaGetErrorString(e));
+    return fail(CG_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define CG_CHECK(call, what)                                \
+    do {                                                    \
+        cudaError_t e_ = (call);                            \
+        if (e_ != cudaSuccess) return cuda_fail(e_, what);  \
+    } while (0)
+
+}  // namespace cg
+
+using namespace cg;
+
+struct cg_sim {
+    int n = 0, logn = 0, C = 0, K = 0;
+    float temp = 1.f;
+    std::vector<uint32_t> c0, c1;
+    std::vector<float> mu, sigma, w;
+    const SizeOps* ops = nullptr;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    float* state[2] = {nullptr, nullptr};
+    int cur = 0;
+    float2* rowspec = nullptr;
+    float2* kspec = nullptr;
+    float2* U = nullptr;
+    float* A = nullptr;
+    float2* tw = nullptr;
+    void* staging = nullptr;
+    double* mass_partial = nullptr;
+    double* mass_out = nullptr;
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    KernelGroups groups{};
+    GrowthParams gp{};
+
+    size_t px() const { return size_t(n) * n; }
+
+    StepArgs args(int from, float* udbg) const {
+        StepArgs a{};
+        a.C = C;
+        a.K = K;
+        a.temp = temp;
+        a.x_in = state[from];
+        a.x_out = state[from ^ 1];
+        a.rowspec = rowspec;
+        a.kspec = kspec;
+        a.U = U;
+        a.A = A;
+        a.tw = tw;
+        a.udbg = udbg;
+        a.groups = groups;
+        a.gp = gp;
+        return a;
+    }
+};
+
+namespace {
+
+void release(cg_sim* s) {
+    if (!s) return;
+    cudaSetDevice(s->device);
+    for (auto& g : s->graph)
+        if (g) cudaGraphExecDestroy(g);
+    for (auto& e : s->ev)
+        if (e) cudaEventDestroy(e);
+    cudaFree(s->state[0]);
+    cudaFree(s->state[1]);
+    cudaFree(s->rowspec);
+    cudaFree(s->kspec);
+    cudaFree(s->U);
+    cudaFree(s->A);
+    cudaFree(s->tw);
+    cudaFree(s->staging);
+    cudaFree(s->mass_partial);
+    cudaFree(s->mass_out);
+    if (s->own_stream && s->stream) cudaStreamDestroy(s->stream);
+    delete s;
+}
+
+int capture_graphs(cg_sim* s) {
+    cudaStream_t cap;
+    CG_CHECK(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking), "cudaStreamCreate(capture)");
+    for (int p = 0; p < 2; ++p) {
+        cudaGraph_t g = nullptr;
+        cudaError_t e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) {
+            cudaError_t le = s->ops->step(s->args(p, nullptr), kPhaseAll, cap);
+            e = cudaStreamEndCapture(cap, &g);
+            if (le != cudaSuccess) e = le;
+        }
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&s->graph[p], g, 0);
+        if (g) cudaGraphDestroy(g);
+        if (e != cudaSuccess) {
+            cudaStreamDestroy(cap);
+            return cuda_fail(e, "capturing the step graph");
+        }
+    }
+    cudaStreamDestroy(cap);
+    return CG_OK;
+}
+
+int build_twiddles(cg_sim* s) {
+    std::vector<float2> h(s->n);
+    for (int m = 0; m < s->n; ++m) {
+        // W_n^m rounded once from double (the reference's table uses an f32
+        // angle, convolution.rs:25-26).
+        const double a = -2.0 * M_PI * double(m) / double(s->n);
+        h[m] = make_float2(float(std::cos(a)), float(std::sin(a)));
+    }
+    CG_CHECK(cudaMemcpy(s->tw, h.data(), sizeof(float2) * s->n, cudaMemcpyHostToDevice),
+             "uploading twiddles");
+    return CG_OK;
+}
+
+bool finite(float v) { return std::isfinite(v); }
+
+}  // namespace
+
+extern "C" {
+
+const char* cg_last_error(void) { return g_last_error.c_str(); }
+
+const char* cg_version(void) { return "cella-gb300 0.1 (sm_103a)"; }
+
+int cg_create(int n, int C, int K, const uint32_t* c0, const uint32_t* c1, const float* mu,
+              const float* sigma, const float* weights, float temp, cg_stream_t stream,
+              cg_sim** out) {
+    if (!out) return fail(CG_ERR_ARG, "cg_create: out is NULL");
+    *out = nullptr;
+    int logn = 0;
+    while ((1 << logn) < n && logn < 30) ++logn;
+    if (n <= 0 || (1 << logn) != n)
+        return fail(CG_ERR_ARG, "grid side %d is not a power of two", n);
+    if (logn < kMinLogN || logn > kMaxLogN)
+        return fail(CG_ERR_UNSUPPORTED, "grid side %d outside [%d, %d]", n, 1 << kMinLogN,
+                    1 << kMaxLogN);
+    if (C < 1 || C > kMaxC) return fail(CG_ERR_ARG, "channel count %d outside [1, %d]", C, kMaxC);
+    if (K < 1 || K > kMaxK) return fail(CG_ERR_ARG, "kernel count %d outside [1, %d]", K, kMaxK);
+    if (!c0 || !c1 || !mu || !sigma || !weights)
+        return fail(CG_ERR_ARG, "cg_create: NULL parameter array");
+    for (int k = 0; k < K; ++k) {
+        if (c0[k] >= uint32_t(C) || c1[k] >= uint32_t(C))
+            return fail(CG_ERR_ARG, "kernel %d maps channel %u -> %u, but C = %d", k, c0[k],
+                        c1[k], C);
+        if (!finite(mu[k]) || !finite(sigma[k]) || !finite(weights[k]) || sigma[k] == 0.f)
+            return fail(CG_ERR_ARG, "kernel %d has a non-finite or zero-sigma growth parameter",
+                        k);
+    }
+    if (!finite(temp)) return fail(CG_ERR_ARG, "temp is not finite");
+
+    cg_sim* s = new (std::nothrow) cg_sim;
+    if (!s) return fail(CG_ERR_OOM, "cg_create: host allocation failed");
+    s->n = n;
+    s->logn = logn;
+    s->C = C;
+    s->K = K;
+    s->temp = temp;
+    s->c0.assign(c0, c0 + K);
+    s->c1.assign(c1, c1 + K);
+    s->mu.assign(mu, mu + K);
+    s->sigma.assign(sigma, sigma + K);
+    s->w.assign(weights, weights + K);
+    s->ops = size_ops(logn);
+
+    // Groups, in increasing k within each channel.
+    int pos = 0;
+    for (int c = 0; c < C; ++c) {
+        s->groups.in_start[c] = pos;
+        for (int k = 0; k < K; ++k)
+            if (int(c0[k]) == c) s->groups.in_idx[pos++] = k;
+        s->groups.in_count[c] = pos - s->groups.in_start[c];
+    }
+    pos = 0;
+    for (int c = 0; c < C; ++c) {
+        s->groups.out_start[c] = pos;
+        for (int k = 0; k < K; ++k)
+            if (int(c1[k]) == c) s->groups.out_idx[pos++] = k;
+        s->groups.out_count[c] = pos - s->groups.out_start[c];
+    }
+    for (int k = 0; k < K; ++k) {
+        s->gp.mu[k] = mu[k];
+        s->gp.inv_s2[k] = float(1.0 / (double(sigma[k]) * double(sigma[k])));
+        s->gp.w[k] = weights[k];
+    }
+
+    int rc = CG_OK;
+    auto chk = [&](cudaError_t e, const char* what) {
+        if (rc == CG_OK && e != cudaSuccess) rc = cuda_fail(e, what);
+        return rc == CG_OK;
+    };
+    chk(cudaGetDevice(&s->device), "cudaGetDevice");
+    if (rc == CG_OK) {
+        if (stream) {
+            s->stream = static_cast<cudaStream_t>(stream);
+        } else if (chk(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking),
+                       "cudaStreamCreate")) {
+            s->own_stream = true;
+        }
+    }
+    const size_t px = s->px();
+    const size_t half = size_t(n / 2) * n;
+    if (rc == CG_OK) chk(s->ops->prepare(), "configuring kernels");
+    if (rc == CG_OK) chk(cudaMalloc(&s->state[0], sizeof(float) * C * px), "cudaMalloc(state)");
+    if (rc == CG_OK) chk(cudaMalloc(&s->state[1], sizeof(float) * C * px), "cudaMalloc(state)");
+    if (rc == CG_OK) chk(cudaMalloc(&s->rowspec, sizeof(float2) * C * half), "cudaMalloc(rowspec)");
+    if (rc == CG_OK)
+        chk(cudaMalloc(&s->kspec, sizeof(float2) * K * (half + n)), "cudaMalloc(kspec)");
+    if (rc == CG_OK) chk(cudaMalloc(&s->U, sizeof(float2) * K * half), "cudaMalloc(U)");
+    if (rc == CG_OK) chk(cudaMalloc(&s->A, sizeof(float) * C * px), "cudaMalloc(A)");
+    if (rc == CG_OK) chk(cudaMalloc(&s->tw, sizeof(float2) * n), "cudaMalloc(twiddles)");
+    if (rc == CG_OK) chk(cudaMalloc(&s->staging, sizeof(double) * px), "cudaMalloc(staging)");
+    if (rc == CG_OK)
+        chk(cudaMalloc(&s->mass_partial, sizeof(double) * C * kMassBlocks), "cudaMalloc(mass)");
+    if (rc == CG_OK) chk(cudaMalloc(&s->mass_out, sizeof(double) * C), "cudaMalloc(mass)");
+    for (int i = 0; i < 4 && rc == CG_OK; ++i) chk(cudaEventCreate(&s->ev[i]), "cudaEventCreate");
+    if (rc == CG_OK) chk(cudaMemsetAsync(s->state[0], 0, sizeof(float) * C * px, s->stream), "memset");
+    if (rc == CG_OK) chk(cudaMemsetAsync(s->state[1], 0, sizeof(float) * C * px, s->stream), "memset");
+    if (rc == CG_OK)
+        chk(cudaMemsetAsync(s->kspec, 0, sizeof(float2) * K * (half + n), s->stream), "memset");
+    if (rc == CG_OK) rc = build_twiddles(s);
+    if (rc == CG_OK) rc = capture_graphs(s);
+    if (rc == CG_OK) chk(cudaStreamSynchronize(s->stream), "cudaStreamSynchronize");
+    if (rc != CG_OK) {
+        release(s);
+        return rc;
+    }
+    *out = s;
+    return CG_OK;
+}
+
+int cg_destroy(cg_sim* s) {
+    if (!s) return fail(CG_ERR_ARG, "cg_destroy: NULL handle");
+    cudaSetDevice(s->device);
+    cudaStreamSynchronize(s->stream);
+    release(s);
+    return CG_OK;
+}
+
+int cg_set_kernel(cg_sim* s, int k, const float* spec) {
+    if (!s || !spec) return fail(CG_ERR_ARG, "cg_set_kernel: NULL argument");
+    if (k < 0 || k >= s->K) return fail(CG_ERR_ARG, "kernel index %d outside [0, %d)", k, s->K);
+    const size_t half = size_t(s->n / 2) * s->n;
+    CG_CHECK(cudaMemcpyAsync(s->staging, spec, sizeof(float2) * s->px(), cudaMemcpyHostToDevice,
+                             s->stream),
+             "uploading kernel spectrum");
+    CG_CHECK(s->ops->pack(static_cast<const float2*>(s->staging), s->kspec + size_t(k) * (half + s->n),
+                          s->stream),
+             "packing kernel spectrum");
+    return CG_OK;
+}
+
+int cg_upload_channel(cg_sim* s, int c, const double* data) {
+    if (!s || !data) return fail(CG_ERR_ARG, "cg_upload_channel: NULL argument");
+    if (c < 0 || c >= s->C) return fail(CG_ERR_ARG, "channel index %d outside [0, %d)", c, s->C);
+    CG_CHECK(cudaMemcpyAsync(s->staging, data, sizeof(double) * s->px(), cudaMemcpyHostToDevice,
+                             s->stream),
+             "uploading channel");
+    CG_CHECK(launch_f64_to_f32(static_cast<const double*>(s->staging),
+                               s->state[s->cur] + size_t(c) * s->px(), s->px(), s->stream),
+             "converting channel");
+    return CG_OK;
+}
+
+int cg_upload_channel_f32(cg_sim* s, int c, const float* data) {
+    if (!s || !data) return fail(CG_ERR_ARG, "cg_upload_channel_f32: NULL argument");
+    if (c < 0 || c >= s->C) return fail(CG_ERR_ARG, "channel index %d outside [0, %d)", c, s->C);
+    CG_CHECK(cudaMemcpyAsync(s->state[s->cur] + size_t(c) * s->px(), data, sizeof(float) * s->px(),
+                             cudaMemcpyHostToDevice, s->stream),
+             "uploading channel");
+    return CG_OK;
+}
+
+int cg_step(cg_sim* s, int nsteps) {
+    if (!s) return fail(CG_ERR_ARG, "cg_step: NULL handle");
+    if (nsteps < 0) return fail(CG_ERR_ARG, "negative step count %d", nsteps);
+    for (int i = 0; i < nsteps; ++i) {
+        CG_CHECK(cudaGraphLaunch(s->graph[s->cur], s->stream), "cudaGraphLaunch");
+        s->cur ^= 1;
+    }
+    return CG_OK;
+}
+
+int cg_iterate(cg_sim* s) { return cg_step(s, 1); }
+
+int cg_iterate_on(cg_sim* s, cg_stream_t stream) {
+    if (!s) return fail(CG_ERR_ARG, "cg_iterate_on: NULL handle");
+    cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : s->stream;
+    CG_CHECK(cudaGraphLaunch(s->graph[s->cur], st), "cudaGraphLaunch");
+    s->cur ^= 1;
+    return CG_OK;
+}
+
+int cg_download_channels(cg_sim* s, float* out) {
+    if (!s || !out) return fail(CG_ERR_ARG, "cg_download_channels: NULL argument");
+    CG_CHECK(cudaMemcpyAsync(out, s->state[s->cur], sizeof(float) * s->C * s->px(),
+                             cudaMemcpyDeviceToHost, s->stream),
+             "downloading channels");
+    CG_CHECK(cudaStreamSynchronize(s->stream), "cudaStreamSynchronize");
+    return CG_OK;
+}
+
+int cg_download_conv_real(cg_sim* s, float* out) {
+    if (!s || !out) return fail(CG_ERR_ARG, "cg_download_conv_real: NULL argument");
+    float* dbg = nullptr;
+    CG_CHECK(cudaMallocAsync(reinterpret_cast<void**>(&dbg), sizeof(float) * s->K * s->px(), s->stream),
+             "cudaMallocAsync(conv)");
+    cudaError_t e = s->ops->step(s->args(s->cur, dbg), kPhaseRowFwd | kPhaseColConv | kPhaseGrowth,
+                                 s->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(out, dbg, sizeof(float) * s->K * s->px(), cudaMemcpyDeviceToHost,
+                            s->stream);
+    cudaFreeAsync(dbg, s->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "computing the convolution buffer");
+    return CG_OK;
+}
+
+int cg_download_affinity(cg_sim* s, float* out) {
+    if (!s || !out) return fail(CG_ERR_ARG, "cg_download_affinity: NULL argument");
+    CG_CHECK(s->ops->step(s->args(s->cur, nullptr), kPhaseRowFwd | kPhaseColConv | kPhaseGrowth,
+                          s->stream),
+             "computing the affinity");
+    CG_CHECK(cudaMemcpyAsync(out, s->A, sizeof(float) * s->C * s->px(), cudaMemcpyDeviceToHost,
+                             s->stream),
+             "downloading the affinity");
+    CG_CHECK(cudaStreamSynchronize(s->stream), "cudaStreamSynchronize");
+    return CG_OK;
+}
+
+int cg_timed_iterate(cg_sim* s, double ms[4]) {
+    if (!s || !ms) return fail(CG_ERR_ARG, "cg_timed_iterate: NULL argument");
+    const StepArgs a = s->args(s->cur, nullptr);
+    const int phases[3] = {kPhaseRowFwd | kPhaseColConv, kPhaseGrowth, kPhaseDiffusion};
+    CG_CHECK(cudaEventRecord(s->ev[0], s->stream), "cudaEventRecord");
+    for (int p = 0; p < 3; ++p) {
+        CG_CHECK(s->ops->step(a, phases[p], s->stream), "launching a phase");
+        CG_CHECK(cudaEventRecord(s->ev[p + 1], s->stream), "cudaEventRecord");
+    }
+    CG_CHECK(cudaEventSynchronize(s->ev[3]), "cudaEventSynchronize");
+    for (int p = 0; p < 3; ++p) {
+        float t = 0.f;
+        CG_CHECK(cudaEventElapsedTime(&t, s->ev[p], s->ev[p + 1]), "cudaEventElapsedTime");
+        ms[p] = t;
+    }
+    ms[3] = 0.0;
+    s->cur ^= 1;
+    return CG_OK;
+}
+
+int cg_profile_kernels(cg_sim* s, int nsteps, double ms[4]) {
+    if (!s || !ms) return fail(CG_ERR_ARG, "cg_profile_kernels: NULL argument");
+    if (nsteps < 1 || nsteps > 1024)
+        return fail(CG_ERR_ARG, "cg_profile_kernels: nsteps %d outside [1, 1024]", nsteps);
+    const int phases[4] = {kPhaseRowFwd, kPhaseColConv, kPhaseGrowth, kPhaseDiffusion};
+    std::vector<cudaEvent_t> ev(size_t(nsteps) * 5, nullptr);
+    int rc = CG_OK;
+    for (auto& e : ev) {
+        cudaError_t ce = cudaEventCreate(&e);
+        if (ce != cudaSuccess) {
+            rc = cuda_fail(ce, "cudaEventCreate");
+            break;
+        }
+    }
+    for (int i = 0; i < nsteps && rc == CG_OK; ++i) {
+        const StepArgs a = s->args(s->cur, nullptr);
+        cudaError_t ce = cudaEventRecord(ev[i * 5], s->stream);
+        for (int p = 0; p < 4 && ce == cudaSuccess; ++p) {
+            ce = s->ops->step(a, phases[p], s->stream);
+            if (ce == cudaSuccess) ce = cudaEventRecord(ev[i * 5 + p + 1], s->stream);
+        }
+        if (ce != cudaSuccess) rc = cuda_fail(ce, "profiling a step");
+        s->cur ^= 1;
+    }
+    if (rc == CG_OK) {
+        cudaError_t ce = cudaEventSynchronize(ev.back());
+        if (ce != cudaSuccess) rc = cuda_fail(ce, "cudaEventSynchronize");
+    }
+    double acc[4] = {0, 0, 0, 0};
+    for (int i = 0; i < nsteps && rc == CG_OK; ++i)
+        for (int p = 0; p < 4; ++p) {
+            float t = 0.f;
+            cudaError_t ce = cudaEventElapsedTime(&t, ev[i * 5 + p], ev[i * 5 + p + 1]);
+            if (ce != cudaSuccess) {
+                rc = cuda_fail(ce, "cudaEventElapsedTime");
+                break;
+            }
+            acc[p] += t;
+        }
+    for (auto& e : ev)
+        if (e) cudaEventDestroy(e);
+    if (rc == CG_OK)
+        for (int p = 0; p < 4; ++p) ms[p] = acc[p] / nsteps;
+    return rc;
+}
+
+int cg_mass_f64(cg_sim* s, double* out) {
+    if (!s || !out) return fail(CG_ERR_ARG, "cg_mass_f64: NULL argument");
+    CG_CHECK(launch_mass_f64(s->state[s->cur], s->C, s->px(), s->mass_partial, kMassBlocks,
+                             s->mass_out, s->stream),
+             "mass reduction");
+    CG_CHECK(cudaMemcpyAsync(out, s->mass_out, sizeof(double) * s->C, cudaMemcpyDeviceToHost,
+                             s->stream),
+             "downloading masses");
+    CG_CHECK(cudaStreamSynchronize(s->stream), "cudaStreamSynchronize");
+    return CG_OK;
+}
+
+int cg_channel_ptr(cg_sim* s, float** p) {
+    if (!s || !p) return fail(CG_ERR_ARG, "cg_channel_ptr: NULL argument");
+    *p = s->state[s->cur];
+    return CG_OK;
+}
+
+int cg_stream(cg_sim* s, cg_stream_t* out) {
+    if (!s || !out) return fail(CG_ERR_ARG, "cg_stream: NULL argument");
+    *out = s->stream;
+    return CG_OK;
+}
+
+int cg_synchronize(cg_sim* s) {
+    if (!s) return fail(CG_ERR_ARG, "cg_synchronize: NULL handle");
+    CG_CHECK(cudaStreamSynchronize(s->stream), "cudaStreamSynchronize");
+    return CG_OK;
+}
+
+}  // extern "C"

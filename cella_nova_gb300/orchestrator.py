@@ -1,0 +1,236 @@
+"""GpuMaceLenia — the reference orchestrator's API over the C ABI.
+
+Mirrors ml-rs/orchestrator/mod.rs (method names, argument meaning and
+order, panics turned into :class:`CellaError`) so that the reference's own
+drivers (main.rs:88-140, profile.rs:32-108, save_pngs.rs:112-135) read the
+same against this class.  Every method is one libcella_gpu call; the step
+runs on the GPU as captured CUDA graphs.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _abi
+from ._abi import check, dptr, fptr, uptr
+
+
+class GpuMaceLenia:
+    """One DiffusionLenia world on the current CUDA device.
+
+    ``GpuMaceLenia(shape, num_channels, num_kernels, c0, c1, mu, sigma,
+    weights, temp)`` follows ``GpuMaceLenia::new`` (mod.rs:79-90):
+    ``shape`` is ``(n, n)``, ``c0[k]`` the channel kernel k reads and
+    ``c1[k]`` the channel its growth feeds.
+    """
+
+    def __init__(self, shape, num_channels, num_kernels, c0, c1, mu, sigma, weights,
+                 temp=1.0, stream=None):
+        shape = tuple(int(s) for s in shape)
+        if len(shape) != 2:
+            raise ValueError("DiffusionLenia requires 2D grids")          # mod.rs:94
+        if shape[0] != shape[1]:
+            raise ValueError("only square grids are supported")          # growth.rs:44
+        self._lib = _abi.load()
+        self.n = shape[0]
+        self.shape = shape
+        self.num_channels = int(num_channels)
+        self.num_kernels = int(num_kernels)
+        self.total_elements = self.n * self.n
+        K = self.num_kernels
+        self.c0 = np.ascontiguousarray(c0, dtype=np.uint32)
+        self.c1 = np.ascontiguousarray(c1, dtype=np.uint32)
+        self.mu = np.ascontiguousarray(mu, dtype=np.float32)
+        self.sigma = np.ascontiguousarray(sigma, dtype=np.float32)
+        self.weights = np.ascontiguousarray(weights, dtype=np.float32)
+        self.temp = float(temp)
+        for name in ("c0", "c1", "mu", "sigma", "weights"):
+            if getattr(self, name).shape != (K,):
+                raise ValueError(f"{name} must have num_kernels = {K} entries")
+        h = ctypes.c_void_p()
+        check(self._lib.cg_create(self.n, self.num_channels, K, uptr(self.c0), uptr(self.c1),
+                                  fptr(self.mu), fptr(self.sigma), fptr(self.weights),
+                                  ctypes.c_float(self.temp),
+                                  ctypes.c_void_p(stream) if stream else None,
+                                  ctypes.byref(h)))
+        self._h = h
+
+    # -- lifetime --------------------------------------------------------
+    def close(self):
+        if getattr(self, "_h", None):
+            check(self._lib.cg_destroy(self._h))
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # -- uploads (mod.rs:207-226) -----------------------------------------
+    def set_kernel(self, kernel_fft, kernel_idx):
+        """Kernel ``kernel_idx``'s full n x n complex spectrum (mod.rs:207)."""
+        a = np.asarray(kernel_fft)
+        if a.size != self.total_elements:
+            raise ValueError(f"kernel spectrum has {a.size} values, expected "
+                             f"{self.total_elements}")                     # mod.rs:208
+        inter = np.empty((self.total_elements, 2), dtype=np.float32)
+        flat = a.reshape(-1)
+        if np.iscomplexobj(flat):
+            inter[:, 0] = flat.real
+            inter[:, 1] = flat.imag
+        else:
+            inter[:] = flat.reshape(-1, 2) if flat.size == 2 * self.total_elements else 0
+        check(self._lib.cg_set_kernel(self._h, int(kernel_idx), fptr(inter)))
+
+    def upload_channel(self, data, channel):
+        """Channel ``channel`` from n*n f64 values (mod.rs:217-226)."""
+        a = np.ascontiguousarray(data, dtype=np.float64).reshape(-1)
+        if a.size != self.total_elements:
+            raise ValueError(f"channel has {a.size} values, expected {self.total_elements}")
+        check(self._lib.cg_upload_channel(self._h, int(channel), dptr(a)))
+
+    def upload_channel_f32(self, data, channel):
+        a = np.ascontiguousarray(data, dtype=np.float32).reshape(-1)
+        if a.size != self.total_elements:
+            raise ValueError(f"channel has {a.size} values, expected {self.total_elements}")
+        check(self._lib.cg_upload_channel_f32(self._h, int(channel), fptr(a)))
+
+    # -- stepping (mod.rs:229-233, 348-466) ------------------------------
+    def iterate(self):
+        check(self._lib.cg_iterate(self._h))
+
+    def run_steps(self, n):
+        check(self._lib.cg_step(self._h, int(n)))
+
+    def iterate_on(self, stream):
+        """iterate_with_encoder (mod.rs:435): enqueue on a caller stream."""
+        check(self._lib.cg_iterate_on(self._h, ctypes.c_void_p(stream)))
+
+    def timed_iterate(self):
+        """[conv, growth, diffusion, copy] device ms for one step (mod.rs:469)."""
+        ms = np.zeros(4, dtype=np.float64)
+        check(self._lib.cg_timed_iterate(self._h, dptr(ms)))
+        return ms
+
+    def profile_kernels(self, nsteps):
+        """Average device ms per kernel over nsteps steps: [row FFT, column
+        convolution, inverse row FFT + growth, diffusion]."""
+        ms = np.zeros(4, dtype=np.float64)
+        check(self._lib.cg_profile_kernels(self._h, int(nsteps), dptr(ms)))
+        return ms
+
+    def synchronize(self):
+        check(self._lib.cg_synchronize(self._h))
+
+    # -- downloads (mod.rs:236-299) --------------------------------------
+    def download_all_channels(self):
+        out = np.empty(self.num_channels * self.total_elements, dtype=np.float32)
+        check(self._lib.cg_download_channels(self._h, fptr(out)))
+        return out
+
+    def download_conv_buffer(self):
+        """Real part of every kernel's convolution before the 1/n^2 scale."""
+        out = np.empty(self.num_kernels * self.total_elements, dtype=np.float32)
+        check(self._lib.cg_download_conv_real(self._h, fptr(out)))
+        return out
+
+    def download_affinity(self):
+        out = np.empty(self.num_channels * self.total_elements, dtype=np.float32)
+        check(self._lib.cg_download_affinity(self._h, fptr(out)))
+        return out
+
+    def mass_f64(self):
+        out = np.zeros(self.num_channels, dtype=np.float64)
+        check(self._lib.cg_mass_f64(self._h, dptr(out)))
+        return out
+
+    def channel_ptr(self) -> int:
+        """Device address of the current state (channel_buffer, mod.rs:202)."""
+        p = ctypes.c_void_p()
+        check(self._lib.cg_channel_ptr(self._h, ctypes.byref(p)))
+        return p.value
+
+    def stream(self) -> int:
+        p = ctypes.c_void_p()
+        check(self._lib.cg_stream(self._h, ctypes.byref(p)))
+        return p.value or 0
+
+    # -- convenience -----------------------------------------------------
+    def upload_state(self, state):
+        state = np.asarray(state)
+        for c in range(self.num_channels):
+            if state.dtype == np.float32:
+                self.upload_channel_f32(state[c], c)
+            else:
+                self.upload_channel(state[c], c)
+
+    def state(self):
+        return self.download_all_channels().reshape(self.num_channels, self.n, self.n)
+
+    @classmethod
+    def from_creature(cls, cr, stream=None):
+        sim = cls((cr.n, cr.n), cr.C, cr.K, cr.c0, cr.c1, cr.mu, cr.sigma, cr.weights,
+                  cr.temp, stream=stream)
+        for k in range(cr.K):
+            sim.set_kernel(cr.kspec[k], k)
+        sim.upload_state(cr.seed)
+        return sim
+
+
+# ---------------------------------------------------------------------------
+# File formats (ml-rs/config.rs) through the C ABI
+# ---------------------------------------------------------------------------
+
+def load_config(path):
+    """load_config (config.rs:32-47) -> dict in orchestrator order (c0 = input)."""
+    lib = _abi.load()
+    cfg = _abi.cg_config()
+    check(lib.cg_load_config_json(str(path).encode(), ctypes.byref(cfg)))
+    try:
+        n, C, K = cfg.seed_size, cfg.num_channels, cfg.num_kernels
+        seed = np.ctypeslib.as_array(cfg.seed_channels, shape=(C * n * n,)).copy()
+        out = {
+            "seed_size": n, "num_channels": C, "num_kernels": K,
+            "seed_channels": seed.reshape(C, n * n),
+            "c0": np.ctypeslib.as_array(cfg.c0, shape=(K,)).copy(),
+            "c1": np.ctypeslib.as_array(cfg.c1, shape=(K,)).copy(),
+            "growth_mu": np.ctypeslib.as_array(cfg.growth_mu, shape=(K,)).copy(),
+            "growth_sigma": np.ctypeslib.as_array(cfg.growth_sigma, shape=(K,)).copy(),
+            "growth_weights": np.ctypeslib.as_array(cfg.growth_weights, shape=(K,)).copy(),
+            "temp": float(cfg.temp),
+        }
+    finally:
+        lib.cg_free_config(ctypes.byref(cfg))
+    return out
+
+
+def load_kernels(path, num_kernels, target_size):
+    """load_kernels (config.rs:56-125) -> (K, n, n) complex64."""
+    lib = _abi.load()
+    out = np.empty((num_kernels, target_size, target_size, 2), dtype=np.float32)
+    check(lib.cg_load_kernels_bin(str(path).encode(), int(num_kernels), int(target_size),
+                                  fptr(out)))
+    return out[..., 0] + 1j * out[..., 1]
+
+
+def setup_simulation(config_path, kernels_path, temp=None, stream=None):
+    """main.rs:88-140 / profile.rs:32-89: config + kernels -> ready world."""
+    cfg = load_config(config_path)
+    n = cfg["seed_size"]
+    sim = GpuMaceLenia((n, n), cfg["num_channels"], cfg["num_kernels"], cfg["c0"], cfg["c1"],
+                       cfg["growth_mu"], cfg["growth_sigma"], cfg["growth_weights"],
+                       cfg["temp"] if temp is None else temp, stream=stream)
+    for c in range(cfg["num_channels"]):
+        sim.upload_channel(cfg["seed_channels"][c], c)
+    ks = load_kernels(kernels_path, cfg["num_kernels"], n)
+    for k in range(cfg["num_kernels"]):
+        sim.set_kernel(ks[k], k)
+    return sim

@@ -1,0 +1,170 @@
+/*
+ * cella_gpu.h — C ABI of the GB300 (sm_103a) DiffusionLenia step.
+ *
+ * Drop-in for the `GpuMaceLenia` orchestrator of anima-zetta/cella-nova
+ * (ml-rs/orchestrator/mod.rs:45-541) and its file loaders (ml-rs/config.rs).
+ * Every entry point takes plain pointers and sizes; none takes a torch or
+ * wgpu type.  The Rust binding a maintainer adds in place of the wgpu path is
+ * shown in INTEGRATION.md.
+ *
+ * Conventions
+ *   - Every function returns CG_OK (0) or a negative cg_status.  The reason
+ *     for the last failure on the calling thread is cg_last_error().  The
+ *     reference panics instead (mod.rs:34, :94, :208, :218; config.rs:33-34).
+ *   - c0[k] is the channel kernel k reads, c1[k] the channel its growth term
+ *     feeds: the orchestrator's order (mod.rs:52-54), i.e. AFTER the swap
+ *     config.rs:40 applies to the JSON fields.  cg_load_config_json applies
+ *     that swap.
+ *   - The library owns its device buffers; callers own their host arrays,
+ *     which are copied.  A handle is not thread-safe; distinct handles are.
+ *   - Work is enqueued on the handle's CUDA stream (its own, or the one given
+ *     to cg_create) and is asynchronous, like wgpu's queue.submit (mod.rs:385);
+ *     downloads block, like map_async + poll(Wait) (mod.rs:255-257).
+ *   - Grid sides are powers of two from 64 to 2048 (the reference accepts
+ *     only 1024 and 2048, mod.rs:30-39); C <= 16 (compute_1024.wgsl:307);
+ *     K <= 64.
+ */
+#ifndef CELLA_GPU_H
+#define CELLA_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    CG_OK = 0,
+    CG_ERR_ARG = -1,         /* bad argument (sizes, indices, NaN parameter) */
+    CG_ERR_OOM = -2,         /* device or host allocation failed */
+    CG_ERR_CUDA = -3,        /* a CUDA runtime call failed */
+    CG_ERR_TIMEOUT = -4,     /* a bounded device wait gave up */
+    CG_ERR_IO = -5,          /* file could not be read or written */
+    CG_ERR_FORMAT = -6,      /* file contents do not match the format */
+    CG_ERR_UNSUPPORTED = -7  /* valid request this build does not serve */
+} cg_status;
+
+typedef struct cg_sim cg_sim;
+typedef void* cg_stream_t; /* a cudaStream_t; NULL = the library's own stream */
+
+/* Message of the last failure on this thread ("" if none). */
+const char* cg_last_error(void);
+
+/* Library version string. */
+const char* cg_version(void);
+
+/* ---------------------------------------------------------------------------
+ * Orchestrator (ml-rs/orchestrator/mod.rs)
+ * ------------------------------------------------------------------------- */
+
+/* GpuMaceLenia::new, mod.rs:79-198.  n: grid side; C channels; K kernels;
+ * c0/c1/mu/sigma/weights: K entries each; temp multiplies the growth sum
+ * inside exp (diffusion.rs:58-66).  Kernels start at zero and channels at
+ * zero until set_kernel / upload_channel.  stream may be NULL. */
+int cg_create(int n, int C, int K, const uint32_t* c0, const uint32_t* c1,
+              const float* mu, const float* sigma, const float* weights,
+              float temp, cg_stream_t stream, cg_sim** out);
+
+/* Drop for GpuMaceLenia: frees every device buffer of the handle. */
+int cg_destroy(cg_sim* sim);
+
+/* GpuMaceLenia::set_kernel, mod.rs:207-214: kernel k's full n*n complex
+ * spectrum, interleaved (re, im) f32, row-major, origin at [0,0]. */
+int cg_set_kernel(cg_sim* sim, int k, const float* spec_interleaved);
+
+/* GpuMaceLenia::upload_channel, mod.rs:217-226: channel c from n*n doubles,
+ * rounded to f32 (mod.rs:220 casts with `as f32`, round-to-nearest). */
+int cg_upload_channel(cg_sim* sim, int c, const double* data);
+
+/* Same as cg_upload_channel from f32 host data (no reference counterpart;
+ * used to re-upload a state that was downloaded). */
+int cg_upload_channel_f32(cg_sim* sim, int c, const float* data);
+
+/* GpuMaceLenia::iterate, mod.rs:348-386: one step, enqueued. */
+int cg_iterate(cg_sim* sim);
+
+/* GpuMaceLenia::run_steps, mod.rs:229-233: nsteps steps, enqueued as CUDA
+ * graph launches. */
+int cg_step(cg_sim* sim, int nsteps);
+
+/* GpuMaceLenia::iterate_with_encoder, mod.rs:435-466: one step enqueued on
+ * the caller's stream instead of the handle's. */
+int cg_iterate_on(cg_sim* sim, cg_stream_t stream);
+
+/* GpuMaceLenia::download_all_channels, mod.rs:236-263: blocking copy of the
+ * C*n*n f32 state, channel-major. */
+int cg_download_channels(cg_sim* sim, float* out);
+
+/* GpuMaceLenia::download_conv_buffer, mod.rs:267-299 (debug): K*n*n f32, the
+ * real part of each kernel's convolution before the 1/n^2 scale
+ * (growth.rs:87), for the CURRENT state (it runs the convolution again and
+ * does not advance the state). */
+int cg_download_conv_real(cg_sim* sim, float* out);
+
+/* Affinity A = exp(temp * sum_k w_k G(u_k)) of the current state, C*n*n f32
+ * (the reference keeps the pre-exp sum in ml::affinity, mod.rs:112; this
+ * build stores the exponential, which is what diffusion reads). */
+int cg_download_affinity(cg_sim* sim, float* out);
+
+/* GpuMaceLenia::timed_iterate, mod.rs:469-540: one step with per-phase
+ * device times in ms: [0] convolution, [1] growth, [2] diffusion, [3] buffer
+ * copy (always 0: the state is ping-ponged, no copy exists). */
+int cg_timed_iterate(cg_sim* sim, double ms[4]);
+
+/* Per-kernel device time, averaged over nsteps steps (1..1024) launched
+ * one kernel at a time with CUDA events between them (no reference
+ * counterpart; a finer split of timed_iterate, mod.rs:469-540).  Advances
+ * the state by nsteps.  ms[0] row FFT, [1] column convolution, [2] inverse
+ * row FFT + growth, [3] diffusion. */
+int cg_profile_kernels(cg_sim* sim, int nsteps, double ms[4]);
+
+/* Per-channel total mass of the current state, summed in FP64 on the GPU
+ * (no reference counterpart: example.rs:547-553 sums in f32 on the CPU).
+ * Blocking; out has C entries. */
+int cg_mass_f64(cg_sim* sim, double* out);
+
+/* GpuMaceLenia::channel_buffer, mod.rs:202-204: device pointer to the
+ * current C*n*n f32 state (valid until the next step or destroy). */
+int cg_channel_ptr(cg_sim* sim, float** dev_ptr);
+
+/* The handle's stream (the one work is enqueued on). */
+int cg_stream(cg_sim* sim, cg_stream_t* out);
+
+/* Device-side synchronisation of the handle's stream. */
+int cg_synchronize(cg_sim* sim);
+
+/* ---------------------------------------------------------------------------
+ * File formats (ml-rs/config.rs)
+ * ------------------------------------------------------------------------- */
+
+/* Parsed seed/{name}.json (config.rs:14-25).  c0/c1 are in orchestrator
+ * order: the loader swaps the JSON fields as config.rs:40 does. */
+typedef struct {
+    int seed_size, num_channels, num_kernels;
+    double* seed_channels;   /* C * n * n, channel-major */
+    uint32_t* c0;            /* K: input channel (JSON "c1") */
+    uint32_t* c1;            /* K: output channel (JSON "c0") */
+    float* growth_mu;        /* K */
+    float* growth_sigma;     /* K */
+    float* growth_weights;   /* K */
+    float temp;              /* optional "temp" key; 1.0 when absent */
+} cg_config;
+
+/* load_config, config.rs:32-47. */
+int cg_load_config_json(const char* path, cg_config* out);
+void cg_free_config(cg_config* cfg);
+
+/* load_kernels, config.rs:56-125: K spectra resampled to target_n (spectral
+ * zero-padding when the file holds a smaller grid, config.rs:81-116).
+ * out: K * target_n * target_n * 2 floats, caller-allocated.  A file holding
+ * a LARGER grid than target_n is rejected (the reference underflows). */
+int cg_load_kernels_bin(const char* path, int K, int target_n, float* out);
+
+/* Size of the grid stored in a kernels .bin (config.rs:61-65). */
+int cg_kernels_bin_size(const char* path, int K, int* src_n);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CELLA_GPU_H */

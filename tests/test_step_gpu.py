@@ -1,0 +1,175 @@
+"""Parity of the CUDA step against the FP64 oracle, through the C ABI.
+
+Every comparison is teacher-forced: the GPU and the oracle start each step
+from the same state (the GPU's f32 state, widened to f64 for the oracle), so
+the difference measures one step's error, which the bar puts at max-abs
+1e-5 (the dynamics are chaotic, so whole trajectories are compared only
+through size-independent properties such as mass).
+"""
+import os
+
+import numpy as np
+import pytest
+
+from cella_nova_gb300 import GpuMaceLenia, setup_simulation
+from cella_nova_gb300.creature import all_pairs, make_creature, write_creature
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+STEP_TOL = 1e-5          # max-abs per step against FP64
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def oracle_step(state, cr, want_u=False, want_aff=False):
+    fn = O.step_c if cr.n <= 256 else O.step_np
+    return fn(state.astype(np.float64), cr.kspec.astype(np.complex128), cr.c0, cr.c1,
+              cr.mu.astype(np.float64), cr.sigma.astype(np.float64),
+              cr.weights.astype(np.float64), cr.temp, want_u=want_u, want_aff=want_aff)
+
+
+def check_steps(cr, steps=3, tol=STEP_TOL):
+    with GpuMaceLenia.from_creature(cr) as sim:
+        errs = []
+        for _ in range(steps):
+            x = sim.state()
+            sim.iterate()
+            got = sim.state()
+            ref, _, _ = oracle_step(x, cr)
+            errs.append(np.abs(got - ref).max())
+        assert max(errs) <= tol, errs
+        return errs
+
+
+@pytest.mark.parametrize("name", ["c1k1_n16", "c3k9_n32", "c2k4_n32", "c4k16_n64"])
+def test_golden_trajectory_from_reference_model(name):
+    """The GPU path against the reference's own PyTorch model (float64)."""
+    g = np.load(os.path.join(GOLDEN, f"{name}.npz"))
+    n, C = int(g["n"]), int(g["C"])
+    with GpuMaceLenia((n, n), C, int(g["K"]), g["c0"], g["c1"], g["mu"], g["sigma"],
+                      g["weights"].astype(np.float32), float(g["temp"])) as sim:
+        for k in range(int(g["K"])):
+            sim.set_kernel(g["kspec"][k], k)
+        sim.upload_state(g["seed"])
+        for t in range(g["states_f64"].shape[0]):
+            sim.iterate()
+            err = np.abs(sim.state() - g["states_f64"][t]).max()
+            # a few steps of free-running f32 against f64: same spread as the
+            # reference's own float32 run
+            ref32 = np.abs(g["states_f32"][t] - g["states_f64"][t]).max()
+            assert err <= max(4 * ref32, STEP_TOL), (t, err, ref32)
+
+
+@pytest.mark.parametrize("n,C,seed,temp", [
+    (16, 1, 1, 1.0), (32, 2, 2, 0.5), (64, 3, 3, 1.0), (64, 4, 4, 2.0),
+    (128, 3, 5, 1.0), (256, 3, 6, 1.3), (256, 1, 7, 0.8),
+])
+def test_step_parity_all_pairs(n, C, seed, temp):
+    cr = make_creature(n, C, seed=seed, temp=temp, radius=(max(2.0, n / 16), max(4.0, n / 6)),
+                       seed_box=n // 2)
+    check_steps(cr)
+
+
+@pytest.mark.parametrize("c0,c1", [
+    ([1, 0, 2, 1], [0, 1, 1, 2]),          # the reference's reverse slot copy mishandles this
+    ([2, 2, 2], [0, 0, 0]),                 # one input feeds one output three times
+    ([0], [2]),                             # channels 0 and 1 get no growth term
+    ([0, 1, 2, 0, 1, 2, 0, 1, 2, 2, 1], [0, 0, 0, 1, 1, 1, 2, 2, 2, 0, 1]),   # K != C^2
+])
+def test_step_parity_irregular_maps(c0, c1):
+    cr = make_creature(64, 3, seed=17, c0=c0, c1=c1, radius=(4, 12), seed_box=32)
+    check_steps(cr)
+
+
+def test_many_kernels_and_channels():
+    C = 8
+    c0 = np.repeat(np.arange(C), 5) % C
+    c1 = (np.arange(5 * C) * 3) % C
+    cr = make_creature(64, C, seed=21, c0=c0, c1=c1, radius=(3, 10), seed_box=32)
+    check_steps(cr, steps=2)
+
+
+def test_conv_buffer_and_affinity_match_oracle():
+    cr = make_creature(128, 3, seed=8, radius=(8, 20), seed_box=64)
+    with GpuMaceLenia.from_creature(cr) as sim:
+        x = sim.state()
+        conv = sim.download_conv_buffer().reshape(cr.K, 128, 128)
+        aff = sim.download_affinity().reshape(cr.C, 128, 128)
+        np.testing.assert_array_equal(sim.state(), x)      # debug reads do not step
+    _, u, A = oracle_step(x, cr, want_u=True, want_aff=True)
+    # download_conv_buffer is the unscaled IFFT (growth.rs:87 scales by 1/n^2)
+    assert np.abs(conv / (128 * 128) - u).max() < 1e-6
+    assert np.abs(aff - A).max() / np.abs(A).max() < 1e-5
+
+
+def test_graph_steps_equal_timed_and_stream_steps():
+    cr = make_creature(128, 3, seed=9, radius=(8, 20), seed_box=64)
+    with GpuMaceLenia.from_creature(cr) as a, GpuMaceLenia.from_creature(cr) as b, \
+            GpuMaceLenia.from_creature(cr) as c:
+        a.run_steps(4)
+        for _ in range(4):
+            ms = b.timed_iterate()
+            assert ms.shape == (4,) and ms[3] == 0.0 and (ms[:3] >= 0).all()
+        import torch
+        s = torch.cuda.Stream()
+        for _ in range(4):
+            c.iterate_on(s.cuda_stream)
+        s.synchronize()
+        np.testing.assert_array_equal(a.state(), b.state())
+        np.testing.assert_array_equal(a.state(), c.state())
+
+
+def test_mass_f64_matches_host_sum_and_is_conserved():
+    cr = make_creature(256, 3, seed=10, radius=(10, 30), seed_box=128)
+    with GpuMaceLenia.from_creature(cr) as sim:
+        m0 = sim.mass_f64()
+        np.testing.assert_allclose(m0, sim.state().astype(np.float64).sum(axis=(1, 2)),
+                                   rtol=1e-12)
+        sim.run_steps(200)
+        m1 = sim.mass_f64()
+        assert np.abs(m1 / m0 - 1).max() < 1e-6
+
+
+def test_reference_files_through_setup_simulation(tmp_path):
+    cr = make_creature(64, 3, seed=11, radius=(4, 12), seed_box=32, temp=1.5)
+    js, kb = write_creature(str(tmp_path), "crit", cr)
+    sim = setup_simulation(js, kb)
+    try:
+        assert abs(sim.temp - 1.5) < 1e-7
+        x = sim.state()
+        np.testing.assert_array_equal(x, cr.seed.astype(np.float32))
+        sim.iterate()
+        ref, _, _ = oracle_step(x, cr)
+        assert np.abs(sim.state() - ref).max() <= STEP_TOL
+    finally:
+        sim.close()
+
+
+@pytest.mark.parametrize("n", [1024, 2048])
+def test_full_size_step_parity(n):
+    """The benchmark configurations (3 channels, 9 kernels) at full size."""
+    cr = make_creature(n, 3, seed=100 + n, temp=1.0)
+    check_steps(cr, steps=1)
+
+
+def test_mass_drift_1000_steps_2048():
+    cr = make_creature(2048, 3, seed=2048, temp=1.0)
+    with GpuMaceLenia.from_creature(cr) as sim:
+        m0 = sim.mass_f64()
+        sim.run_steps(1000)
+        m1 = sim.mass_f64()
+        x = sim.state()
+    assert np.isfinite(x).all()
+    assert np.abs(m1 / m0 - 1).max() < 1e-6, m1 / m0 - 1
+
+
+def test_kernel_reupload_and_zero_kernel():
+    """set_kernel overwrites; an all-zero spectrum gives u = 0 everywhere."""
+    cr = make_creature(64, 2, seed=12, radius=(4, 10), seed_box=32)
+    with GpuMaceLenia.from_creature(cr) as sim:
+        sim.set_kernel(np.zeros((64, 64), np.complex64), 0)
+        conv = sim.download_conv_buffer().reshape(cr.K, 64, 64)
+        assert np.abs(conv[0]).max() == 0.0
+        sim.set_kernel(cr.kspec[0], 0)
+        conv = sim.download_conv_buffer().reshape(cr.K, 64, 64)
+        assert np.abs(conv[0]).max() > 0.0
