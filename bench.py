@@ -254,25 +254,9 @@ def run_ours(args):
     # end to end through the public API with host buffers: per step, upload
     # the state (f64, as upload_channel takes it) from pinned memory, step,
     # download the f32 state
-    host_in = torch.empty((C_CH, px), dtype=torch.float64, pin_memory=True).numpy()
-    host_out = torch.empty((C_CH * px,), dtype=torch.float32, pin_memory=True).numpy()
-    host_in[:] = cr.seed.reshape(C_CH, px)
-    from cella_nova_gb300 import _abi
-    lib = sim._lib
-    e2e_steps = max(3, min(args.steps, 50))
-    for _ in range(2):
-        for c in range(C_CH):
-            _abi.check(lib.cg_upload_channel(sim._h, c, _abi.dptr(host_in[c])))
-        _abi.check(lib.cg_iterate(sim._h))
-        _abi.check(lib.cg_download_channels(sim._h, _abi.fptr(host_out)))
-    barrier(dist, world)
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        for c in range(C_CH):
-            _abi.check(lib.cg_upload_channel(sim._h, c, _abi.dptr(host_in[c])))
-        _abi.check(lib.cg_iterate(sim._h))
-        _abi.check(lib.cg_download_channels(sim._h, _abi.fptr(host_out)))
-    e2e_s = max_over_ranks(time.perf_counter() - t0, dist, world)
+    e2e = None
+    if not args.no_e2e:
+        e2e = e2e_run(sim, cr, args, dist, world)
     sampler.stop()
 
     cpu = None
@@ -302,8 +286,7 @@ def run_ours(args):
                      "frac": bpp * px / step_s / 1e9 / peak, "peak_source": peak_kind},
         "kernel_ms": {"row_r2c": kms[0], "col_conv": kms[1], "row_c2r_growth": kms[2],
                       "diffusion": kms[3]},
-        "e2e": {"value": world * px * e2e_steps / e2e_s, "unit": UNIT,
-                "h2d_bytes_per_step": C_CH * px * 8, "d2h_bytes_per_step": C_CH * px * 4},
+        "e2e": e2e,
         "gpu_launches": 4 * args.steps,
         "clocks": clocks,
     }
@@ -317,6 +300,36 @@ def run_ours(args):
     return 0
 
 
+def e2e_run(sim, cr, args, dist, world):
+    """Per step through the public C ABI with host buffers: upload the state
+    (f64, as upload_channel takes it) from pinned memory, one step, download
+    the f32 state (a blocking copy)."""
+    import torch
+    from cella_nova_gb300 import _abi
+    px = cr.n * cr.n
+    host_in = torch.empty((C_CH, px), dtype=torch.float64, pin_memory=True).numpy()
+    host_out = torch.empty((C_CH * px,), dtype=torch.float32, pin_memory=True).numpy()
+    host_in[:] = cr.seed.reshape(C_CH, px)
+    from cella_nova_gb300 import _abi
+    lib = sim._lib
+    e2e_steps = max(3, min(args.steps, 50))
+    for _ in range(2):
+        for c in range(C_CH):
+            _abi.check(lib.cg_upload_channel(sim._h, c, _abi.dptr(host_in[c])))
+        _abi.check(lib.cg_iterate(sim._h))
+        _abi.check(lib.cg_download_channels(sim._h, _abi.fptr(host_out)))
+    barrier(dist, world)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        for c in range(C_CH):
+            _abi.check(lib.cg_upload_channel(sim._h, c, _abi.dptr(host_in[c])))
+        _abi.check(lib.cg_iterate(sim._h))
+        _abi.check(lib.cg_download_channels(sim._h, _abi.fptr(host_out)))
+    e2e_s = max_over_ranks(time.perf_counter() - t0, dist, world)
+    return {"value": world * px * e2e_steps / e2e_s, "unit": UNIT,
+            "h2d_bytes_per_step": C_CH * px * 8, "d2h_bytes_per_step": C_CH * px * 4}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -324,6 +337,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

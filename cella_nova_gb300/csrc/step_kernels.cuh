@@ -272,12 +272,29 @@ __global__ void __launch_bounds__(256) k_diffusion(const float* __restrict__ A,
     __syncthreads();
     for (int i = threadIdx.x; i < QH * QW; i += blockDim.x) {
         const int r = i / QW, q = i % QW;
-        float z = 0.f;
+        // Z as an unevaluated float pair (zh + zl): TwoSum keeps every
+        // rounding error, so zh + zl is the 3x3 sum to ~1e-14.  A plain f32
+        // sum is off by a fixed relative amount wherever A is constant
+        // (G = -1 for every kernel across a whole region), which drifts the
+        // total mass by ~1e-8 per step; with the exact Z the only errors
+        // left are the unbiased roundings of q, the sum of q and the product.
+        float zh = sA[r][q], zl = 0.f;
 #pragma unroll
-        for (int di = 0; di < 3; ++di)
-#pragma unroll
-            for (int dj = 0; dj < 3; ++dj) z += sA[r + di][q + dj];
-        sQ[r][q] = sQ[r][q] / z;
+        for (int t = 1; t < 9; ++t) {
+            const float b = sA[r + t / 3][q + t % 3];
+            const float s = zh + b;
+            const float bb = s - zh;
+            zl += (zh - (s - bb)) + (b - bb);
+            zh = s;
+        }
+        const float z = zh + zl;
+        zl = zl - (z - zh);
+        zh = z;
+        // q = x / (zh + zl), from the exact remainder of x / zh
+        const float xv = sQ[r][q];
+        const float q0 = xv / zh;
+        const float rem = fmaf(-q0, zh, xv);
+        sQ[r][q] = q0 + (rem - q0 * zl) / zh;
     }
     __syncthreads();
     float* oc = out + size_t(c) * N * N;
