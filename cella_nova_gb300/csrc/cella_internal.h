@@ -46,6 +46,7 @@ struct StepArgs {
     float* A;
     const float2* tw;
     float* udbg;   // optional [K][n][n] f32: Re(conv) before the 1/n^2 scale
+    int* err;      // device error word (bounded waits that timed out)
     KernelGroups groups;
     GrowthParams gp;
 };

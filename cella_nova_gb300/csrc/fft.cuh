@@ -88,10 +88,19 @@ struct Dft<1, INV> {
     __device__ __forceinline__ static void run(float2*) {}
 };
 
-// Radix of the pass that starts at sub-transform size NS.
-template <int L, int NS>
+// Radix of the pass that starts at sub-transform size NS.  Greedy plans use
+// radix 16 until fewer than 16 remain (16,16,...,rem); REMFIRST plans put
+// the remainder first (rem,16,16,...), so the first pass of a REMFIRST
+// inverse sees exactly the index sets the last pass of a greedy forward
+// transform left in each thread's registers.
+__host__ __device__ constexpr int rem_radix(int L) {
+    int b = 0;
+    while ((1 << b) < L) ++b;
+    return (b % 4) == 0 ? (L >= 16 ? 16 : L) : (1 << (b % 4));
+}
+template <int L, int NS, bool REMFIRST = false>
 struct PassRadix {
-    static constexpr int R = (L / NS >= 16) ? 16 : (L / NS);
+    static constexpr int R = (REMFIRST && NS == 1) ? rem_radix(L) : ((L / NS >= 16) ? 16 : (L / NS));
 };
 
 // Radix of the last pass of a length-L transform.
@@ -111,8 +120,8 @@ __host__ __device__ constexpr int last_radix(int L) {
 // (j div NS)*NS*R + (j mod NS) + q*NS.  All loads finish (barrier) before any
 // store, so in-place passes are safe; a second barrier closes the pass.
 //   twN : W_N^m = exp(-2*pi*i*m/N), m in [0, N); TWS = N / L.
-//   ld(s, i)                -> float2
-//   st(s, i, v, it, q)      (it, q) name the register slot that held v.
+//   ld(s, i, it, q)         -> float2
+//   st(s, i, v, it, q)      (it, q) name the register slot of the value.
 template <int L, int R, int NS, bool INV, int T, int S, int TWS, class LD, class ST>
 __device__ __forceinline__ void stockham_pass(LD& ld, ST& st, const float2* __restrict__ twN) {
     constexpr int J = L / R;
@@ -125,7 +134,7 @@ __device__ __forceinline__ void stockham_pass(LD& ld, ST& st, const float2* __re
         if (ITEMS % T == 0 || item < ITEMS) {
             const int s = item / J, j = item % J;
 #pragma unroll
-            for (int r = 0; r < R; ++r) v[it][r] = ld(s, j + r * J);
+            for (int r = 0; r < R; ++r) v[it][r] = ld(s, j + r * J, it, r);
         }
     }
     __syncthreads();
@@ -154,17 +163,17 @@ __device__ __forceinline__ void stockham_pass(LD& ld, ST& st, const float2* __re
 
 // Full length-L transform: first pass reads through `ld`, middle passes use
 // shared memory through smld/smst, the last pass writes through `stl`.
-template <int L, int NS, bool INV, int T, int S, int TWS>
+template <int L, int NS, bool INV, int T, int S, int TWS, bool REMFIRST = false>
 struct FftPasses {
     template <class LD, class SMLD, class SMST, class STL>
     __device__ __forceinline__ static void run(LD& ld, SMLD& smld, SMST& smst, STL& stl,
                                                const float2* __restrict__ twN) {
-        constexpr int R = PassRadix<L, NS>::R;
+        constexpr int R = PassRadix<L, NS, REMFIRST>::R;
         if constexpr (NS * R == L) {
             stockham_pass<L, R, NS, INV, T, S, TWS>(ld, stl, twN);
         } else {
             stockham_pass<L, R, NS, INV, T, S, TWS>(ld, smst, twN);
-            FftPasses<L, NS * R, INV, T, S, TWS>::run(smld, smld, smst, stl, twN);
+            FftPasses<L, NS * R, INV, T, S, TWS, false>::run(smld, smld, smst, stl, twN);
         }
     }
 };

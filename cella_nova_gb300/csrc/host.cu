@@ -86,6 +86,7 @@ struct cg_sim {
     void* staging = nullptr;
     double* mass_partial = nullptr;
     double* mass_out = nullptr;
+    int* err = nullptr;   // device error word written by bounded waits
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     KernelGroups groups{};
@@ -106,6 +107,7 @@ struct cg_sim {
         a.A = A;
         a.tw = tw;
         a.udbg = udbg;
+        a.err = err;
         a.groups = groups;
         a.gp = gp;
         return a;
@@ -131,6 +133,7 @@ void release(cg_sim* s) {
     cudaFree(s->staging);
     cudaFree(s->mass_partial);
     cudaFree(s->mass_out);
+    cudaFree(s->err);
     if (s->own_stream && s->stream) cudaStreamDestroy(s->stream);
     delete s;
 }
@@ -171,6 +174,24 @@ int build_twiddles(cg_sim* s) {
 }
 
 bool finite(float v) { return std::isfinite(v); }
+
+// After a synchronisation: report (and clear) a device-side wait timeout.
+int check_device_error(cg_sim* s) {
+    int h = 0;
+    CG_CHECK(cudaMemcpy(&h, s->err, sizeof(int), cudaMemcpyDeviceToHost), "reading error word");
+    if (h != 0) {
+        cudaMemset(s->err, 0, sizeof(int));
+        return fail(CG_ERR_TIMEOUT, "a device-side wait for an asynchronous copy timed out "
+                                    "(error word %d); the last steps are invalid", h);
+    }
+    return CG_OK;
+}
+
+#define CG_SYNC_CHECK(s)                               \
+    do {                                               \
+        int rc_ = check_device_error(s);               \
+        if (rc_ != CG_OK) return rc_;                  \
+    } while (0)
 
 }  // namespace
 
@@ -270,6 +291,8 @@ int cg_create(int n, int C, int K, const uint32_t* c0, const uint32_t* c1, const
     if (rc == CG_OK)
         chk(cudaMalloc(&s->mass_partial, sizeof(double) * C * kMassBlocks), "cudaMalloc(mass)");
     if (rc == CG_OK) chk(cudaMalloc(&s->mass_out, sizeof(double) * C), "cudaMalloc(mass)");
+    if (rc == CG_OK) chk(cudaMalloc(&s->err, sizeof(int)), "cudaMalloc(err)");
+    if (rc == CG_OK) chk(cudaMemset(s->err, 0, sizeof(int)), "memset(err)");
     for (int i = 0; i < 4 && rc == CG_OK; ++i) chk(cudaEventCreate(&s->ev[i]), "cudaEventCreate");
     if (rc == CG_OK) chk(cudaMemsetAsync(s->state[0], 0, sizeof(float) * C * px, s->stream), "memset");
     if (rc == CG_OK) chk(cudaMemsetAsync(s->state[1], 0, sizeof(float) * C * px, s->stream), "memset");
@@ -354,6 +377,7 @@ int cg_download_channels(cg_sim* s, float* out) {
                              cudaMemcpyDeviceToHost, s->stream),
              "downloading channels");
     CG_CHECK(cudaStreamSynchronize(s->stream), "cudaStreamSynchronize");
+    CG_SYNC_CHECK(s);
     return CG_OK;
 }
 
@@ -370,6 +394,7 @@ int cg_download_conv_real(cg_sim* s, float* out) {
     cudaFreeAsync(dbg, s->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
     if (e != cudaSuccess) return cuda_fail(e, "computing the convolution buffer");
+    CG_SYNC_CHECK(s);
     return CG_OK;
 }
 
@@ -382,6 +407,7 @@ int cg_download_affinity(cg_sim* s, float* out) {
                              s->stream),
              "downloading the affinity");
     CG_CHECK(cudaStreamSynchronize(s->stream), "cudaStreamSynchronize");
+    CG_SYNC_CHECK(s);
     return CG_OK;
 }
 
@@ -402,6 +428,7 @@ int cg_timed_iterate(cg_sim* s, double ms[4]) {
     }
     ms[3] = 0.0;
     s->cur ^= 1;
+    CG_SYNC_CHECK(s);
     return CG_OK;
 }
 
@@ -448,6 +475,7 @@ int cg_profile_kernels(cg_sim* s, int nsteps, double ms[4]) {
         if (e) cudaEventDestroy(e);
     if (rc == CG_OK)
         for (int p = 0; p < 4; ++p) ms[p] = acc[p] / nsteps;
+    if (rc == CG_OK) rc = check_device_error(s);
     return rc;
 }
 
@@ -460,6 +488,7 @@ int cg_mass_f64(cg_sim* s, double* out) {
                              s->stream),
              "downloading masses");
     CG_CHECK(cudaStreamSynchronize(s->stream), "cudaStreamSynchronize");
+    CG_SYNC_CHECK(s);
     return CG_OK;
 }
 
@@ -478,6 +507,7 @@ int cg_stream(cg_sim* s, cg_stream_t* out) {
 int cg_synchronize(cg_sim* s) {
     if (!s) return fail(CG_ERR_ARG, "cg_synchronize: NULL handle");
     CG_CHECK(cudaStreamSynchronize(s->stream), "cudaStreamSynchronize");
+    CG_SYNC_CHECK(s);
     return CG_OK;
 }
 

@@ -21,6 +21,7 @@
 // (real) packed into the imaginary part of X[0] (real).
 #pragma once
 #include "cella_internal.h"
+#include "async_copy.cuh"
 #include "fft.cuh"
 
 namespace cg {
@@ -29,17 +30,21 @@ template <int LOGN>
 struct Geo {
     static constexpr int N = 1 << LOGN;
     static constexpr int M = N / 2;
-    // Row kernels: RB rows per CTA, RT threads.
+    // Row kernels: RB rows per CTA, RT threads.  The row pitch RP keeps the
+    // kx-major transposes conflict-free: odd for RB >= 16 (a half-warp reads
+    // 16 rows of one column), 2 mod 16 for RB = 8 (8 rows x 2 columns).
     static constexpr int RB0 = 8192 / M;
     static constexpr int RB = RB0 < 8 ? 8 : (RB0 > N ? N : RB0);
     static constexpr int RT = 512;
-    static constexpr int RP = padded_len(M) + 1;   // odd pitch: conflict-free column reads
-    static constexpr size_t ROW_SMEM = size_t(RB) * RP * sizeof(float2);
-    // Column kernel: TW columns per CTA, CT threads, spectrum + work buffer.
+    static constexpr int RP = padded_len(M) + (RB >= 16 ? 1 : 2);
+    static constexpr size_t R2C_SMEM = size_t(RB) * RP * sizeof(float2);
+    static constexpr size_t C2R_SMEM = 2 * R2C_SMEM;    // double-buffered input
+    // Column kernel: TW columns per CTA, CT threads; a padded work buffer
+    // and an unpadded staging tile that bulk copies fill.
     static constexpr int TW = 2;
     static constexpr int CT = 256;
     static constexpr int CP = padded_len(N) + 1;
-    static constexpr size_t COL_SMEM = size_t(2 * TW) * CP * sizeof(float2);
+    static constexpr size_t COL_SMEM = (size_t(TW) * CP + size_t(TW) * N) * sizeof(float2);
     // Diffusion tile.
     static constexpr int TX = N < 64 ? N : 64;
     static constexpr int TY = N < 32 ? N : 32;
@@ -58,13 +63,13 @@ __global__ void __launch_bounds__(512) k_row_r2c(const float* __restrict__ state
                                                   float2* __restrict__ rowspec,
                                                   const float2* __restrict__ tw) {
     using G = Geo<LOGN>;
-    extern __shared__ float2 sm[];
+    extern __shared__ __align__(16) float2 sm[];
     const int c = blockIdx.y;
     const int y0 = blockIdx.x * G::RB;
     const float2* src =
         reinterpret_cast<const float2*>(state + (size_t(c) * G::N + y0) * G::N);
-    auto ld0 = [&](int s, int i) { return __ldg(&src[size_t(s) * G::M + i]); };
-    auto smld = [&](int s, int i) { return sm[s * G::RP + pidx(i)]; };
+    auto ld0 = [&](int s, int i, int, int) { return __ldg(&src[size_t(s) * G::M + i]); };
+    auto smld = [&](int s, int i, int, int) { return sm[s * G::RP + pidx(i)]; };
     auto smst = [&](int s, int i, float2 v, int, int) { sm[s * G::RP + pidx(i)] = v; };
     FftPasses<G::M, 1, false, G::RT, G::RB, 2>::run(ld0, smld, smst, smst, tw);
 
@@ -94,61 +99,144 @@ __global__ void __launch_bounds__(512) k_row_r2c(const float* __restrict__ state
     }
 }
 
-// ---------------------------------------------------------------------------
-// Column pass: for TW consecutive kx of input channel c, the forward column
-// FFT once, then for every kernel k with c0[k] == c the product with the
-// kernel's half spectrum and the inverse column FFT, written to U[k].
-// Column 0 carries two real-row spectra (kx = 0 and kx = n/2): with
-// P = FA + i FB its column FFT, the kernel products recombine as
-//   P(ky) alpha(ky) + conj P(-ky) beta(ky),
-// alpha/beta = (K(.,0) +- K(.,n/2))/2 (prepared by k_pack_kernel).
-// grid (M/TW, C), block CT.
-// ---------------------------------------------------------------------------
-template <int LOGN>
-__global__ void __launch_bounds__(256) k_col_conv(const float2* __restrict__ rowspec,
-                                                   const float2* __restrict__ kspec,
-                                                   float2* __restrict__ U,
-                                                   const float2* __restrict__ tw,
-                                                   const KernelGroups groups) {
-    using G = Geo<LOGN>;
-    const int c = blockIdx.y;
-    const int cnt = groups.in_count[c];
-    if (cnt == 0) return;
-    extern __shared__ float2 sm[];
-    float2* F = sm;
-    float2* W = sm + G::TW * G::CP;
-    const int kx0 = blockIdx.x * G::TW;
-
-    const float2* src = rowspec + (size_t(c) * G::M + kx0) * G::N;
-    auto ld0 = [&](int s, int i) { return __ldg(&src[size_t(s) * G::N + i]); };
-    auto fld = [&](int s, int i) { return F[s * G::CP + pidx(i)]; };
-    auto fst = [&](int s, int i, float2 v, int, int) { F[s * G::CP + pidx(i)] = v; };
-    FftPasses<G::N, 1, false, G::CT, G::TW, 1>::run(ld0, fld, fst, fst, tw);
-
-    auto wld = [&](int s, int i) { return W[s * G::CP + pidx(i)]; };
-    auto wst = [&](int s, int i, float2 v, int, int) { W[s * G::CP + pidx(i)] = v; };
-    const int base = groups.in_start[c];
-    for (int gi = 0; gi < cnt; ++gi) {
-        const int k = groups.in_idx[base + gi];
-        const float2* ks = kspec + (size_t(k) * (G::M + 1) + kx0) * G::N;
-        const float2* kb = kspec + (size_t(k) * (G::M + 1) + G::M) * G::N;
-        auto ldm = [&](int s, int i) {
-            const float2 p = F[s * G::CP + pidx(i)];
-            const float2 kv = __ldg(&ks[size_t(s) * G::N + i]);
-            if (kx0 + s == 0) {
-                const float2 pm = cconj(F[pidx((G::N - i) & (G::N - 1))]);
-                return cadd(cmul(p, kv), cmul(pm, __ldg(&kb[i])));
-            }
-            return cmul(p, kv);
-        };
-        float2* dst = U + (size_t(k) * G::M + kx0) * G::N;
-        auto gst = [&](int s, int i, float2 v, int, int) { dst[size_t(s) * G::N + i] = v; };
-        FftPasses<G::N, 1, true, G::CT, G::TW, 1>::run(ldm, wld, wst, gst, tw);
+// Run the first pass of a transform, then `hook()`, then the rest.
+template <int L, bool INV, int T, int S, int TWS, bool REMFIRST, class LD, class SMLD, class SMST,
+          class STL, class HOOK>
+__device__ __forceinline__ void fft_with_hook(LD& ld, SMLD& smld, SMST& smst, STL& stl,
+                                              const float2* __restrict__ twN, HOOK hook) {
+    constexpr int R = PassRadix<L, 1, REMFIRST>::R;
+    if constexpr (R == L) {
+        stockham_pass<L, R, 1, INV, T, S, TWS>(ld, stl, twN);
+        hook();
+    } else {
+        stockham_pass<L, R, 1, INV, T, S, TWS>(ld, smst, twN);
+        hook();
+        FftPasses<L, R, INV, T, S, TWS, false>::run(smld, smld, smst, stl, twN);
     }
 }
 
 // ---------------------------------------------------------------------------
-// Inverse row pass + growth: for every output channel c and every kernel k
+// Column pass: for TW consecutive kx of input channel c, the forward column
+// FFT once, then for every kernel k with c0[k] == c the product with the
+// kernel's half spectrum and the inverse column FFT, written to U[k].
+//
+// Data movement: the input columns and each kernel's spectrum columns are
+// contiguous (kx-major layouts), so each arrives by one 1-D bulk copy (TMA)
+// into the staging tile KS, tracked by an mbarrier; the next kernel's copy
+// is issued as soon as the current one has been consumed by the first
+// inverse pass, and lands while the remaining passes run.  The forward
+// spectrum never returns to shared memory: the forward plan ends with the
+// radix the inverse plan starts with, so each thread keeps exactly the
+// values its first inverse pass needs in registers (F).
+//
+// Column 0 carries two real-row spectra (kx = 0 and kx = n/2): with
+// P = FA + i FB its column FFT, the kernel products recombine as
+//   P(ky) alpha(ky) + conj P(-ky) beta(ky),
+// alpha/beta = (K(.,0) +- K(.,n/2))/2 (prepared by k_pack_kernel); P(-ky)
+// lives in another thread, so that tile swaps column 0 through W first.
+// grid (M/TW, C), block CT.
+// ---------------------------------------------------------------------------
+template <int LOGN>
+__global__ void __launch_bounds__(256, 2) k_col_conv(const float2* __restrict__ rowspec,
+                                                      const float2* __restrict__ kspec,
+                                                      float2* __restrict__ U,
+                                                      const float2* __restrict__ tw,
+                                                      const KernelGroups groups, int* err) {
+    using G = Geo<LOGN>;
+    constexpr int N = G::N, M = G::M, TW = G::TW, T = G::CT;
+    const int c = blockIdx.y;
+    const int cnt = groups.in_count[c];
+    if (cnt == 0) return;
+    extern __shared__ __align__(128) float2 sm[];
+    float2* W = sm;
+    float2* KS = sm + TW * G::CP;
+    __shared__ __align__(8) uint64_t bar;
+    const int kx0 = blockIdx.x * TW;
+    const int base = groups.in_start[c];
+    constexpr uint32_t kTileBytes = uint32_t(TW) * N * sizeof(float2);
+
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        fence_barrier_init();
+    }
+    __syncthreads();
+    uint32_t phase = 0;
+    auto issue = [&](const float2* src) {   // all threads call; thread 0 copies
+        fence_proxy_async_smem();
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            mbar_arrive_expect_tx(&bar, kTileBytes);
+            bulk_g2s(KS, src, kTileBytes, &bar);
+        }
+    };
+    auto wait_tile = [&]() -> bool {
+        const bool ok = mbar_wait(&bar, phase & 1, err);
+        if (__syncthreads_or(!ok)) {
+            // give the copy in flight one more bounded chance to land before
+            // this CTA's shared memory is released
+            mbar_wait(&bar, phase & 1, nullptr);
+            return false;
+        }
+        ++phase;
+        return true;
+    };
+    auto kernel_tile = [&](int gi) {
+        const int k = groups.in_idx[base + gi];
+        return kspec + (size_t(k) * (M + 1) + kx0) * N;
+    };
+
+    issue(rowspec + (size_t(c) * M + kx0) * N);
+    if (!wait_tile()) return;
+
+    constexpr int RL = last_radix(N);
+    static_assert(PassRadix<N, 1, true>::R == RL,
+                  "the inverse must start with the radix the forward ends with");
+    constexpr int JL = N / RL;
+    constexpr int IPTL = (TW * JL + T - 1) / T;
+    float2 F[IPTL][RL];
+    auto ld_in = [&](int s, int i, int, int) { return KS[s * N + i]; };
+    auto wld = [&](int s, int i, int, int) { return W[s * G::CP + pidx(i)]; };
+    auto wst = [&](int s, int i, float2 v, int, int) { W[s * G::CP + pidx(i)] = v; };
+    auto keep = [&](int, int, float2 v, int it, int r) { F[it][r] = v; };
+    fft_with_hook<N, false, T, TW, 1, false>(ld_in, wld, wst, keep, tw,
+                                            [&]() { issue(kernel_tile(0)); });
+
+    for (int gi = 0; gi < cnt; ++gi) {
+        if (!wait_tile()) return;
+        if (kx0 == 0) {   // publish column 0 for the conj P(-ky) reads
+#pragma unroll
+            for (int it = 0; it < IPTL; ++it) {
+                const int item = threadIdx.x + it * T;
+                if ((TW * JL) % T == 0 || item < TW * JL) {
+                    if (item / JL == 0) {
+#pragma unroll
+                        for (int r = 0; r < RL; ++r) W[pidx(item % JL + r * JL)] = F[it][r];
+                    }
+                }
+            }
+            __syncthreads();
+        }
+        const int k = groups.in_idx[base + gi];
+        const float2* kb = kspec + (size_t(k) * (M + 1) + M) * N;
+        auto ld_mul = [&](int s, int i, int it, int r) {
+            const float2 p = F[it][r];
+            const float2 kv = KS[s * N + i];
+            if (kx0 + s == 0) {
+                const float2 pm = cconj(W[pidx((N - i) & (N - 1))]);
+                return cadd(cmul(p, kv), cmul(pm, __ldg(&kb[i])));
+            }
+            return cmul(p, kv);
+        };
+        float2* dst = U + (size_t(k) * M + kx0) * N;
+        auto gst = [&](int s, int i, float2 v, int, int) { dst[size_t(s) * N + i] = v; };
+        fft_with_hook<N, true, T, TW, 1, true>(ld_mul, wld, wst, gst, tw, [&]() {
+            if (gi + 1 < cnt) issue(kernel_tile(gi + 1));
+        });
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Inverse row pass + growth, one output channel per CTA: for every kernel k
 // with c1[k] == c (in increasing k, as mcl_growth_main accumulates,
 // compute_1024.wgsl:313-320): C2R of the rows of U[k], then
 //   u = value (the 1/n^2 of growth.rs:87 is folded into kspec),
@@ -156,157 +244,179 @@ __global__ void __launch_bounds__(256) k_col_conv(const float2* __restrict__ row
 // then A[c] = exp(temp * acc) (diffusion.rs:58-66 applies temp inside exp).
 // C2R: Z[m] = E + i O, E = X[m] + conj X[M-m], O = (X[m] - conj X[M-m]) W_N^-m,
 // z = IFFT_M(Z) = (x[2j], x[2j+1]).
-// grid (N/RB), block RT.
+// The next kernel's U tile is gathered (a transpose, per-element cp.async)
+// into the second buffer while the current one is transformed.
+// grid (N/RB, C), block RT.
 // ---------------------------------------------------------------------------
 template <int LOGN>
 __global__ void __launch_bounds__(512) k_row_c2r_growth(const float2* __restrict__ U,
                                                          float* __restrict__ A,
                                                          const float2* __restrict__ tw,
                                                          const KernelGroups groups,
-                                                         const GrowthParams gp, int C,
-                                                         float temp, float* __restrict__ udbg,
+                                                         const GrowthParams gp, float temp,
+                                                         float* __restrict__ udbg,
                                                          float udbg_scale) {
     using G = Geo<LOGN>;
-    extern __shared__ float2 sm[];
+    extern __shared__ __align__(16) float2 sm[];
+    const int c = blockIdx.y;
     const int y0 = blockIdx.x * G::RB;
     constexpr int RL = last_radix(G::M);
     constexpr int JL = G::M / RL;
     constexpr int ITEMS = G::RB * JL;
     constexpr int IPT = (ITEMS + G::RT - 1) / G::RT;
+    constexpr int BUF = G::RB * G::RP;
+    const int cnt = groups.out_count[c], base = groups.out_start[c];
 
-    auto smld = [&](int s, int i) { return sm[s * G::RP + pidx(i)]; };
-    auto smst = [&](int s, int i, float2 v, int, int) { sm[s * G::RP + pidx(i)] = v; };
-    auto ld0 = [&](int s, int m) -> float2 {
-        const float2* row = sm + s * G::RP;
-        if (m == 0) {
-            const float2 x = row[0];
-            return make_float2(x.x + x.y, x.x - x.y);
+    auto gather = [&](int gi, float2* buf) {
+        const int k = groups.out_idx[base + gi];
+        const float2* src = U + size_t(k) * G::M * G::N + y0;
+        for (int item = threadIdx.x; item < G::RB * G::M; item += G::RT) {
+            const int s = item % G::RB, kx = item / G::RB;
+            cp_async8(&buf[s * G::RP + pidx(kx)], &src[size_t(kx) * G::N + s]);
         }
-        const float2 a = row[pidx(m)];
-        const float2 b = cconj(row[pidx(G::M - m)]);
-        const float2 E = cadd(a, b);
-        const float2 O = cmulc(csub(a, b), __ldg(&tw[m]));
-        return make_float2(E.x - O.y, E.y + O.x);
+        cp_async_commit();
     };
 
-    for (int c = 0; c < C; ++c) {
-        float2 acc[IPT][RL];
+    float2 acc[IPT][RL];
 #pragma unroll
-        for (int it = 0; it < IPT; ++it)
+    for (int it = 0; it < IPT; ++it)
 #pragma unroll
-            for (int r = 0; r < RL; ++r) acc[it][r] = make_float2(0.f, 0.f);
+        for (int r = 0; r < RL; ++r) acc[it][r] = make_float2(0.f, 0.f);
 
-        const int cnt = groups.out_count[c], base = groups.out_start[c];
-        for (int gi = 0; gi < cnt; ++gi) {
-            const int k = groups.out_idx[base + gi];
-            const float2* src = U + size_t(k) * G::M * G::N + y0;
-            for (int item = threadIdx.x; item < G::RB * G::M; item += G::RT) {
-                const int s = item % G::RB, kx = item / G::RB;
-                sm[s * G::RP + pidx(kx)] = __ldg(&src[size_t(kx) * G::N + s]);
-            }
-            __syncthreads();
-            const float mu = gp.mu[k], is2 = gp.inv_s2[k], w = gp.w[k];
-            float* ud = udbg ? udbg + (size_t(k) * G::N + y0) * G::N : nullptr;
-            auto gst = [&](int s, int i, float2 v, int it, int r) {
-                const float dx = v.x - mu, dy = v.y - mu;
-                const float gx = 2.f * expf(-0.5f * dx * dx * is2) - 1.f;
-                const float gy = 2.f * expf(-0.5f * dy * dy * is2) - 1.f;
-                acc[it][r].x += gx * w;
-                acc[it][r].y += gy * w;
-                if (ud) {
-                    reinterpret_cast<float2*>(ud + size_t(s) * G::N)[i] =
-                        make_float2(v.x * udbg_scale, v.y * udbg_scale);
-                }
-            };
-            FftPasses<G::M, 1, true, G::RT, G::RB, 2>::run(ld0, smld, smst, gst, tw);
+    if (cnt > 0) gather(0, sm);
+    for (int gi = 0; gi < cnt; ++gi) {
+        float2* buf = sm + (gi & 1) * BUF;
+        if (gi + 1 < cnt) {
+            gather(gi + 1, sm + ((gi + 1) & 1) * BUF);
+            cp_async_wait<1>();
+        } else {
+            cp_async_wait<0>();
         }
+        __syncthreads();
+        auto smld = [&](int s, int i, int, int) { return buf[s * G::RP + pidx(i)]; };
+        auto smst = [&](int s, int i, float2 v, int, int) { buf[s * G::RP + pidx(i)] = v; };
+        auto ld0 = [&](int s, int m, int, int) -> float2 {
+            const float2* row = buf + s * G::RP;
+            if (m == 0) {
+                const float2 x = row[0];
+                return make_float2(x.x + x.y, x.x - x.y);
+            }
+            const float2 a = row[pidx(m)];
+            const float2 b = cconj(row[pidx(G::M - m)]);
+            const float2 E = cadd(a, b);
+            const float2 O = cmulc(csub(a, b), __ldg(&tw[m]));
+            return make_float2(E.x - O.y, E.y + O.x);
+        };
+        const int k = groups.out_idx[base + gi];
+        const float mu = gp.mu[k], is2 = gp.inv_s2[k], w = gp.w[k];
+        float* ud = udbg ? udbg + (size_t(k) * G::N + y0) * G::N : nullptr;
+        auto gst = [&](int s, int i, float2 v, int it, int r) {
+            const float dx = v.x - mu, dy = v.y - mu;
+            const float gx = 2.f * expf(-0.5f * dx * dx * is2) - 1.f;
+            const float gy = 2.f * expf(-0.5f * dy * dy * is2) - 1.f;
+            acc[it][r].x += gx * w;
+            acc[it][r].y += gy * w;
+            if (ud) {
+                reinterpret_cast<float2*>(ud + size_t(s) * G::N)[i] =
+                    make_float2(v.x * udbg_scale, v.y * udbg_scale);
+            }
+        };
+        FftPasses<G::M, 1, true, G::RT, G::RB, 2>::run(ld0, smld, smst, gst, tw);
+    }
 
-        float* Ac = A + (size_t(c) * G::N + y0) * G::N;
+    float* Ac = A + (size_t(c) * G::N + y0) * G::N;
 #pragma unroll
-        for (int it = 0; it < IPT; ++it) {
-            const int item = threadIdx.x + it * G::RT;
-            if (ITEMS % G::RT == 0 || item < ITEMS) {
-                const int s = item / JL, j = item % JL;
+    for (int it = 0; it < IPT; ++it) {
+        const int item = threadIdx.x + it * G::RT;
+        if (ITEMS % G::RT == 0 || item < ITEMS) {
+            const int s = item / JL, j = item % JL;
 #pragma unroll
-                for (int r = 0; r < RL; ++r) {
-                    const int i = j + r * JL;
-                    reinterpret_cast<float2*>(Ac + size_t(s) * G::N)[i] =
-                        make_float2(expf(temp * acc[it][r].x), expf(temp * acc[it][r].y));
-                }
+            for (int r = 0; r < RL; ++r) {
+                const int i = j + r * JL;
+                reinterpret_cast<float2*>(Ac + size_t(s) * G::N)[i] =
+                    make_float2(expf(temp * acc[it][r].x), expf(temp * acc[it][r].y));
             }
         }
     }
 }
 
 // ---------------------------------------------------------------------------
-// Diffusion: Z = toroidal 3x3 sum of A, new = A * (3x3 sum of state / Z),
-// summed in the reference's order (example.rs:275-301,
-// compute_1024.wgsl:356-411).  One channel tile per CTA; A is read with a
-// 2-pixel halo and the state with a 1-pixel halo, so both passes and the
-// state copy of mod.rs:377-383 collapse into one kernel writing x_out.
-// grid (N/TX, N/TY, C), block 256.
+// Diffusion: Z = toroidal 3x3 sum of A, new = A * (3x3 sum of state / Z)
+// (example.rs:272-303, compute_1024.wgsl:341-413).  One channel tile per
+// CTA; A is read with a 2-pixel halo and the state with a 1-pixel halo, so
+// both passes and the state copy of mod.rs:377-383 collapse into one kernel
+// writing x_out.
+//
+// Mass conservation needs Z to be the exact sum of the nine A values: a
+// rounded f32 sum is off by the same relative amount wherever A is constant
+// (G = -1 for every kernel over a whole region), which drifts the total mass
+// by ~1e-8 per step.  Each A is split into a 12-bit head and an exact tail;
+// sums of up to nine heads are exact in f32 as long as the nine values lie
+// within a factor 2^8 of each other, and the tails are summed in f32
+// (relative weight 2^-12), so zh + zl is Z to ~1e-11.  q = x / Z comes from a
+// reciprocal refined with the exact remainder, i.e. ~correctly rounded.
+// grid (N/TX, N/TY, C), block 256 (64 x 4).
 // ---------------------------------------------------------------------------
+__device__ __forceinline__ float head12(float a) {
+    return __int_as_float(__float_as_int(a) & 0xFFFFF000);
+}
+
 template <int LOGN>
 __global__ void __launch_bounds__(256) k_diffusion(const float* __restrict__ A,
                                                     const float* __restrict__ x,
                                                     float* __restrict__ out) {
     using G = Geo<LOGN>;
     constexpr int N = G::N, TX = G::TX, TY = G::TY;
-    constexpr int AW = TX + 4, AH = TY + 4, QW = TX + 2, QH = TY + 2;
-    __shared__ float sA[AH][AW];
-    __shared__ float sQ[QH][QW];
+    constexpr int AW = TX + 4, AH = TY + 4, HW = TX + 2, QH = TY + 2;
+    __shared__ float sAh[AH][AW], sAl[AH][AW], sHh[AH][HW], sHl[AH][HW], sQ[QH][HW];
+    const int tx = threadIdx.x & 63, ty = threadIdx.x >> 6;
     const int c = blockIdx.z;
     const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
     const float* Ac = A + size_t(c) * N * N;
     const float* xc = x + size_t(c) * N * N;
-    for (int i = threadIdx.x; i < AH * AW; i += blockDim.x) {
-        const int r = i / AW, q = i % AW;
-        const int gy = (y0 + r - 2) & (N - 1), gx = (x0 + q - 2) & (N - 1);
-        sA[r][q] = __ldg(&Ac[size_t(gy) * N + gx]);
+
+    for (int r = ty; r < AH; r += 4) {
+        const float* row = Ac + size_t((y0 + r - 2) & (N - 1)) * N;
+        for (int q = tx; q < AW; q += 64) {
+            const float a = __ldg(&row[(x0 + q - 2) & (N - 1)]);
+            const float h = head12(a);
+            sAh[r][q] = h;
+            sAl[r][q] = a - h;
+        }
     }
-    for (int i = threadIdx.x; i < QH * QW; i += blockDim.x) {
-        const int r = i / QW, q = i % QW;
-        const int gy = (y0 + r - 1) & (N - 1), gx = (x0 + q - 1) & (N - 1);
-        sQ[r][q] = __ldg(&xc[size_t(gy) * N + gx]);
+    for (int r = ty; r < QH; r += 4) {
+        const float* row = xc + size_t((y0 + r - 1) & (N - 1)) * N;
+        for (int q = tx; q < HW; q += 64) sQ[r][q] = __ldg(&row[(x0 + q - 1) & (N - 1)]);
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < QH * QW; i += blockDim.x) {
-        const int r = i / QW, q = i % QW;
-        // Z as an unevaluated float pair (zh + zl): TwoSum keeps every
-        // rounding error, so zh + zl is the 3x3 sum to ~1e-14.  A plain f32
-        // sum is off by a fixed relative amount wherever A is constant
-        // (G = -1 for every kernel across a whole region), which drifts the
-        // total mass by ~1e-8 per step; with the exact Z the only errors
-        // left are the unbiased roundings of q, the sum of q and the product.
-        float zh = sA[r][q], zl = 0.f;
-#pragma unroll
-        for (int t = 1; t < 9; ++t) {
-            const float b = sA[r + t / 3][q + t % 3];
-            const float s = zh + b;
-            const float bb = s - zh;
-            zl += (zh - (s - bb)) + (b - bb);
-            zh = s;
+    for (int r = ty; r < AH; r += 4)
+        for (int q = tx; q < HW; q += 64) {
+            sHh[r][q] = sAh[r][q] + sAh[r][q + 1] + sAh[r][q + 2];
+            sHl[r][q] = sAl[r][q] + sAl[r][q + 1] + sAl[r][q + 2];
         }
-        const float z = zh + zl;
-        zl = zl - (z - zh);
-        zh = z;
-        // q = x / (zh + zl), from the exact remainder of x / zh
-        const float xv = sQ[r][q];
-        const float q0 = xv / zh;
-        const float rem = fmaf(-q0, zh, xv);
-        sQ[r][q] = q0 + (rem - q0 * zl) / zh;
-    }
+    __syncthreads();
+    for (int r = ty; r < QH; r += 4)
+        for (int q = tx; q < HW; q += 64) {
+            const float zh = sHh[r][q] + sHh[r + 1][q] + sHh[r + 2][q];
+            const float zt = sHl[r][q] + sHl[r + 1][q] + sHl[r + 2][q];
+            const float z = zh + zt;
+            const float zl = zt - (z - zh);
+            const float xv = sQ[r][q];
+            const float rz = rcp_approx(z);
+            const float q0 = xv * rz;
+            const float rem = fmaf(-q0, z, xv);
+            sQ[r][q] = fmaf(rem - q0 * zl, rz, q0);
+        }
     __syncthreads();
     float* oc = out + size_t(c) * N * N;
-    for (int i = threadIdx.x; i < TY * TX; i += blockDim.x) {
-        const int r = i / TX, q = i % TX;
-        float s = 0.f;
-#pragma unroll
-        for (int di = 0; di < 3; ++di)
-#pragma unroll
-            for (int dj = 0; dj < 3; ++dj) s += sQ[r + di][q + dj];
-        oc[size_t(y0 + r) * N + x0 + q] = sA[r + 2][q + 2] * s;
-    }
+    for (int r = ty; r < TY; r += 4)
+        for (int q = tx; q < TX; q += 64) {
+            const float s0 = sQ[r][q] + sQ[r][q + 1] + sQ[r][q + 2];
+            const float s1 = sQ[r + 1][q] + sQ[r + 1][q + 1] + sQ[r + 1][q + 2];
+            const float s2 = sQ[r + 2][q] + sQ[r + 2][q + 1] + sQ[r + 2][q + 2];
+            const float a = sAh[r + 2][q + 2] + sAl[r + 2][q + 2];
+            oc[size_t(y0 + r) * N + x0 + q] = a * ((s0 + s1) + s2);
+        }
 }
 
 // ---------------------------------------------------------------------------
@@ -344,11 +454,11 @@ cudaError_t prepare_size() {
     using G = Geo<LOGN>;
     cudaError_t e;
     if ((e = cudaFuncSetAttribute(k_row_r2c<LOGN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  int(G::ROW_SMEM))) != cudaSuccess)
+                                  int(G::R2C_SMEM))) != cudaSuccess)
         return e;
     if ((e = cudaFuncSetAttribute(k_row_c2r_growth<LOGN>,
                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  int(G::ROW_SMEM))) != cudaSuccess)
+                                  int(G::C2R_SMEM))) != cudaSuccess)
         return e;
     return cudaFuncSetAttribute(k_col_conv<LOGN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 int(G::COL_SMEM));
@@ -358,14 +468,14 @@ template <int LOGN>
 cudaError_t launch_step(const StepArgs& a, int phases, cudaStream_t st) {
     using G = Geo<LOGN>;
     if (phases & kPhaseRowFwd)
-        k_row_r2c<LOGN><<<dim3(G::N / G::RB, a.C), G::RT, G::ROW_SMEM, st>>>(a.x_in, a.rowspec,
+        k_row_r2c<LOGN><<<dim3(G::N / G::RB, a.C), G::RT, G::R2C_SMEM, st>>>(a.x_in, a.rowspec,
                                                                             a.tw);
     if (phases & kPhaseColConv)
         k_col_conv<LOGN><<<dim3(G::M / G::TW, a.C), G::CT, G::COL_SMEM, st>>>(
-            a.rowspec, a.kspec, a.U, a.tw, a.groups);
+            a.rowspec, a.kspec, a.U, a.tw, a.groups, a.err);
     if (phases & kPhaseGrowth)
-        k_row_c2r_growth<LOGN><<<G::N / G::RB, G::RT, G::ROW_SMEM, st>>>(
-            a.U, a.A, a.tw, a.groups, a.gp, a.C, a.temp, a.udbg, float(G::N) * float(G::N));
+        k_row_c2r_growth<LOGN><<<dim3(G::N / G::RB, a.C), G::RT, G::C2R_SMEM, st>>>(
+            a.U, a.A, a.tw, a.groups, a.gp, a.temp, a.udbg, float(G::N) * float(G::N));
     if (phases & kPhaseDiffusion)
         k_diffusion<LOGN><<<dim3(G::N / G::TX, G::N / G::TY, a.C), 256, 0, st>>>(a.A, a.x_in,
                                                                                  a.x_out);
