@@ -375,19 +375,48 @@ __global__ void __launch_bounds__(256) k_diffusion(const float* __restrict__ A,
     const float* Ac = A + size_t(c) * N * N;
     const float* xc = x + size_t(c) * N * N;
 
-    for (int r = ty; r < AH; r += 4) {
+    // All halo loads are issued before any is stored, so each thread keeps
+    // ~20 independent DRAM reads in flight instead of one at a time.
+    constexpr int RA = (AH + 3) / 4, RQ = (QH + 3) / 4, CA = (AW + 63) / 64, CQ = (HW + 63) / 64;
+    float av[RA][CA], xin[RQ][CQ];
+#pragma unroll
+    for (int i = 0; i < RA; ++i) {
+        const int r = ty + 4 * i;
         const float* row = Ac + size_t((y0 + r - 2) & (N - 1)) * N;
-        for (int q = tx; q < AW; q += 64) {
-            const float a = __ldg(&row[(x0 + q - 2) & (N - 1)]);
-            const float h = head12(a);
-            sAh[r][q] = h;
-            sAl[r][q] = a - h;
+#pragma unroll
+        for (int j = 0; j < CA; ++j) {
+            const int q = tx + 64 * j;
+            if (r < AH && q < AW) av[i][j] = __ldg(&row[(x0 + q - 2) & (N - 1)]);
         }
     }
-    for (int r = ty; r < QH; r += 4) {
+#pragma unroll
+    for (int i = 0; i < RQ; ++i) {
+        const int r = ty + 4 * i;
         const float* row = xc + size_t((y0 + r - 1) & (N - 1)) * N;
-        for (int q = tx; q < HW; q += 64) sQ[r][q] = __ldg(&row[(x0 + q - 1) & (N - 1)]);
+#pragma unroll
+        for (int j = 0; j < CQ; ++j) {
+            const int q = tx + 64 * j;
+            if (r < QH && q < HW) xin[i][j] = __ldg(&row[(x0 + q - 1) & (N - 1)]);
+        }
     }
+#pragma unroll
+    for (int i = 0; i < RA; ++i)
+#pragma unroll
+        for (int j = 0; j < CA; ++j) {
+            const int r = ty + 4 * i, q = tx + 64 * j;
+            if (r < AH && q < AW) {
+                const float h = head12(av[i][j]);
+                sAh[r][q] = h;
+                sAl[r][q] = av[i][j] - h;
+            }
+        }
+#pragma unroll
+    for (int i = 0; i < RQ; ++i)
+#pragma unroll
+        for (int j = 0; j < CQ; ++j) {
+            const int r = ty + 4 * i, q = tx + 64 * j;
+            if (r < QH && q < HW) sQ[r][q] = xin[i][j];
+        }
     __syncthreads();
     for (int r = ty; r < AH; r += 4)
         for (int q = tx; q < HW; q += 64) {
