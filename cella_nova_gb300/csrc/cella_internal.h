@@ -34,7 +34,7 @@ struct GrowthParams {
 //                 (K(.,0)+K(.,n/2))/2, column n/2 holds (K(.,0)-K(.,n/2))/2
 //   U           : [K][n/2][n] complex — column-inverted products, kx-major
 //   A           : [C][n][n] f32 — exp(temp * weighted growth)
-//   tw          : [n] complex — W_n^m
+//   tw          : W_n^m (m < n), then the per-pass FFT twiddle tables
 struct StepArgs {
     int C, K;
     float temp;
@@ -64,12 +64,17 @@ enum : int {
 typedef cudaError_t (*launch_step_fn)(const StepArgs&, int phases, cudaStream_t);
 typedef cudaError_t (*pack_kernel_fn)(const float2* full, float2* out, cudaStream_t);
 typedef cudaError_t (*prepare_fn)();
+typedef int (*twiddle_count_fn)();
 
 struct SizeOps {
     launch_step_fn step;
     pack_kernel_fn pack;
     prepare_fn prepare;
+    twiddle_count_fn twiddle_count;   // float2 entries of the twiddle buffer
 };
+
+// Fill the twiddle buffer of an n-point grid (host side, double precision).
+void build_twiddle_tables(int n, float2* out);
 
 const SizeOps* size_ops(int logn);
 

@@ -98,10 +98,28 @@ __host__ __device__ constexpr int rem_radix(int L) {
     while ((1 << b) < L) ++b;
     return (b % 4) == 0 ? (L >= 16 ? 16 : L) : (1 << (b % 4));
 }
+__host__ __device__ constexpr int plan_radix(int L, int ns, bool remfirst) {
+    return (remfirst && ns == 1) ? rem_radix(L) : ((L / ns >= 16) ? 16 : (L / ns));
+}
 template <int L, int NS, bool REMFIRST = false>
 struct PassRadix {
-    static constexpr int R = (REMFIRST && NS == 1) ? rem_radix(L) : ((L / NS >= 16) ? 16 : (L / NS));
+    static constexpr int R = plan_radix(L, NS, REMFIRST);
 };
+
+// Per-pass twiddle tables.  The pass starting at sub-transform size NS > 1
+// with radix R reads W_{NS*R}^{r*k} for r in [1, R), k in [0, NS), stored at
+// tw_offset(L, plan, NS) + (r-1)*NS + k: consecutive butterflies read
+// consecutive entries (one or two L1 wavefronts per warp).
+__host__ __device__ constexpr int tw_offset(int L, bool remfirst, int NS) {
+    int off = 0, ns = 1;
+    while (ns < NS) {
+        const int R = plan_radix(L, ns, remfirst);
+        if (ns > 1) off += (R - 1) * ns;
+        ns *= R;
+    }
+    return off;
+}
+__host__ __device__ constexpr int tw_size(int L, bool remfirst) { return tw_offset(L, remfirst, L); }
 
 // Radix of the last pass of a length-L transform.
 __host__ __device__ constexpr int last_radix(int L) {
@@ -119,11 +137,11 @@ __host__ __device__ constexpr int last_radix(int L) {
 // W_{NS*R}^{r*(j mod NS)}, runs DFT-R and stores v[q] at
 // (j div NS)*NS*R + (j mod NS) + q*NS.  All loads finish (barrier) before any
 // store, so in-place passes are safe; a second barrier closes the pass.
-//   twN : W_N^m = exp(-2*pi*i*m/N), m in [0, N); TWS = N / L.
+//   twp : this pass's table (tw_offset layout).
 //   ld(s, i, it, q)         -> float2
 //   st(s, i, v, it, q)      (it, q) name the register slot of the value.
-template <int L, int R, int NS, bool INV, int T, int S, int TWS, class LD, class ST>
-__device__ __forceinline__ void stockham_pass(LD& ld, ST& st, const float2* __restrict__ twN) {
+template <int L, int R, int NS, bool INV, int T, int S, class LD, class ST>
+__device__ __forceinline__ void stockham_pass(LD& ld, ST& st, const float2* __restrict__ twp) {
     constexpr int J = L / R;
     constexpr int ITEMS = S * J;
     constexpr int IPT = (ITEMS + T - 1) / T;
@@ -147,7 +165,7 @@ __device__ __forceinline__ void stockham_pass(LD& ld, ST& st, const float2* __re
             if (NS > 1) {
 #pragma unroll
                 for (int r = 1; r < R; ++r) {
-                    float2 w = __ldg(&twN[r * k * (L / (NS * R)) * TWS]);
+                    float2 w = __ldg(&twp[(r - 1) * NS + k]);
                     if (INV) w.y = -w.y;
                     v[it][r] = cmul(v[it][r], w);
                 }
@@ -163,17 +181,19 @@ __device__ __forceinline__ void stockham_pass(LD& ld, ST& st, const float2* __re
 
 // Full length-L transform: first pass reads through `ld`, middle passes use
 // shared memory through smld/smst, the last pass writes through `stl`.
-template <int L, int NS, bool INV, int T, int S, int TWS, bool REMFIRST = false>
+// `tab` is the plan's twiddle table (tw_offset layout).
+template <int L, int NS, bool INV, int T, int S, bool REMFIRST = false>
 struct FftPasses {
     template <class LD, class SMLD, class SMST, class STL>
     __device__ __forceinline__ static void run(LD& ld, SMLD& smld, SMST& smst, STL& stl,
-                                               const float2* __restrict__ twN) {
+                                               const float2* __restrict__ tab) {
         constexpr int R = PassRadix<L, NS, REMFIRST>::R;
+        const float2* twp = tab + tw_offset(L, REMFIRST, NS);
         if constexpr (NS * R == L) {
-            stockham_pass<L, R, NS, INV, T, S, TWS>(ld, stl, twN);
+            stockham_pass<L, R, NS, INV, T, S>(ld, stl, twp);
         } else {
-            stockham_pass<L, R, NS, INV, T, S, TWS>(ld, smst, twN);
-            FftPasses<L, NS * R, INV, T, S, TWS, false>::run(smld, smld, smst, stl, twN);
+            stockham_pass<L, R, NS, INV, T, S>(ld, smst, twp);
+            FftPasses<L, NS * R, INV, T, S, REMFIRST>::run(smld, smld, smst, stl, tab);
         }
     }
 };

@@ -20,6 +20,7 @@
 
 #include "cella_gpu.h"
 #include "cella_internal.h"
+#include "fft.cuh"
 
 namespace cg {
 extern const SizeOps size_ops_l4, size_ops_l5, size_ops_l6, size_ops_l7, size_ops_l8, size_ops_l9, size_ops_l10,
@@ -62,6 +63,40 @@ int cuda_fail(cudaError_t e, const char* what) {
         cudaError_t e_ = (call);                            \
         if (e_ != cudaSuccess) return cuda_fail(e_, what);  \
     } while (0)
+
+// W_n^m for m < n, then the Stockham pass tables (fft.cuh tw_offset layout)
+// of the column forward plan (greedy), the column inverse plan (remainder
+// first) and the row plan (greedy, length n/2).  Every entry is rounded once
+// from double; the reference builds its table from an f32 angle
+// (convolution.rs:19-30).
+static void fill_plan(int L, bool remfirst, float2* out) {
+    int ns = 1;
+    while (ns < L) {
+        const int R = plan_radix(L, ns, remfirst);
+        if (ns > 1) {
+            float2* t = out + tw_offset(L, remfirst, ns);
+            for (int r = 1; r < R; ++r)
+                for (int k = 0; k < ns; ++k) {
+                    const double a = -2.0 * M_PI * double(r) * double(k) / double(ns * R);
+                    t[(r - 1) * ns + k] = make_float2(float(std::cos(a)), float(std::sin(a)));
+                }
+        }
+        ns *= R;
+    }
+}
+
+void build_twiddle_tables(int n, float2* out) {
+    for (int m = 0; m < n; ++m) {
+        const double a = -2.0 * M_PI * double(m) / double(n);
+        out[m] = make_float2(float(std::cos(a)), float(std::sin(a)));
+    }
+    float2* p = out + n;
+    fill_plan(n, false, p);
+    p += tw_size(n, false);
+    fill_plan(n, true, p);
+    p += tw_size(n, true);
+    fill_plan(n / 2, false, p);
+}
 
 }  // namespace cg
 
@@ -161,14 +196,9 @@ int capture_graphs(cg_sim* s) {
 }
 
 int build_twiddles(cg_sim* s) {
-    std::vector<float2> h(s->n);
-    for (int m = 0; m < s->n; ++m) {
-        // W_n^m rounded once from double (the reference's table uses an f32
-        // angle, convolution.rs:25-26).
-        const double a = -2.0 * M_PI * double(m) / double(s->n);
-        h[m] = make_float2(float(std::cos(a)), float(std::sin(a)));
-    }
-    CG_CHECK(cudaMemcpy(s->tw, h.data(), sizeof(float2) * s->n, cudaMemcpyHostToDevice),
+    std::vector<float2> h(size_t(s->ops->twiddle_count()));
+    build_twiddle_tables(s->n, h.data());
+    CG_CHECK(cudaMemcpy(s->tw, h.data(), sizeof(float2) * h.size(), cudaMemcpyHostToDevice),
              "uploading twiddles");
     return CG_OK;
 }
@@ -286,7 +316,8 @@ int cg_create(int n, int C, int K, const uint32_t* c0, const uint32_t* c1, const
         chk(cudaMalloc(&s->kspec, sizeof(float2) * K * (half + n)), "cudaMalloc(kspec)");
     if (rc == CG_OK) chk(cudaMalloc(&s->U, sizeof(float2) * K * half), "cudaMalloc(U)");
     if (rc == CG_OK) chk(cudaMalloc(&s->A, sizeof(float) * C * px), "cudaMalloc(A)");
-    if (rc == CG_OK) chk(cudaMalloc(&s->tw, sizeof(float2) * n), "cudaMalloc(twiddles)");
+    if (rc == CG_OK)
+        chk(cudaMalloc(&s->tw, sizeof(float2) * s->ops->twiddle_count()), "cudaMalloc(twiddles)");
     if (rc == CG_OK) chk(cudaMalloc(&s->staging, sizeof(double) * px), "cudaMalloc(staging)");
     if (rc == CG_OK)
         chk(cudaMalloc(&s->mass_partial, sizeof(double) * C * kMassBlocks), "cudaMalloc(mass)");

@@ -45,6 +45,12 @@ struct Geo {
     static constexpr int CT = 256;
     static constexpr int CP = padded_len(N) + 1;
     static constexpr size_t COL_SMEM = (size_t(TW) * CP + size_t(TW) * N) * sizeof(float2);
+    // Twiddle buffer: W_N^m (m < N), then the pass tables of the column
+    // forward plan, the column inverse plan and the row plan.
+    static constexpr int TW_COL_FWD = N;
+    static constexpr int TW_COL_INV = TW_COL_FWD + tw_size(N, false);
+    static constexpr int TW_ROW = TW_COL_INV + tw_size(N, true);
+    static constexpr int TW_TOTAL = TW_ROW + tw_size(M, false);
     // Diffusion tile.
     static constexpr int TX = N < 64 ? N : 64;
     static constexpr int TY = N < 32 ? N : 32;
@@ -71,7 +77,7 @@ __global__ void __launch_bounds__(512) k_row_r2c(const float* __restrict__ state
     auto ld0 = [&](int s, int i, int, int) { return __ldg(&src[size_t(s) * G::M + i]); };
     auto smld = [&](int s, int i, int, int) { return sm[s * G::RP + pidx(i)]; };
     auto smst = [&](int s, int i, float2 v, int, int) { sm[s * G::RP + pidx(i)] = v; };
-    FftPasses<G::M, 1, false, G::RT, G::RB, 2>::run(ld0, smld, smst, smst, tw);
+    FftPasses<G::M, 1, false, G::RT, G::RB>::run(ld0, smld, smst, smst, tw + G::TW_ROW);
 
     constexpr int H = G::M / 2;
     for (int item = threadIdx.x; item < G::RB * (H + 1); item += G::RT) {
@@ -100,18 +106,18 @@ __global__ void __launch_bounds__(512) k_row_r2c(const float* __restrict__ state
 }
 
 // Run the first pass of a transform, then `hook()`, then the rest.
-template <int L, bool INV, int T, int S, int TWS, bool REMFIRST, class LD, class SMLD, class SMST,
+template <int L, bool INV, int T, int S, bool REMFIRST, class LD, class SMLD, class SMST,
           class STL, class HOOK>
 __device__ __forceinline__ void fft_with_hook(LD& ld, SMLD& smld, SMST& smst, STL& stl,
-                                              const float2* __restrict__ twN, HOOK hook) {
+                                              const float2* __restrict__ tab, HOOK hook) {
     constexpr int R = PassRadix<L, 1, REMFIRST>::R;
     if constexpr (R == L) {
-        stockham_pass<L, R, 1, INV, T, S, TWS>(ld, stl, twN);
+        stockham_pass<L, R, 1, INV, T, S>(ld, stl, tab);
         hook();
     } else {
-        stockham_pass<L, R, 1, INV, T, S, TWS>(ld, smst, twN);
+        stockham_pass<L, R, 1, INV, T, S>(ld, smst, tab);
         hook();
-        FftPasses<L, R, INV, T, S, TWS, false>::run(smld, smld, smst, stl, twN);
+        FftPasses<L, R, INV, T, S, REMFIRST>::run(smld, smld, smst, stl, tab);
     }
 }
 
@@ -198,8 +204,8 @@ __global__ void __launch_bounds__(256, 2) k_col_conv(const float2* __restrict__ 
     auto wld = [&](int s, int i, int, int) { return W[s * G::CP + pidx(i)]; };
     auto wst = [&](int s, int i, float2 v, int, int) { W[s * G::CP + pidx(i)] = v; };
     auto keep = [&](int, int, float2 v, int it, int r) { F[it][r] = v; };
-    fft_with_hook<N, false, T, TW, 1, false>(ld_in, wld, wst, keep, tw,
-                                            [&]() { issue(kernel_tile(0)); });
+    fft_with_hook<N, false, T, TW, false>(ld_in, wld, wst, keep, tw + G::TW_COL_FWD,
+                                         [&]() { issue(kernel_tile(0)); });
 
     for (int gi = 0; gi < cnt; ++gi) {
         if (!wait_tile()) return;
@@ -229,7 +235,7 @@ __global__ void __launch_bounds__(256, 2) k_col_conv(const float2* __restrict__ 
         };
         float2* dst = U + (size_t(k) * M + kx0) * N;
         auto gst = [&](int s, int i, float2 v, int, int) { dst[size_t(s) * N + i] = v; };
-        fft_with_hook<N, true, T, TW, 1, true>(ld_mul, wld, wst, gst, tw, [&]() {
+        fft_with_hook<N, true, T, TW, true>(ld_mul, wld, wst, gst, tw + G::TW_COL_INV, [&]() {
             if (gi + 1 < cnt) issue(kernel_tile(gi + 1));
         });
     }
@@ -321,7 +327,7 @@ __global__ void __launch_bounds__(512) k_row_c2r_growth(const float2* __restrict
                     make_float2(v.x * udbg_scale, v.y * udbg_scale);
             }
         };
-        FftPasses<G::M, 1, true, G::RT, G::RB, 2>::run(ld0, smld, smst, gst, tw);
+        FftPasses<G::M, 1, true, G::RT, G::RB>::run(ld0, smld, smst, gst, tw + G::TW_ROW);
     }
 
     float* Ac = A + (size_t(c) * G::N + y0) * G::N;
@@ -361,6 +367,22 @@ __device__ __forceinline__ float head12(float a) {
     return __int_as_float(__float_as_int(a) & 0xFFFFF000);
 }
 
+// Visit every (r, q) of an H x W region of a tile with 256 threads: rows in
+// steps of 4 with q = lane index (no divergence for q < 64), then the few
+// columns past 64 as one flat loop.
+template <int H, int W, class F>
+__device__ __forceinline__ void for_tile(F fn) {
+    const int tx = threadIdx.x & 63, ty = threadIdx.x >> 6;
+    constexpr int W0 = W < 64 ? W : 64;
+#pragma unroll 4
+    for (int r = ty; r < H; r += 4)
+        if (tx < W0) fn(r, tx);
+    if constexpr (W > 64) {
+        constexpr int E = W - 64;
+        for (int i = threadIdx.x; i < H * E; i += 256) fn(i / E, 64 + i % E);
+    }
+}
+
 template <int LOGN>
 __global__ void __launch_bounds__(256) k_diffusion(const float* __restrict__ A,
                                                     const float* __restrict__ x,
@@ -369,6 +391,7 @@ __global__ void __launch_bounds__(256) k_diffusion(const float* __restrict__ A,
     constexpr int N = G::N, TX = G::TX, TY = G::TY;
     constexpr int AW = TX + 4, AH = TY + 4, HW = TX + 2, QH = TY + 2;
     __shared__ float sAh[AH][AW], sAl[AH][AW], sHh[AH][HW], sHl[AH][HW], sQ[QH][HW];
+    float (*sQs)[TX] = reinterpret_cast<float (*)[TX]>(&sHh[0][0]);   // reuses sHh
     const int tx = threadIdx.x & 63, ty = threadIdx.x >> 6;
     const int c = blockIdx.z;
     const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
@@ -410,42 +433,40 @@ __global__ void __launch_bounds__(256) k_diffusion(const float* __restrict__ A,
                 sAl[r][q] = av[i][j] - h;
             }
         }
+    __syncthreads();
+    // horizontal 3-sums of the heads (exact) and of the tails
+    for_tile<AH, HW>([&](int r, int q) {
+        sHh[r][q] = sAh[r][q] + sAh[r][q + 1] + sAh[r][q + 2];
+        sHl[r][q] = sAl[r][q] + sAl[r][q + 1] + sAl[r][q + 2];
+    });
+    __syncthreads();
+    // Z = zh + zl on the 1-pixel halo, then q = x / Z (x still in registers)
 #pragma unroll
     for (int i = 0; i < RQ; ++i)
 #pragma unroll
         for (int j = 0; j < CQ; ++j) {
             const int r = ty + 4 * i, q = tx + 64 * j;
-            if (r < QH && q < HW) sQ[r][q] = xin[i][j];
+            if (r < QH && q < HW) {
+                const float zh = sHh[r][q] + sHh[r + 1][q] + sHh[r + 2][q];
+                const float zt = sHl[r][q] + sHl[r + 1][q] + sHl[r + 2][q];
+                const float z = zh + zt;
+                const float zl = zt - (z - zh);
+                const float xv = xin[i][j];
+                const float rz = rcp_approx(z);
+                const float q0 = xv * rz;
+                const float rem = fmaf(-q0, z, xv);
+                sQ[r][q] = fmaf(rem - q0 * zl, rz, q0);
+            }
         }
-    __syncthreads();
-    for (int r = ty; r < AH; r += 4)
-        for (int q = tx; q < HW; q += 64) {
-            sHh[r][q] = sAh[r][q] + sAh[r][q + 1] + sAh[r][q + 2];
-            sHl[r][q] = sAl[r][q] + sAl[r][q + 1] + sAl[r][q + 2];
-        }
-    __syncthreads();
-    for (int r = ty; r < QH; r += 4)
-        for (int q = tx; q < HW; q += 64) {
-            const float zh = sHh[r][q] + sHh[r + 1][q] + sHh[r + 2][q];
-            const float zt = sHl[r][q] + sHl[r + 1][q] + sHl[r + 2][q];
-            const float z = zh + zt;
-            const float zl = zt - (z - zh);
-            const float xv = sQ[r][q];
-            const float rz = rcp_approx(z);
-            const float q0 = xv * rz;
-            const float rem = fmaf(-q0, z, xv);
-            sQ[r][q] = fmaf(rem - q0 * zl, rz, q0);
-        }
+    __syncthreads();   // sHh is reused as sQs below
+    // horizontal 3-sums of q, then the vertical sum times A
+    for_tile<QH, TX>([&](int r, int q) { sQs[r][q] = sQ[r][q] + sQ[r][q + 1] + sQ[r][q + 2]; });
     __syncthreads();
     float* oc = out + size_t(c) * N * N;
-    for (int r = ty; r < TY; r += 4)
-        for (int q = tx; q < TX; q += 64) {
-            const float s0 = sQ[r][q] + sQ[r][q + 1] + sQ[r][q + 2];
-            const float s1 = sQ[r + 1][q] + sQ[r + 1][q + 1] + sQ[r + 1][q + 2];
-            const float s2 = sQ[r + 2][q] + sQ[r + 2][q + 1] + sQ[r + 2][q + 2];
-            const float a = sAh[r + 2][q + 2] + sAl[r + 2][q + 2];
-            oc[size_t(y0 + r) * N + x0 + q] = a * ((s0 + s1) + s2);
-        }
+    for_tile<TY, TX>([&](int r, int q) {
+        const float a = sAh[r + 2][q + 2] + sAl[r + 2][q + 2];
+        oc[size_t(y0 + r) * N + x0 + q] = a * ((sQs[r][q] + sQs[r + 1][q]) + sQs[r + 2][q]);
+    });
 }
 
 // ---------------------------------------------------------------------------
@@ -512,6 +533,11 @@ cudaError_t launch_step(const StepArgs& a, int phases, cudaStream_t st) {
 }
 
 template <int LOGN>
+int twiddle_count() {
+    return Geo<LOGN>::TW_TOTAL;
+}
+
+template <int LOGN>
 cudaError_t launch_pack(const float2* full, float2* out, cudaStream_t st) {
     using G = Geo<LOGN>;
     const int total = G::M * G::N;
@@ -525,5 +551,5 @@ cudaError_t launch_pack(const float2* full, float2* out, cudaStream_t st) {
     namespace cg {                                                                      \
     extern const SizeOps size_ops_l##LOGN;                                              \
     const SizeOps size_ops_l##LOGN = {launch_step<LOGN>, launch_pack<LOGN>,             \
-                                      prepare_size<LOGN>};                              \
+                                      prepare_size<LOGN>, twiddle_count<LOGN>};         \
     }
