@@ -65,6 +65,7 @@ SIGNATURES = {
     "cg_timed_iterate": ([_P, _DP], _I),
     "cg_profile_kernels": ([_P, _I, _DP], _I),
     "cg_mass_f64": ([_P, _DP], _I),
+    "cg_mass_f64_noalloc": ([_P, _I, _I, _P, _P], _I),
     "cg_channel_ptr": ([_P, ctypes.POINTER(_P)], _I),
     "cg_stream": ([_P, ctypes.POINTER(_P)], _I),
     "cg_synchronize": ([_P], _I),

@@ -1,4 +1,8 @@
 // Size-independent kernels: f64 -> f32 channel upload and the FP64 mass sum.
+#include <mutex>
+#include <unordered_map>
+
+#include "cella_gpu.h"
 #include "cella_internal.h"
 
 namespace cg {
@@ -69,4 +73,58 @@ cudaError_t launch_mass_f64(const float* x, int C, size_t px, double* partial, i
     return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------------------
+// Mass reduction without device allocation (cg_mass_f64_noalloc).
+//
+// The per-block partial sums live in this fixed array instead of a buffer
+// from cudaMalloc.  Every GPU that loads the library holds it (37,888 bytes)
+// until the process exits.  Host code cannot pass the array's name to a
+// kernel: on the host that name is only a stand-in, not a device address, so
+// the address is looked up once per device with cudaGetSymbolAddress while
+// that device is current, and cached.
+// ---------------------------------------------------------------------------
+constexpr int kNoAllocMaxC = kMaxC;
+static __device__ __align__(256) double g_mass_scratch[kNoAllocMaxC * kMassBlocks];
+
+int fail(int code, const char* fmt, ...);
+
+static cudaError_t mass_scratch_address(double** out) {
+    static std::mutex mu;
+    static std::unordered_map<int, double*> by_device;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lock(mu);
+    auto it = by_device.find(dev);
+    if (it == by_device.end()) {
+        void* p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_mass_scratch);
+        if (e != cudaSuccess) return e;
+        it = by_device.emplace(dev, static_cast<double*>(p)).first;
+    }
+    *out = it->second;
+    return cudaSuccess;
+}
+
 }  // namespace cg
+
+extern "C" int cg_mass_f64_noalloc(const float* dev_state, int n, int C, double* dev_out,
+                                   cg_stream_t stream) {
+    using namespace cg;
+    if (!dev_state || !dev_out) return fail(CG_ERR_ARG, "cg_mass_f64_noalloc: NULL pointer");
+    if (n < 1) return fail(CG_ERR_ARG, "cg_mass_f64_noalloc: grid side %d < 1", n);
+    if (C < 1 || C > kNoAllocMaxC)
+        return fail(CG_ERR_ARG,
+                    "cg_mass_f64_noalloc: %d channels; its fixed scratch holds at most %d", C,
+                    kNoAllocMaxC);
+    double* scratch = nullptr;
+    cudaError_t e = mass_scratch_address(&scratch);
+    if (e != cudaSuccess)
+        return fail(CG_ERR_CUDA, "cg_mass_f64_noalloc: scratch address: %s", cudaGetErrorString(e));
+    // k_mass_partial overwrites every slot it uses, so nothing needs clearing.
+    e = launch_mass_f64(dev_state, C, size_t(n) * size_t(n), scratch, kMassBlocks, dev_out,
+                        static_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess)
+        return fail(CG_ERR_CUDA, "cg_mass_f64_noalloc: launch: %s", cudaGetErrorString(e));
+    return CG_OK;
+}

@@ -124,6 +124,26 @@ int cg_profile_kernels(cg_sim* sim, int nsteps, double ms[4]);
  * Blocking; out has C entries. */
 int cg_mass_f64(cg_sim* sim, double* out);
 
+/* Per-channel FP64 total mass of a C*n*n f32 state that the caller already
+ * holds on the device, written to dev_out (C doubles, device memory).  It
+ * allocates nothing: no cudaMalloc, cudaFree or allocating library call.  It
+ * is for callers that cannot allocate device memory while they run, such as
+ * code that works inside a memory budget another component has already
+ * reserved, or a loop where cudaMalloc's implicit device-wide
+ * synchronisation is not acceptable.  No counterpart in the reference.
+ *   - C <= 16 (CG_ERR_ARG beyond): its scratch is a fixed 16 x 296-double
+ *     array in device memory, held by every GPU that loads the library
+ *     until the process exits.
+ *   - The first call on a device looks up that array's device address with
+ *     cudaGetSymbolAddress (the device must be current); make that first
+ *     call before any stream capture.
+ *   - Work is enqueued on `stream` (NULL = the legacy default stream) and
+ *     dev_out is valid once that stream is synchronised.
+ *   - All calls share the one array: calls that overlap on the GPU (other
+ *     streams, other threads) race and give wrong sums; serialise them. */
+int cg_mass_f64_noalloc(const float* dev_state, int n, int C, double* dev_out,
+                        cg_stream_t stream);
+
 /* GpuMaceLenia::channel_buffer, mod.rs:202-204: device pointer to the
  * current C*n*n f32 state (valid until the next step or destroy). */
 int cg_channel_ptr(cg_sim* sim, float** dev_ptr);
