@@ -102,4 +102,11 @@ __device__ __forceinline__ float rcp_approx(float x) {
     return r;
 }
 
+// 2^x to a few ulp (MUFU); subnormal results flush to zero.
+__device__ __forceinline__ float ex2_approx(float x) {
+    float r;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
 }  // namespace cg

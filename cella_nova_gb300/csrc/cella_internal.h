@@ -19,11 +19,14 @@ struct KernelGroups {
     int out_idx[kMaxK];   // kernels sorted by c1
 };
 
-// Growth parameters per kernel (growth.rs:46-75): mu, 1/sigma^2, weight.
+// Growth parameters per kernel (growth.rs:46-75), pre-scaled on the host:
+// mu, c2 = -log2(e) / (2 sigma^2), w2 = 2 w; and per output channel the sum
+// of its kernels' weights (in increasing k).
 struct GrowthParams {
     float mu[kMaxK];
-    float inv_s2[kMaxK];
-    float w[kMaxK];
+    float c2[kMaxK];
+    float w2[kMaxK];
+    float wsum[kMaxC];
 };
 
 // Everything one step's launches need.  Planar layouts, all device pointers:

@@ -288,8 +288,14 @@ int cg_create(int n, int C, int K, const uint32_t* c0, const uint32_t* c1, const
     }
     for (int k = 0; k < K; ++k) {
         s->gp.mu[k] = mu[k];
-        s->gp.inv_s2[k] = float(1.0 / (double(sigma[k]) * double(sigma[k])));
-        s->gp.w[k] = weights[k];
+        s->gp.c2[k] = float(-1.4426950408889634 / (2.0 * double(sigma[k]) * double(sigma[k])));
+        s->gp.w2[k] = 2.0f * weights[k];
+    }
+    for (int c = 0; c < C; ++c) {
+        float ws = 0.f;   // f32, increasing k: the reference's sum of w * (-1)
+        for (int i = 0; i < s->groups.out_count[c]; ++i)
+            ws += weights[s->groups.out_idx[s->groups.out_start[c] + i]];
+        s->gp.wsum[c] = ws;
     }
 
     int rc = CG_OK;

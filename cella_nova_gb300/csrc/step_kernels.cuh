@@ -248,6 +248,8 @@ __global__ void __launch_bounds__(256, 2) k_col_conv(const float2* __restrict__ 
 //   u = value (the 1/n^2 of growth.rs:87 is folded into kspec),
 //   g = 2 exp(-(u-mu)^2 / (2 sigma^2)) - 1,  acc += w g;
 // then A[c] = exp(temp * acc) (diffusion.rs:58-66 applies temp inside exp).
+// The exponential of the bump is ex2.approx (a few ulp, like expf) on a
+// host-folded scale c2 = -log2(e) / (2 sigma^2).
 // C2R: Z[m] = E + i O, E = X[m] + conj X[M-m], O = (X[m] - conj X[M-m]) W_N^-m,
 // z = IFFT_M(Z) = (x[2j], x[2j+1]).
 // The next kernel's U tile is gathered (a transpose, per-element cp.async)
@@ -314,14 +316,14 @@ __global__ void __launch_bounds__(512) k_row_c2r_growth(const float2* __restrict
             return make_float2(E.x - O.y, E.y + O.x);
         };
         const int k = groups.out_idx[base + gi];
-        const float mu = gp.mu[k], is2 = gp.inv_s2[k], w = gp.w[k];
+        const float mu = gp.mu[k], c2 = gp.c2[k], w2 = gp.w2[k];
         float* ud = udbg ? udbg + (size_t(k) * G::N + y0) * G::N : nullptr;
+        // w G = w (2 e - 1) with e = exp(-(u-mu)^2 / (2 sigma^2)) = 2^(d^2 c2):
+        // accumulate 2 w e here, subtract sum(w) once per channel below.
         auto gst = [&](int s, int i, float2 v, int it, int r) {
             const float dx = v.x - mu, dy = v.y - mu;
-            const float gx = 2.f * expf(-0.5f * dx * dx * is2) - 1.f;
-            const float gy = 2.f * expf(-0.5f * dy * dy * is2) - 1.f;
-            acc[it][r].x += gx * w;
-            acc[it][r].y += gy * w;
+            acc[it][r].x = fmaf(w2, ex2_approx(dx * dx * c2), acc[it][r].x);
+            acc[it][r].y = fmaf(w2, ex2_approx(dy * dy * c2), acc[it][r].y);
             if (ud) {
                 reinterpret_cast<float2*>(ud + size_t(s) * G::N)[i] =
                     make_float2(v.x * udbg_scale, v.y * udbg_scale);
@@ -331,6 +333,7 @@ __global__ void __launch_bounds__(512) k_row_c2r_growth(const float2* __restrict
     }
 
     float* Ac = A + (size_t(c) * G::N + y0) * G::N;
+    const float wsum = gp.wsum[c];
 #pragma unroll
     for (int it = 0; it < IPT; ++it) {
         const int item = threadIdx.x + it * G::RT;
@@ -340,7 +343,8 @@ __global__ void __launch_bounds__(512) k_row_c2r_growth(const float2* __restrict
             for (int r = 0; r < RL; ++r) {
                 const int i = j + r * JL;
                 reinterpret_cast<float2*>(Ac + size_t(s) * G::N)[i] =
-                    make_float2(expf(temp * acc[it][r].x), expf(temp * acc[it][r].y));
+                    make_float2(expf(temp * (acc[it][r].x - wsum)),
+                                expf(temp * (acc[it][r].y - wsum)));
             }
         }
     }
@@ -399,40 +403,49 @@ __global__ void __launch_bounds__(256) k_diffusion(const float* __restrict__ A,
     const float* xc = x + size_t(c) * N * N;
 
     // All halo loads are issued before any is stored, so each thread keeps
-    // ~20 independent DRAM reads in flight instead of one at a time.
-    constexpr int RA = (AH + 3) / 4, RQ = (QH + 3) / 4, CA = (AW + 63) / 64, CQ = (HW + 63) / 64;
-    float av[RA][CA], xin[RQ][CQ];
+    // ~20 independent DRAM reads in flight instead of one at a time.  Lanes
+    // cover columns 0..63; the 2-4 columns past 64 go through flat tails.
+    constexpr int RA = (AH + 3) / 4, RQ = (QH + 3) / 4;
+    constexpr int A0 = AW < 64 ? AW : 64, Q0 = HW < 64 ? HW : 64;
+    float av[RA], xin[RQ];
 #pragma unroll
     for (int i = 0; i < RA; ++i) {
         const int r = ty + 4 * i;
-        const float* row = Ac + size_t((y0 + r - 2) & (N - 1)) * N;
-#pragma unroll
-        for (int j = 0; j < CA; ++j) {
-            const int q = tx + 64 * j;
-            if (r < AH && q < AW) av[i][j] = __ldg(&row[(x0 + q - 2) & (N - 1)]);
-        }
+        if (r < AH && tx < A0)
+            av[i] = __ldg(&Ac[size_t((y0 + r - 2) & (N - 1)) * N + ((x0 + tx - 2) & (N - 1))]);
     }
 #pragma unroll
     for (int i = 0; i < RQ; ++i) {
         const int r = ty + 4 * i;
-        const float* row = xc + size_t((y0 + r - 1) & (N - 1)) * N;
-#pragma unroll
-        for (int j = 0; j < CQ; ++j) {
-            const int q = tx + 64 * j;
-            if (r < QH && q < HW) xin[i][j] = __ldg(&row[(x0 + q - 1) & (N - 1)]);
+        if (r < QH && tx < Q0)
+            xin[i] = __ldg(&xc[size_t((y0 + r - 1) & (N - 1)) * N + ((x0 + tx - 1) & (N - 1))]);
+    }
+    if constexpr (AW > 64) {
+        constexpr int E = AW - 64;
+        for (int t = threadIdx.x; t < AH * E; t += 256) {
+            const int r = t / E, q = 64 + t % E;
+            const float a = __ldg(&Ac[size_t((y0 + r - 2) & (N - 1)) * N + ((x0 + q - 2) & (N - 1))]);
+            const float h = head12(a);
+            sAh[r][q] = h;
+            sAl[r][q] = a - h;
+        }
+    }
+    if constexpr (HW > 64) {
+        constexpr int E = HW - 64;
+        for (int t = threadIdx.x; t < QH * E; t += 256) {
+            const int r = t / E, q = 64 + t % E;
+            sQ[r][q] = __ldg(&xc[size_t((y0 + r - 1) & (N - 1)) * N + ((x0 + q - 1) & (N - 1))]);
         }
     }
 #pragma unroll
-    for (int i = 0; i < RA; ++i)
-#pragma unroll
-        for (int j = 0; j < CA; ++j) {
-            const int r = ty + 4 * i, q = tx + 64 * j;
-            if (r < AH && q < AW) {
-                const float h = head12(av[i][j]);
-                sAh[r][q] = h;
-                sAl[r][q] = av[i][j] - h;
-            }
+    for (int i = 0; i < RA; ++i) {
+        const int r = ty + 4 * i;
+        if (r < AH && tx < A0) {
+            const float h = head12(av[i]);
+            sAh[r][tx] = h;
+            sAl[r][tx] = av[i] - h;
         }
+    }
     __syncthreads();
     // horizontal 3-sums of the heads (exact) and of the tails
     for_tile<AH, HW>([&](int r, int q) {
@@ -440,24 +453,29 @@ __global__ void __launch_bounds__(256) k_diffusion(const float* __restrict__ A,
         sHl[r][q] = sAl[r][q] + sAl[r][q + 1] + sAl[r][q + 2];
     });
     __syncthreads();
-    // Z = zh + zl on the 1-pixel halo, then q = x / Z (x still in registers)
+    // Z = zh + zl on the 1-pixel halo, then q = x / Z
+    auto qval = [&](int r, int q, float xv) {
+        const float zh = sHh[r][q] + sHh[r + 1][q] + sHh[r + 2][q];
+        const float zt = sHl[r][q] + sHl[r + 1][q] + sHl[r + 2][q];
+        const float z = zh + zt;
+        const float zl = zt - (z - zh);
+        const float rz = rcp_approx(z);
+        const float q0 = xv * rz;
+        const float rem = fmaf(-q0, z, xv);
+        return fmaf(rem - q0 * zl, rz, q0);
+    };
 #pragma unroll
-    for (int i = 0; i < RQ; ++i)
-#pragma unroll
-        for (int j = 0; j < CQ; ++j) {
-            const int r = ty + 4 * i, q = tx + 64 * j;
-            if (r < QH && q < HW) {
-                const float zh = sHh[r][q] + sHh[r + 1][q] + sHh[r + 2][q];
-                const float zt = sHl[r][q] + sHl[r + 1][q] + sHl[r + 2][q];
-                const float z = zh + zt;
-                const float zl = zt - (z - zh);
-                const float xv = xin[i][j];
-                const float rz = rcp_approx(z);
-                const float q0 = xv * rz;
-                const float rem = fmaf(-q0, z, xv);
-                sQ[r][q] = fmaf(rem - q0 * zl, rz, q0);
-            }
+    for (int i = 0; i < RQ; ++i) {
+        const int r = ty + 4 * i;
+        if (r < QH && tx < Q0) sQ[r][tx] = qval(r, tx, xin[i]);
+    }
+    if constexpr (HW > 64) {
+        constexpr int E = HW - 64;
+        for (int t = threadIdx.x; t < QH * E; t += 256) {
+            const int r = t / E, q = 64 + t % E;
+            sQ[r][q] = qval(r, q, sQ[r][q]);
         }
+    }
     __syncthreads();   // sHh is reused as sQs below
     // horizontal 3-sums of q, then the vertical sum times A
     for_tile<QH, TX>([&](int r, int q) { sQs[r][q] = sQ[r][q] + sQ[r][q + 1] + sQ[r][q + 2]; });
