@@ -11,7 +11,8 @@ ABI (include/cella_gpu.h); this package is its Python binding:
 * :mod:`cella_nova_gb300.build` — builds the library in-tree.
 """
 from ._abi import CellaError, load as load_library  # noqa: F401
-from .orchestrator import GpuMaceLenia, load_config, load_kernels, setup_simulation  # noqa: F401
+from .orchestrator import (GpuMaceLenia, GpuMaceLeniaBatch, load_config, load_kernels,  # noqa: F401
+                           setup_simulation)
 
-__all__ = ["CellaError", "GpuMaceLenia", "load_config", "load_kernels", "setup_simulation",
+__all__ = ["CellaError", "GpuMaceLenia", "GpuMaceLeniaBatch", "load_config", "load_kernels", "setup_simulation",
            "load_library"]

@@ -69,6 +69,18 @@ SIGNATURES = {
     "cg_channel_ptr": ([_P, ctypes.POINTER(_P)], _I),
     "cg_stream": ([_P, ctypes.POINTER(_P)], _I),
     "cg_synchronize": ([_P], _I),
+    "cg_batch_create": ([_I, ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_I), _UP, _UP,
+                         _FP, _FP, _FP, _FP, _P, ctypes.POINTER(_P)], _I),
+    "cg_batch_destroy": ([_P], _I),
+    "cg_batch_set_kernel": ([_P, _I, _I, _FP], _I),
+    "cg_batch_upload_channel": ([_P, _I, _I, _DP], _I),
+    "cg_batch_step": ([_P, _I], _I),
+    "cg_batch_download_channels": ([_P, _I, _FP], _I),
+    "cg_batch_mass_f64": ([_P, _I, _DP], _I),
+    "cg_batch_synchronize": ([_P], _I),
+    "cg_batch_profile": ([_P, _I, _DP], _I),
+    "cg_batch_stream": ([_P, ctypes.POINTER(_P)], _I),
+    "cg_batch_info": ([_P, ctypes.POINTER(_I), ctypes.POINTER(_I)], _I),
     "cg_load_config_json": ([ctypes.c_char_p, ctypes.POINTER(cg_config)], _I),
     "cg_free_config": ([ctypes.POINTER(cg_config)], None),
     "cg_load_kernels_bin": ([ctypes.c_char_p, _I, _I, _FP], _I),

@@ -22,7 +22,7 @@ LIB = os.path.join(PKG, "libcella_gpu.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_SOURCES = ["host.cu", "kernels_common.cu", "kernels_small.cu", "kernels_mid.cu",
-              "kernels_l11.cu"]
+              "kernels_l11.cu", "batch.cu"]
 CXX_SOURCES = ["config_io.cpp"]
 
 

@@ -82,6 +82,26 @@ def ring_kernel(n: int, R: float, b) -> np.ndarray:
     return k / s if s > 0 else k
 
 
+def _kernel_spectrum_torch(n: int, R: float, b, device) -> np.ndarray:
+    """ring_kernel + fft2 in float64 with torch on `device` (same math)."""
+    import torch
+    d = (torch.arange(n, device=device, dtype=torch.float64) + n // 2) % n - n // 2
+    r = torch.sqrt(d[:, None] ** 2 + d[None, :] ** 2) / R
+    B = len(b)
+    rb = r * B
+    idx = torch.floor(rb)
+    t = rb - idx
+    inside = (t > 0) & (t < 1) & (r < 1.0)
+    tt = torch.where(inside, t, torch.full_like(t, 0.5))
+    core = torch.where(inside, torch.exp(4.0 - 1.0 / (tt * (1.0 - tt))), torch.zeros_like(t))
+    bw = torch.tensor(list(b) + [0.0], dtype=torch.float64, device=device)
+    k = core * bw[idx.clamp(0, B).long()]
+    s = k.sum()
+    if float(s) > 0:
+        k = k / s
+    return torch.fft.fft2(k).to(torch.complex64).cpu().numpy()
+
+
 def all_pairs(C: int):
     """Kernels over every (input, output) pair, in the orchestrator's order.
 
@@ -96,11 +116,13 @@ def all_pairs(C: int):
 def make_creature(n: int, C: int = 3, *, seed: int = 0, K: int | None = None,
                   c0=None, c1=None, radius=None, temp: float = 1.0,
                   seed_box: int = 256, mu_range=(0.05, 0.3),
-                  sigma_range=(0.01, 0.08)) -> Creature:
+                  sigma_range=(0.01, 0.08), device=None) -> Creature:
     """Draw a creature from ``default_rng(seed)``.
 
     radius: (lo, hi) for R_k; default scales (12, 30) px at 1024^2 with n.
     seed_box: side of the central square seeded with U[0,1] (clipped to n/2).
+    device: if given (a torch device), the kernel spectra are computed there
+    with torch in float64 instead of numpy (same draws, same math).
     """
     rng = np.random.default_rng(seed)
     if c0 is None or c1 is None:
@@ -122,7 +144,10 @@ def make_creature(n: int, C: int = 3, *, seed: int = 0, K: int | None = None,
         b = rng.uniform(0.0, 1.0, size=B)
         b[rng.integers(0, B)] = max(b.max(), 0.25)   # never an all-zero kernel
         rings.append(b.tolist())
-        kspec[k] = np.fft.fft2(ring_kernel(n, R[k], b)).astype(np.complex64)
+        if device is not None:
+            kspec[k] = _kernel_spectrum_torch(n, R[k], b, device)
+        else:
+            kspec[k] = np.fft.fft2(ring_kernel(n, R[k], b)).astype(np.complex64)
     mu = rng.uniform(*mu_range, size=K).astype(np.float32)
     sigma = rng.uniform(*sigma_range, size=K).astype(np.float32)
     w = rng.uniform(0.0, 1.0, size=K)

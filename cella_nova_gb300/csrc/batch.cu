@@ -1,0 +1,661 @@
+// batch.cu — many DiffusionLenia worlds of uneven size, channel and kernel
+// count, advanced together: one persistent launch per phase, the whole step
+// captured in one CUDA graph per ping-pong parity.
+//
+// The reference runs one world per GpuMaceLenia (ml-rs/orchestrator/mod.rs)
+// and batches only in its PyTorch model, where every world shares one shape
+// (train/lenia_org.py:47, state (B,C,H,W)).  Here each phase's work (row
+// blocks, column tiles, diffusion tiles of every world and channel) is a list
+// of items; persistent CTAs take items from a counter, one item ahead, and
+// run the same per-size device bodies as the single-world kernels.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <type_traits>
+#include <vector>
+
+#include "cella_gpu.h"
+#include "cella_internal.h"
+#include "step_kernels.cuh"
+
+namespace cg {
+
+constexpr int kBatchMinLogN = 6;   // 64^2 .. 2048^2 in one batch
+constexpr int kBatchMaxLogN = 11;
+
+struct WorldDesc {
+    int logn, C, K;
+    float temp;
+    float* state[2];
+    float2* rowspec;
+    const float2* kspec;
+    float2* U;
+    float* A;
+    const float2* tw;
+    KernelGroups groups;
+    GrowthParams gp;
+};
+
+struct WorkItem {
+    int world, c, a, b;   // a, b: row/column offsets of the unit
+};
+
+// Size dispatch: one case per supported grid side.  Each case calls a
+// non-inlined per-size item function, so every size gets its own register
+// allocation (inlining all sizes into one loop made the compiler spill the
+// column pass's register-resident spectrum).
+#define CG_SIZE_SWITCH(logn, CALL)      \
+    switch (logn) {                     \
+        case 6: CALL(6); break;         \
+        case 7: CALL(7); break;         \
+        case 8: CALL(8); break;         \
+        case 9: CALL(9); break;         \
+        case 10: CALL(10); break;       \
+        default: CALL(11); break;       \
+    }
+
+template <int L>
+__device__ __noinline__ void item_r2c(const WorldDesc& w, const WorkItem& it, int parity,
+                                      float2* sm) {
+    row_r2c_body<L>(w.state[parity], w.rowspec, w.tw, it.c, it.a, sm);
+}
+template <int L>
+__device__ __noinline__ bool item_col(const WorldDesc& w, const WorkItem& it, float2* sm,
+                                      uint64_t* bar, uint32_t* phase, int* err) {
+    uint32_t ph = *phase;
+    const bool ok = col_conv_body<L>(w.rowspec, w.kspec, w.U, w.tw, w.groups, it.c, it.a, sm, bar,
+                                     ph, err);
+    *phase = ph;
+    return ok;
+}
+template <int L>
+__device__ __noinline__ void item_c2r(const WorldDesc& w, const WorkItem& it, float2* sm) {
+    row_c2r_growth_body<L>(w.U, w.A, w.tw, w.groups, w.gp, w.temp, nullptr, 0.f, it.c, it.a, sm);
+}
+template <int L>
+__device__ __noinline__ void item_diff(const WorldDesc& w, const WorkItem& it, int parity,
+                                       float* sm) {
+    diffusion_body<L>(w.A, w.state[parity], w.state[parity ^ 1], it.c, it.a, it.b, sm);
+}
+
+// Work queue with one item of lookahead: thread 0 claims the next item while
+// the block runs the current one, so the atomic's latency is hidden.
+struct Queue {
+    int* counter;
+    int count;
+    int* slot;   // shared
+    int ahead;   // thread 0 only
+
+    __device__ int first() {
+        if (threadIdx.x == 0) {
+            *slot = atomicAdd(counter, 1);
+            ahead = atomicAdd(counter, 1);
+        }
+        __syncthreads();
+        const int i = *slot;
+        __syncthreads();
+        return i;
+    }
+    __device__ int next() {
+        if (threadIdx.x == 0) {
+            *slot = ahead;
+            ahead = atomicAdd(counter, 1);
+        }
+        __syncthreads();
+        const int i = *slot;
+        __syncthreads();
+        return i;
+    }
+};
+
+__global__ void __launch_bounds__(512) kb_row_r2c(const WorldDesc* __restrict__ worlds,
+                                                   const WorkItem* __restrict__ items, int count,
+                                                   int* counter, int parity) {
+    extern __shared__ __align__(128) float2 smb_r2c[];
+    __shared__ int slot;
+    Queue q{counter, count, &slot, 0};
+    for (int i = q.first(); i < count; i = q.next()) {
+        const WorkItem it = items[i];
+        const WorldDesc& w = worlds[it.world];
+#define CALL(L) item_r2c<L>(w, it, parity, smb_r2c)
+        CG_SIZE_SWITCH(w.logn, CALL)
+#undef CALL
+    }
+}
+
+__global__ void __launch_bounds__(256, 2) kb_col_conv(const WorldDesc* __restrict__ worlds,
+                                                       const WorkItem* __restrict__ items,
+                                                       int count, int* counter, int* err) {
+    extern __shared__ __align__(128) float2 smb_col[];
+    __shared__ __align__(8) uint64_t bar;
+    __shared__ int slot;
+    __shared__ uint32_t phase;
+    init_tile_barrier(&bar);
+    if (threadIdx.x == 0) phase = 0;
+    __syncthreads();
+    bool ok = true;
+    Queue q{counter, count, &slot, 0};
+    for (int i = q.first(); i < count; i = q.next()) {
+        if (!ok) continue;   // drain the queue without touching memory
+        const WorkItem it = items[i];
+        const WorldDesc& w = worlds[it.world];
+#define CALL(L) ok = item_col<L>(w, it, smb_col, &bar, &phase, err)
+        CG_SIZE_SWITCH(w.logn, CALL)
+#undef CALL
+    }
+}
+
+__global__ void __launch_bounds__(512) kb_row_c2r_growth(const WorldDesc* __restrict__ worlds,
+                                                          const WorkItem* __restrict__ items,
+                                                          int count, int* counter) {
+    extern __shared__ __align__(128) float2 smb_c2r[];
+    __shared__ int slot;
+    Queue q{counter, count, &slot, 0};
+    for (int i = q.first(); i < count; i = q.next()) {
+        const WorkItem it = items[i];
+        const WorldDesc& w = worlds[it.world];
+#define CALL(L) item_c2r<L>(w, it, smb_c2r)
+        CG_SIZE_SWITCH(w.logn, CALL)
+#undef CALL
+    }
+}
+
+__global__ void __launch_bounds__(256) kb_diffusion(const WorldDesc* __restrict__ worlds,
+                                                     const WorkItem* __restrict__ items,
+                                                     int count, int* counter, int parity) {
+    extern __shared__ __align__(128) float smb_diff[];
+    __shared__ int slot;
+    Queue q{counter, count, &slot, 0};
+    for (int i = q.first(); i < count; i = q.next()) {
+        const WorkItem it = items[i];
+        const WorldDesc& w = worlds[it.world];
+#define CALL(L) item_diff<L>(w, it, parity, smb_diff)
+        CG_SIZE_SWITCH(w.logn, CALL)
+#undef CALL
+    }
+}
+
+// Per-size shared-memory needs (bytes) of the four phases.
+struct PhaseSmem {
+    size_t r2c, col, c2r, diff;
+};
+template <int LOGN>
+PhaseSmem phase_smem() {
+    using G = Geo<LOGN>;
+    return {G::R2C_SMEM, G::COL_SMEM, G::C2R_SMEM, DiffGeo<LOGN>::SMEM};
+}
+static PhaseSmem phase_smem_for(int logn) {
+    switch (logn) {
+        case 6: return phase_smem<6>();
+        case 7: return phase_smem<7>();
+        case 8: return phase_smem<8>();
+        case 9: return phase_smem<9>();
+        case 10: return phase_smem<10>();
+        default: return phase_smem<11>();
+    }
+}
+struct UnitGeo {
+    int RB, TW, TX, TY;
+};
+template <int LOGN>
+UnitGeo unit_geo() {
+    using G = Geo<LOGN>;
+    return {G::RB, G::TW, G::TX, G::TY};
+}
+static UnitGeo unit_geo_for(int logn) {
+    switch (logn) {
+        case 6: return unit_geo<6>();
+        case 7: return unit_geo<7>();
+        case 8: return unit_geo<8>();
+        case 9: return unit_geo<9>();
+        case 10: return unit_geo<10>();
+        default: return unit_geo<11>();
+    }
+}
+
+}  // namespace cg
+
+using namespace cg;
+
+struct cg_batch {
+    struct World {
+        int n = 0, logn = 0, C = 0, K = 0;
+        float temp = 1.f;
+        float* state[2] = {nullptr, nullptr};
+        float2* rowspec = nullptr;
+        float2* kspec = nullptr;
+        float2* U = nullptr;
+        float* A = nullptr;
+        KernelGroups groups{};
+        GrowthParams gp{};
+    };
+    std::vector<World> worlds;
+    std::vector<float2*> tw_by_logn = std::vector<float2*>(kMaxLogN + 1, nullptr);
+    WorldDesc* d_worlds = nullptr;
+    WorkItem* d_items[4] = {nullptr, nullptr, nullptr, nullptr};
+    int count[4] = {0, 0, 0, 0};
+    int grid[4] = {0, 0, 0, 0};
+    size_t smem[4] = {0, 0, 0, 0};
+    int* counters = nullptr;   // 4 ints, reset at the start of every step
+    int* err = nullptr;
+    void* staging = nullptr;
+    double* mass_partial = nullptr;
+    double* mass_out = nullptr;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    int cur = 0;
+    int device = 0;
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    size_t max_px = 0;
+};
+
+namespace {
+
+void batch_release(cg_batch* b) {
+    if (!b) return;
+    cudaSetDevice(b->device);
+    for (auto& g : b->graph)
+        if (g) cudaGraphExecDestroy(g);
+    for (auto& e : b->ev)
+        if (e) cudaEventDestroy(e);
+    for (auto& w : b->worlds) {
+        cudaFree(w.state[0]);
+        cudaFree(w.state[1]);
+        cudaFree(w.rowspec);
+        cudaFree(w.kspec);
+        cudaFree(w.U);
+        cudaFree(w.A);
+    }
+    for (auto p : b->tw_by_logn) cudaFree(p);
+    cudaFree(b->d_worlds);
+    for (auto p : b->d_items) cudaFree(p);
+    cudaFree(b->counters);
+    cudaFree(b->err);
+    cudaFree(b->staging);
+    cudaFree(b->mass_partial);
+    cudaFree(b->mass_out);
+    if (b->own_stream && b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+}
+
+cudaError_t launch_phase(cg_batch* b, int phase, int parity, cudaStream_t st) {
+    if (b->count[phase] == 0) return cudaSuccess;
+    int* ctr = b->counters + phase;
+    switch (phase) {
+        case 0:
+            kb_row_r2c<<<b->grid[0], 512, b->smem[0], st>>>(b->d_worlds, b->d_items[0],
+                                                            b->count[0], ctr, parity);
+            break;
+        case 1:
+            kb_col_conv<<<b->grid[1], 256, b->smem[1], st>>>(b->d_worlds, b->d_items[1],
+                                                             b->count[1], ctr, b->err);
+            break;
+        case 2:
+            kb_row_c2r_growth<<<b->grid[2], 512, b->smem[2], st>>>(b->d_worlds, b->d_items[2],
+                                                                   b->count[2], ctr);
+            break;
+        default:
+            kb_diffusion<<<b->grid[3], 256, b->smem[3], st>>>(b->d_worlds, b->d_items[3],
+                                                              b->count[3], ctr, parity);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t enqueue_step(cg_batch* b, int parity, cudaStream_t st) {
+    cudaError_t e = cudaMemsetAsync(b->counters, 0, 4 * sizeof(int), st);
+    for (int p = 0; p < 4 && e == cudaSuccess; ++p) e = launch_phase(b, p, parity, st);
+    return e;
+}
+
+int batch_sync_check(cg_batch* b) {
+    int h = 0;
+    cudaError_t e = cudaMemcpy(&h, b->err, sizeof(int), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(e, "reading error word");
+    if (h != 0) {
+        cudaMemset(b->err, 0, sizeof(int));
+        return fail(CG_ERR_TIMEOUT, "a device-side wait for an asynchronous copy timed out");
+    }
+    return CG_OK;
+}
+
+}  // namespace
+
+#define BCHECK(call, what)                                   \
+    do {                                                     \
+        cudaError_t e_ = (call);                             \
+        if (e_ != cudaSuccess) return cuda_fail(e_, what);   \
+    } while (0)
+
+extern "C" {
+
+int cg_batch_create(int n_worlds, const int* n, const int* C, const int* K, const uint32_t* c0,
+                    const uint32_t* c1, const float* mu, const float* sigma, const float* weights,
+                    const float* temp, cg_stream_t stream, cg_batch** out) {
+    if (!out) return fail(CG_ERR_ARG, "cg_batch_create: out is NULL");
+    *out = nullptr;
+    if (n_worlds < 1 || n_worlds > 4096)
+        return fail(CG_ERR_ARG, "world count %d outside [1, 4096]", n_worlds);
+    if (!n || !C || !K || !c0 || !c1 || !mu || !sigma || !weights || !temp)
+        return fail(CG_ERR_ARG, "cg_batch_create: NULL array");
+    cg_batch* b = new (std::nothrow) cg_batch;
+    if (!b) return fail(CG_ERR_OOM, "cg_batch_create: host allocation failed");
+    b->worlds.resize(n_worlds);
+    size_t koff = 0;
+    for (int w = 0; w < n_worlds; ++w) {
+        int logn = 0;
+        int rc = validate_world(n[w], C[w], K[w], c0 + koff, c1 + koff, mu + koff, sigma + koff,
+                                weights + koff, temp[w], &logn);
+        if (rc == CG_OK && logn < kBatchMinLogN) {
+            rc = fail(CG_ERR_UNSUPPORTED, "batched worlds need a grid side of at least %d",
+                      1 << kBatchMinLogN);
+        }
+        if (rc != CG_OK) {
+            char buf[600];
+            snprintf(buf, sizeof buf, "world %d: %s", w, cg_last_error());
+            delete b;
+            return fail(rc, "%s", buf);
+        }
+        auto& W = b->worlds[w];
+        W.n = n[w];
+        W.logn = logn;
+        W.C = C[w];
+        W.K = K[w];
+        W.temp = temp[w];
+        build_groups(W.C, W.K, c0 + koff, c1 + koff, mu + koff, sigma + koff, weights + koff,
+                     &W.groups, &W.gp);
+        koff += size_t(K[w]);
+        b->max_px = std::max(b->max_px, size_t(W.n) * W.n);
+    }
+
+    int rc = CG_OK;
+    auto chk = [&](cudaError_t e, const char* what) {
+        if (rc == CG_OK && e != cudaSuccess) rc = cuda_fail(e, what);
+        return rc == CG_OK;
+    };
+    chk(cudaGetDevice(&b->device), "cudaGetDevice");
+    if (rc == CG_OK) {
+        if (stream) {
+            b->stream = static_cast<cudaStream_t>(stream);
+        } else if (chk(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking),
+                       "cudaStreamCreate")) {
+            b->own_stream = true;
+        }
+    }
+    // per-world buffers and per-size twiddles
+    for (auto& W : b->worlds) {
+        if (rc != CG_OK) break;
+        const size_t px = size_t(W.n) * W.n, half = size_t(W.n / 2) * W.n;
+        chk(cudaMalloc(&W.state[0], sizeof(float) * W.C * px), "cudaMalloc(state)");
+        chk(cudaMalloc(&W.state[1], sizeof(float) * W.C * px), "cudaMalloc(state)");
+        chk(cudaMalloc(&W.rowspec, sizeof(float2) * W.C * half), "cudaMalloc(rowspec)");
+        chk(cudaMalloc(&W.kspec, sizeof(float2) * W.K * (half + W.n)), "cudaMalloc(kspec)");
+        chk(cudaMalloc(&W.U, sizeof(float2) * W.K * half), "cudaMalloc(U)");
+        chk(cudaMalloc(&W.A, sizeof(float) * W.C * px), "cudaMalloc(A)");
+        if (rc == CG_OK) {
+            chk(cudaMemsetAsync(W.state[0], 0, sizeof(float) * W.C * px, b->stream), "memset");
+            chk(cudaMemsetAsync(W.state[1], 0, sizeof(float) * W.C * px, b->stream), "memset");
+            chk(cudaMemsetAsync(W.kspec, 0, sizeof(float2) * W.K * (half + W.n), b->stream),
+                "memset");
+        }
+        if (rc == CG_OK && !b->tw_by_logn[W.logn]) {
+            const SizeOps* ops = size_ops(W.logn);
+            std::vector<float2> h(size_t(ops->twiddle_count()));
+            build_twiddle_tables(W.n, h.data());
+            if (chk(cudaMalloc(&b->tw_by_logn[W.logn], sizeof(float2) * h.size()),
+                    "cudaMalloc(twiddles)"))
+                chk(cudaMemcpy(b->tw_by_logn[W.logn], h.data(), sizeof(float2) * h.size(),
+                               cudaMemcpyHostToDevice),
+                    "uploading twiddles");
+            chk(ops->prepare(), "configuring kernels");
+        }
+    }
+    // descriptors
+    std::vector<WorldDesc> descs(n_worlds);
+    for (int w = 0; w < n_worlds && rc == CG_OK; ++w) {
+        const auto& W = b->worlds[w];
+        WorldDesc& d = descs[w];
+        d.logn = W.logn;
+        d.C = W.C;
+        d.K = W.K;
+        d.temp = W.temp;
+        d.state[0] = W.state[0];
+        d.state[1] = W.state[1];
+        d.rowspec = W.rowspec;
+        d.kspec = W.kspec;
+        d.U = W.U;
+        d.A = W.A;
+        d.tw = b->tw_by_logn[W.logn];
+        d.groups = W.groups;
+        d.gp = W.gp;
+    }
+    if (rc == CG_OK && chk(cudaMalloc(&b->d_worlds, sizeof(WorldDesc) * n_worlds), "cudaMalloc"))
+        chk(cudaMemcpy(b->d_worlds, descs.data(), sizeof(WorldDesc) * n_worlds,
+                       cudaMemcpyHostToDevice),
+            "uploading world descriptors");
+    // work lists, largest grids first so the queues end on small items
+    std::vector<int> order(n_worlds);
+    for (int w = 0; w < n_worlds; ++w) order[w] = w;
+    std::stable_sort(order.begin(), order.end(),
+                     [&](int a, int c) { return b->worlds[a].n > b->worlds[c].n; });
+    std::vector<WorkItem> lists[4];
+    PhaseSmem need{0, 0, 0, 0};
+    for (int w : order) {
+        const auto& W = b->worlds[w];
+        const UnitGeo g = unit_geo_for(W.logn);
+        const PhaseSmem ps = phase_smem_for(W.logn);
+        need.r2c = std::max(need.r2c, ps.r2c);
+        need.col = std::max(need.col, ps.col);
+        need.c2r = std::max(need.c2r, ps.c2r);
+        need.diff = std::max(need.diff, ps.diff);
+        for (int c = 0; c < W.C; ++c)
+            for (int y0 = 0; y0 < W.n; y0 += g.RB) lists[0].push_back({w, c, y0, 0});
+        for (int c = 0; c < W.C; ++c)
+            if (W.groups.in_count[c] > 0)
+                for (int x0 = 0; x0 < W.n / 2; x0 += g.TW) lists[1].push_back({w, c, x0, 0});
+        for (int c = 0; c < W.C; ++c)
+            for (int y0 = 0; y0 < W.n; y0 += g.RB) lists[2].push_back({w, c, y0, 0});
+        for (int c = 0; c < W.C; ++c)
+            for (int y0 = 0; y0 < W.n; y0 += g.TY)
+                for (int x0 = 0; x0 < W.n; x0 += g.TX) lists[3].push_back({w, c, x0, y0});
+    }
+    b->smem[0] = need.r2c;
+    b->smem[1] = need.col;
+    b->smem[2] = need.c2r;
+    b->smem[3] = need.diff;
+    for (int p = 0; p < 4 && rc == CG_OK; ++p) {
+        b->count[p] = int(lists[p].size());
+        if (chk(cudaMalloc(&b->d_items[p], sizeof(WorkItem) * std::max<size_t>(1, lists[p].size())),
+                "cudaMalloc(items)"))
+            chk(cudaMemcpy(b->d_items[p], lists[p].data(), sizeof(WorkItem) * lists[p].size(),
+                           cudaMemcpyHostToDevice),
+                "uploading work lists");
+    }
+    // persistent grids: as many CTAs as can be resident
+    if (rc == CG_OK) {
+        int sms = 0;
+        chk(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device), "attr");
+        const void* fns[4] = {reinterpret_cast<const void*>(kb_row_r2c),
+                              reinterpret_cast<const void*>(kb_col_conv),
+                              reinterpret_cast<const void*>(kb_row_c2r_growth),
+                              reinterpret_cast<const void*>(kb_diffusion)};
+        const int threads[4] = {512, 256, 512, 256};
+        for (int p = 0; p < 4 && rc == CG_OK; ++p) {
+            chk(cudaFuncSetAttribute(fns[p], cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     int(b->smem[p])),
+                "cudaFuncSetAttribute");
+            int per_sm = 0;
+            chk(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fns[p], threads[p],
+                                                              b->smem[p]),
+                "occupancy");
+            b->grid[p] = std::max(1, std::min(per_sm * sms, std::max(1, b->count[p])));
+        }
+    }
+    if (rc == CG_OK) chk(cudaMalloc(&b->counters, 4 * sizeof(int)), "cudaMalloc(counters)");
+    if (rc == CG_OK) chk(cudaMalloc(&b->err, sizeof(int)), "cudaMalloc(err)");
+    if (rc == CG_OK) chk(cudaMemset(b->err, 0, sizeof(int)), "memset(err)");
+    if (rc == CG_OK) chk(cudaMalloc(&b->staging, sizeof(double) * b->max_px), "cudaMalloc(staging)");
+    if (rc == CG_OK)
+        chk(cudaMalloc(&b->mass_partial, sizeof(double) * kMaxC * kMassBlocks), "cudaMalloc(mass)");
+    if (rc == CG_OK) chk(cudaMalloc(&b->mass_out, sizeof(double) * kMaxC), "cudaMalloc(mass)");
+    for (int i = 0; i < 5 && rc == CG_OK; ++i) chk(cudaEventCreate(&b->ev[i]), "cudaEventCreate");
+    // graphs
+    if (rc == CG_OK) {
+        cudaStream_t cap;
+        if (chk(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking), "cudaStreamCreate")) {
+            for (int p = 0; p < 2 && rc == CG_OK; ++p) {
+                cudaGraph_t g = nullptr;
+                cudaError_t e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
+                if (e == cudaSuccess) {
+                    cudaError_t le = enqueue_step(b, p, cap);
+                    e = cudaStreamEndCapture(cap, &g);
+                    if (le != cudaSuccess) e = le;
+                }
+                if (e == cudaSuccess) e = cudaGraphInstantiate(&b->graph[p], g, 0);
+                if (g) cudaGraphDestroy(g);
+                chk(e, "capturing the batched step graph");
+            }
+            cudaStreamDestroy(cap);
+        }
+    }
+    if (rc == CG_OK) chk(cudaStreamSynchronize(b->stream), "cudaStreamSynchronize");
+    if (rc != CG_OK) {
+        batch_release(b);
+        return rc;
+    }
+    *out = b;
+    return CG_OK;
+}
+
+int cg_batch_destroy(cg_batch* b) {
+    if (!b) return fail(CG_ERR_ARG, "cg_batch_destroy: NULL handle");
+    cudaSetDevice(b->device);
+    cudaStreamSynchronize(b->stream);
+    batch_release(b);
+    return CG_OK;
+}
+
+static int world_check(cg_batch* b, int w) {
+    if (!b) return fail(CG_ERR_ARG, "NULL batch handle");
+    if (w < 0 || w >= int(b->worlds.size()))
+        return fail(CG_ERR_ARG, "world index %d outside [0, %zu)", w, b->worlds.size());
+    return CG_OK;
+}
+
+int cg_batch_set_kernel(cg_batch* b, int world, int k, const float* spec) {
+    int rc = world_check(b, world);
+    if (rc != CG_OK) return rc;
+    auto& W = b->worlds[world];
+    if (!spec) return fail(CG_ERR_ARG, "cg_batch_set_kernel: NULL spectrum");
+    if (k < 0 || k >= W.K) return fail(CG_ERR_ARG, "kernel index %d outside [0, %d)", k, W.K);
+    const size_t px = size_t(W.n) * W.n, half = size_t(W.n / 2) * W.n;
+    BCHECK(cudaMemcpyAsync(b->staging, spec, sizeof(float2) * px, cudaMemcpyHostToDevice,
+                           b->stream),
+           "uploading kernel spectrum");
+    BCHECK(size_ops(W.logn)->pack(static_cast<const float2*>(b->staging),
+                                  W.kspec + size_t(k) * (half + W.n), b->stream),
+           "packing kernel spectrum");
+    return CG_OK;
+}
+
+int cg_batch_upload_channel(cg_batch* b, int world, int c, const double* data) {
+    int rc = world_check(b, world);
+    if (rc != CG_OK) return rc;
+    auto& W = b->worlds[world];
+    if (!data) return fail(CG_ERR_ARG, "cg_batch_upload_channel: NULL data");
+    if (c < 0 || c >= W.C) return fail(CG_ERR_ARG, "channel index %d outside [0, %d)", c, W.C);
+    const size_t px = size_t(W.n) * W.n;
+    BCHECK(cudaMemcpyAsync(b->staging, data, sizeof(double) * px, cudaMemcpyHostToDevice,
+                           b->stream),
+           "uploading channel");
+    BCHECK(launch_f64_to_f32(static_cast<const double*>(b->staging),
+                             W.state[b->cur] + size_t(c) * px, px, b->stream),
+           "converting channel");
+    return CG_OK;
+}
+
+int cg_batch_step(cg_batch* b, int nsteps) {
+    if (!b) return fail(CG_ERR_ARG, "cg_batch_step: NULL handle");
+    if (nsteps < 0) return fail(CG_ERR_ARG, "negative step count %d", nsteps);
+    for (int i = 0; i < nsteps; ++i) {
+        BCHECK(cudaGraphLaunch(b->graph[b->cur], b->stream), "cudaGraphLaunch");
+        b->cur ^= 1;
+    }
+    return CG_OK;
+}
+
+int cg_batch_download_channels(cg_batch* b, int world, float* out) {
+    int rc = world_check(b, world);
+    if (rc != CG_OK) return rc;
+    if (!out) return fail(CG_ERR_ARG, "cg_batch_download_channels: NULL output");
+    auto& W = b->worlds[world];
+    BCHECK(cudaMemcpyAsync(out, W.state[b->cur], sizeof(float) * W.C * size_t(W.n) * W.n,
+                           cudaMemcpyDeviceToHost, b->stream),
+           "downloading channels");
+    BCHECK(cudaStreamSynchronize(b->stream), "cudaStreamSynchronize");
+    return batch_sync_check(b);
+}
+
+int cg_batch_mass_f64(cg_batch* b, int world, double* out) {
+    int rc = world_check(b, world);
+    if (rc != CG_OK) return rc;
+    if (!out) return fail(CG_ERR_ARG, "cg_batch_mass_f64: NULL output");
+    auto& W = b->worlds[world];
+    BCHECK(launch_mass_f64(W.state[b->cur], W.C, size_t(W.n) * W.n, b->mass_partial, kMassBlocks,
+                           b->mass_out, b->stream),
+           "mass reduction");
+    BCHECK(cudaMemcpyAsync(out, b->mass_out, sizeof(double) * W.C, cudaMemcpyDeviceToHost,
+                           b->stream),
+           "downloading masses");
+    BCHECK(cudaStreamSynchronize(b->stream), "cudaStreamSynchronize");
+    return batch_sync_check(b);
+}
+
+int cg_batch_synchronize(cg_batch* b) {
+    if (!b) return fail(CG_ERR_ARG, "cg_batch_synchronize: NULL handle");
+    BCHECK(cudaStreamSynchronize(b->stream), "cudaStreamSynchronize");
+    return batch_sync_check(b);
+}
+
+int cg_batch_profile(cg_batch* b, int nsteps, double ms[4]) {
+    if (!b || !ms) return fail(CG_ERR_ARG, "cg_batch_profile: NULL argument");
+    if (nsteps < 1 || nsteps > 1024) return fail(CG_ERR_ARG, "nsteps %d outside [1, 1024]", nsteps);
+    double acc[4] = {0, 0, 0, 0};
+    for (int i = 0; i < nsteps; ++i) {
+        BCHECK(cudaMemsetAsync(b->counters, 0, 4 * sizeof(int), b->stream), "memset");
+        BCHECK(cudaEventRecord(b->ev[0], b->stream), "cudaEventRecord");
+        for (int p = 0; p < 4; ++p) {
+            BCHECK(launch_phase(b, p, b->cur, b->stream), "launching a phase");
+            BCHECK(cudaEventRecord(b->ev[p + 1], b->stream), "cudaEventRecord");
+        }
+        BCHECK(cudaEventSynchronize(b->ev[4]), "cudaEventSynchronize");
+        for (int p = 0; p < 4; ++p) {
+            float t = 0.f;
+            BCHECK(cudaEventElapsedTime(&t, b->ev[p], b->ev[p + 1]), "cudaEventElapsedTime");
+            acc[p] += t;
+        }
+        b->cur ^= 1;
+    }
+    for (int p = 0; p < 4; ++p) ms[p] = acc[p] / nsteps;
+    return batch_sync_check(b);
+}
+
+int cg_batch_stream(cg_batch* b, cg_stream_t* out) {
+    if (!b || !out) return fail(CG_ERR_ARG, "cg_batch_stream: NULL argument");
+    *out = b->stream;
+    return CG_OK;
+}
+
+int cg_batch_info(cg_batch* b, int* items4, int* grid4) {
+    if (!b) return fail(CG_ERR_ARG, "cg_batch_info: NULL handle");
+    for (int p = 0; p < 4; ++p) {
+        if (items4) items4[p] = b->count[p];
+        if (grid4) grid4[p] = b->grid[p];
+    }
+    return CG_OK;
+}
+
+}  // extern "C"

@@ -79,6 +79,19 @@ struct SizeOps {
 // Fill the twiddle buffer of an n-point grid (host side, double precision).
 void build_twiddle_tables(int n, float2* out);
 
+// Status helpers shared by the C ABI translation units (host.cu).
+int fail(int code, const char* fmt, ...);
+int cuda_fail(cudaError_t e, const char* what);
+
+// Argument checks of one world (cg_create / cg_batch_create); sets *logn.
+int validate_world(int n, int C, int K, const uint32_t* c0, const uint32_t* c1, const float* mu,
+                   const float* sigma, const float* weights, float temp, int* logn_out);
+
+// Kernel groups and pre-scaled growth parameters from the per-kernel maps
+// (host.cu); used by the single-world and the batched paths alike.
+void build_groups(int C, int K, const uint32_t* c0, const uint32_t* c1, const float* mu,
+                  const float* sigma, const float* weights, KernelGroups* g, GrowthParams* gp);
+
 const SizeOps* size_ops(int logn);
 
 // Size-independent kernels (kernels_common.cu).

@@ -98,6 +98,64 @@ void build_twiddle_tables(int n, float2* out) {
     fill_plan(n / 2, false, p);
 }
 
+static bool finite(float v) { return std::isfinite(v); }
+
+int validate_world(int n, int C, int K, const uint32_t* c0, const uint32_t* c1, const float* mu,
+                   const float* sigma, const float* weights, float temp, int* logn_out) {
+    int logn = 0;
+    while ((1 << logn) < n && logn < 30) ++logn;
+    if (n <= 0 || (1 << logn) != n)
+        return fail(CG_ERR_ARG, "grid side %d is not a power of two", n);
+    if (logn < kMinLogN || logn > kMaxLogN)
+        return fail(CG_ERR_UNSUPPORTED, "grid side %d outside [%d, %d]", n, 1 << kMinLogN,
+                    1 << kMaxLogN);
+    if (C < 1 || C > kMaxC) return fail(CG_ERR_ARG, "channel count %d outside [1, %d]", C, kMaxC);
+    if (K < 1 || K > kMaxK) return fail(CG_ERR_ARG, "kernel count %d outside [1, %d]", K, kMaxK);
+    if (!c0 || !c1 || !mu || !sigma || !weights)
+        return fail(CG_ERR_ARG, "NULL parameter array");
+    for (int k = 0; k < K; ++k) {
+        if (c0[k] >= uint32_t(C) || c1[k] >= uint32_t(C))
+            return fail(CG_ERR_ARG, "kernel %d maps channel %u -> %u, but C = %d", k, c0[k],
+                        c1[k], C);
+        if (!finite(mu[k]) || !finite(sigma[k]) || !finite(weights[k]) || sigma[k] == 0.f)
+            return fail(CG_ERR_ARG, "kernel %d has a non-finite or zero-sigma growth parameter",
+                        k);
+    }
+    if (!finite(temp)) return fail(CG_ERR_ARG, "temp is not finite");
+    *logn_out = logn;
+    return CG_OK;
+}
+
+void build_groups(int C, int K, const uint32_t* c0, const uint32_t* c1, const float* mu,
+                  const float* sigma, const float* weights, KernelGroups* g, GrowthParams* gp) {
+    *g = KernelGroups{};
+    *gp = GrowthParams{};
+    int pos = 0;
+    for (int c = 0; c < C; ++c) {   // in increasing k within each channel
+        g->in_start[c] = pos;
+        for (int k = 0; k < K; ++k)
+            if (int(c0[k]) == c) g->in_idx[pos++] = k;
+        g->in_count[c] = pos - g->in_start[c];
+    }
+    pos = 0;
+    for (int c = 0; c < C; ++c) {
+        g->out_start[c] = pos;
+        for (int k = 0; k < K; ++k)
+            if (int(c1[k]) == c) g->out_idx[pos++] = k;
+        g->out_count[c] = pos - g->out_start[c];
+    }
+    for (int k = 0; k < K; ++k) {
+        gp->mu[k] = mu[k];
+        gp->c2[k] = float(-1.4426950408889634 / (2.0 * double(sigma[k]) * double(sigma[k])));
+        gp->w2[k] = 2.0f * weights[k];
+    }
+    for (int c = 0; c < C; ++c) {
+        float ws = 0.f;   // f32, increasing k: the reference's sum of w * (-1)
+        for (int i = 0; i < g->out_count[c]; ++i) ws += weights[g->out_idx[g->out_start[c] + i]];
+        gp->wsum[c] = ws;
+    }
+}
+
 }  // namespace cg
 
 using namespace cg;
@@ -203,7 +261,6 @@ int build_twiddles(cg_sim* s) {
     return CG_OK;
 }
 
-bool finite(float v) { return std::isfinite(v); }
 
 // After a synchronisation: report (and clear) a device-side wait timeout.
 int check_device_error(cg_sim* s) {
@@ -237,25 +294,8 @@ int cg_create(int n, int C, int K, const uint32_t* c0, const uint32_t* c1, const
     if (!out) return fail(CG_ERR_ARG, "cg_create: out is NULL");
     *out = nullptr;
     int logn = 0;
-    while ((1 << logn) < n && logn < 30) ++logn;
-    if (n <= 0 || (1 << logn) != n)
-        return fail(CG_ERR_ARG, "grid side %d is not a power of two", n);
-    if (logn < kMinLogN || logn > kMaxLogN)
-        return fail(CG_ERR_UNSUPPORTED, "grid side %d outside [%d, %d]", n, 1 << kMinLogN,
-                    1 << kMaxLogN);
-    if (C < 1 || C > kMaxC) return fail(CG_ERR_ARG, "channel count %d outside [1, %d]", C, kMaxC);
-    if (K < 1 || K > kMaxK) return fail(CG_ERR_ARG, "kernel count %d outside [1, %d]", K, kMaxK);
-    if (!c0 || !c1 || !mu || !sigma || !weights)
-        return fail(CG_ERR_ARG, "cg_create: NULL parameter array");
-    for (int k = 0; k < K; ++k) {
-        if (c0[k] >= uint32_t(C) || c1[k] >= uint32_t(C))
-            return fail(CG_ERR_ARG, "kernel %d maps channel %u -> %u, but C = %d", k, c0[k],
-                        c1[k], C);
-        if (!finite(mu[k]) || !finite(sigma[k]) || !finite(weights[k]) || sigma[k] == 0.f)
-            return fail(CG_ERR_ARG, "kernel %d has a non-finite or zero-sigma growth parameter",
-                        k);
-    }
-    if (!finite(temp)) return fail(CG_ERR_ARG, "temp is not finite");
+    int rc0 = validate_world(n, C, K, c0, c1, mu, sigma, weights, temp, &logn);
+    if (rc0 != CG_OK) return rc0;
 
     cg_sim* s = new (std::nothrow) cg_sim;
     if (!s) return fail(CG_ERR_OOM, "cg_create: host allocation failed");
@@ -271,32 +311,7 @@ int cg_create(int n, int C, int K, const uint32_t* c0, const uint32_t* c1, const
     s->w.assign(weights, weights + K);
     s->ops = size_ops(logn);
 
-    // Groups, in increasing k within each channel.
-    int pos = 0;
-    for (int c = 0; c < C; ++c) {
-        s->groups.in_start[c] = pos;
-        for (int k = 0; k < K; ++k)
-            if (int(c0[k]) == c) s->groups.in_idx[pos++] = k;
-        s->groups.in_count[c] = pos - s->groups.in_start[c];
-    }
-    pos = 0;
-    for (int c = 0; c < C; ++c) {
-        s->groups.out_start[c] = pos;
-        for (int k = 0; k < K; ++k)
-            if (int(c1[k]) == c) s->groups.out_idx[pos++] = k;
-        s->groups.out_count[c] = pos - s->groups.out_start[c];
-    }
-    for (int k = 0; k < K; ++k) {
-        s->gp.mu[k] = mu[k];
-        s->gp.c2[k] = float(-1.4426950408889634 / (2.0 * double(sigma[k]) * double(sigma[k])));
-        s->gp.w2[k] = 2.0f * weights[k];
-    }
-    for (int c = 0; c < C; ++c) {
-        float ws = 0.f;   // f32, increasing k: the reference's sum of w * (-1)
-        for (int i = 0; i < s->groups.out_count[c]; ++i)
-            ws += weights[s->groups.out_idx[s->groups.out_start[c] + i]];
-        s->gp.wsum[c] = ws;
-    }
+    build_groups(C, K, c0, c1, mu, sigma, weights, &s->groups, &s->gp);
 
     int rc = CG_OK;
     auto chk = [&](cudaError_t e, const char* what) {

@@ -65,13 +65,11 @@ struct Geo {
 // grid (N/RB, C), block RT.
 // ---------------------------------------------------------------------------
 template <int LOGN>
-__global__ void __launch_bounds__(512) k_row_r2c(const float* __restrict__ state,
-                                                  float2* __restrict__ rowspec,
-                                                  const float2* __restrict__ tw) {
+__device__ __forceinline__ void row_r2c_body(const float* __restrict__ state,
+                                             float2* __restrict__ rowspec,
+                                             const float2* __restrict__ tw, int c, int y0,
+                                             float2* sm) {
     using G = Geo<LOGN>;
-    extern __shared__ __align__(16) float2 sm[];
-    const int c = blockIdx.y;
-    const int y0 = blockIdx.x * G::RB;
     const float2* src =
         reinterpret_cast<const float2*>(state + (size_t(c) * G::N + y0) * G::N);
     auto ld0 = [&](int s, int i, int, int) { return __ldg(&src[size_t(s) * G::M + i]); };
@@ -103,6 +101,14 @@ __global__ void __launch_bounds__(512) k_row_r2c(const float* __restrict__ state
         const int s = item % G::RB, kx = item / G::RB;
         dst[size_t(kx) * G::N + s] = sm[s * G::RP + pidx(kx)];
     }
+}
+
+template <int LOGN>
+__global__ void __launch_bounds__(512) k_row_r2c(const float* __restrict__ state,
+                                                  float2* __restrict__ rowspec,
+                                                  const float2* __restrict__ tw) {
+    extern __shared__ __align__(128) float2 sm_r2c[];
+    row_r2c_body<LOGN>(state, rowspec, tw, blockIdx.y, blockIdx.x * Geo<LOGN>::RB, sm_r2c);
 }
 
 // Run the first pass of a transform, then `hook()`, then the rest.
@@ -142,31 +148,26 @@ __device__ __forceinline__ void fft_with_hook(LD& ld, SMLD& smld, SMST& smst, ST
 // lives in another thread, so that tile swaps column 0 through W first.
 // grid (M/TW, C), block CT.
 // ---------------------------------------------------------------------------
+// Returns false if a bounded wait timed out (the error word is set).  `bar`
+// is an initialised mbarrier owned by the caller and `phase` counts its
+// completed phases, so one CTA can run many tiles back to back.
 template <int LOGN>
-__global__ void __launch_bounds__(256, 2) k_col_conv(const float2* __restrict__ rowspec,
-                                                      const float2* __restrict__ kspec,
-                                                      float2* __restrict__ U,
-                                                      const float2* __restrict__ tw,
-                                                      const KernelGroups groups, int* err) {
+__device__ __forceinline__ bool col_conv_body(const float2* __restrict__ rowspec,
+                                              const float2* __restrict__ kspec,
+                                              float2* __restrict__ U,
+                                              const float2* __restrict__ tw,
+                                              const KernelGroups& groups, int c, int kx0,
+                                              float2* sm, uint64_t* barp, uint32_t& phase,
+                                              int* err) {
     using G = Geo<LOGN>;
     constexpr int N = G::N, M = G::M, TW = G::TW, T = G::CT;
-    const int c = blockIdx.y;
     const int cnt = groups.in_count[c];
-    if (cnt == 0) return;
-    extern __shared__ __align__(128) float2 sm[];
+    if (cnt == 0) return true;
     float2* W = sm;
     float2* KS = sm + TW * G::CP;
-    __shared__ __align__(8) uint64_t bar;
-    const int kx0 = blockIdx.x * TW;
+    uint64_t& bar = *barp;
     const int base = groups.in_start[c];
     constexpr uint32_t kTileBytes = uint32_t(TW) * N * sizeof(float2);
-
-    if (threadIdx.x == 0) {
-        mbar_init(&bar, 1);
-        fence_barrier_init();
-    }
-    __syncthreads();
-    uint32_t phase = 0;
     auto issue = [&](const float2* src) {   // all threads call; thread 0 copies
         fence_proxy_async_smem();
         __syncthreads();
@@ -192,7 +193,7 @@ __global__ void __launch_bounds__(256, 2) k_col_conv(const float2* __restrict__ 
     };
 
     issue(rowspec + (size_t(c) * M + kx0) * N);
-    if (!wait_tile()) return;
+    if (!wait_tile()) return false;
 
     constexpr int RL = last_radix(N);
     static_assert(PassRadix<N, 1, true>::R == RL,
@@ -208,7 +209,7 @@ __global__ void __launch_bounds__(256, 2) k_col_conv(const float2* __restrict__ 
                                          [&]() { issue(kernel_tile(0)); });
 
     for (int gi = 0; gi < cnt; ++gi) {
-        if (!wait_tile()) return;
+        if (!wait_tile()) return false;
         if (kx0 == 0) {   // publish column 0 for the conj P(-ky) reads
 #pragma unroll
             for (int it = 0; it < IPTL; ++it) {
@@ -239,6 +240,31 @@ __global__ void __launch_bounds__(256, 2) k_col_conv(const float2* __restrict__ 
             if (gi + 1 < cnt) issue(kernel_tile(gi + 1));
         });
     }
+    return true;
+}
+
+__device__ __forceinline__ void init_tile_barrier(uint64_t* bar) {
+    if (threadIdx.x == 0) {
+        mbar_init(bar, 1);
+        fence_barrier_init();
+    }
+    __syncthreads();
+}
+
+template <int LOGN>
+__global__ void __launch_bounds__(256, 2) k_col_conv(const float2* __restrict__ rowspec,
+                                                      const float2* __restrict__ kspec,
+                                                      float2* __restrict__ U,
+                                                      const float2* __restrict__ tw,
+                                                      const __grid_constant__ KernelGroups groups,
+                                                      int* err) {
+    extern __shared__ __align__(128) float2 sm_col[];
+    __shared__ __align__(8) uint64_t bar;
+    if (groups.in_count[blockIdx.y] == 0) return;
+    init_tile_barrier(&bar);
+    uint32_t phase = 0;
+    col_conv_body<LOGN>(rowspec, kspec, U, tw, groups, blockIdx.y, blockIdx.x * Geo<LOGN>::TW,
+                        sm_col, &bar, phase, err);
 }
 
 // ---------------------------------------------------------------------------
@@ -257,17 +283,14 @@ __global__ void __launch_bounds__(256, 2) k_col_conv(const float2* __restrict__ 
 // grid (N/RB, C), block RT.
 // ---------------------------------------------------------------------------
 template <int LOGN>
-__global__ void __launch_bounds__(512) k_row_c2r_growth(const float2* __restrict__ U,
-                                                         float* __restrict__ A,
-                                                         const float2* __restrict__ tw,
-                                                         const KernelGroups groups,
-                                                         const GrowthParams gp, float temp,
-                                                         float* __restrict__ udbg,
-                                                         float udbg_scale) {
+__device__ __forceinline__ void row_c2r_growth_body(const float2* __restrict__ U,
+                                                    float* __restrict__ A,
+                                                    const float2* __restrict__ tw,
+                                                    const KernelGroups& groups,
+                                                    const GrowthParams& gp, float temp,
+                                                    float* __restrict__ udbg, float udbg_scale,
+                                                    int c, int y0, float2* sm) {
     using G = Geo<LOGN>;
-    extern __shared__ __align__(16) float2 sm[];
-    const int c = blockIdx.y;
-    const int y0 = blockIdx.x * G::RB;
     constexpr int RL = last_radix(G::M);
     constexpr int JL = G::M / RL;
     constexpr int ITEMS = G::RB * JL;
@@ -350,6 +373,19 @@ __global__ void __launch_bounds__(512) k_row_c2r_growth(const float2* __restrict
     }
 }
 
+template <int LOGN>
+__global__ void __launch_bounds__(512) k_row_c2r_growth(const float2* __restrict__ U,
+                                                         float* __restrict__ A,
+                                                         const float2* __restrict__ tw,
+                                                         const __grid_constant__ KernelGroups groups,
+                                                         const __grid_constant__ GrowthParams gp,
+                                                         float temp, float* __restrict__ udbg,
+                                                         float udbg_scale) {
+    extern __shared__ __align__(128) float2 sm_c2r[];
+    row_c2r_growth_body<LOGN>(U, A, tw, groups, gp, temp, udbg, udbg_scale, blockIdx.y,
+                              blockIdx.x * Geo<LOGN>::RB, sm_c2r);
+}
+
 // ---------------------------------------------------------------------------
 // Diffusion: Z = toroidal 3x3 sum of A, new = A * (3x3 sum of state / Z)
 // (example.rs:272-303, compute_1024.wgsl:341-413).  One channel tile per
@@ -388,17 +424,28 @@ __device__ __forceinline__ void for_tile(F fn) {
 }
 
 template <int LOGN>
-__global__ void __launch_bounds__(256) k_diffusion(const float* __restrict__ A,
-                                                    const float* __restrict__ x,
-                                                    float* __restrict__ out) {
+struct DiffGeo {
+    static constexpr int TX = Geo<LOGN>::TX, TY = Geo<LOGN>::TY;
+    static constexpr int AW = TX + 4, AH = TY + 4, HW = TX + 2, QH = TY + 2;
+    static constexpr size_t SMEM = size_t(2 * AH * AW + 2 * AH * HW + QH * HW) * sizeof(float);
+};
+
+template <int LOGN>
+__device__ __forceinline__ void diffusion_body(const float* __restrict__ A,
+                                               const float* __restrict__ x,
+                                               float* __restrict__ out, int c, int x0, int y0,
+                                               float* smf) {
     using G = Geo<LOGN>;
+    using D = DiffGeo<LOGN>;
     constexpr int N = G::N, TX = G::TX, TY = G::TY;
-    constexpr int AW = TX + 4, AH = TY + 4, HW = TX + 2, QH = TY + 2;
-    __shared__ float sAh[AH][AW], sAl[AH][AW], sHh[AH][HW], sHl[AH][HW], sQ[QH][HW];
-    float (*sQs)[TX] = reinterpret_cast<float (*)[TX]>(&sHh[0][0]);   // reuses sHh
+    constexpr int AW = D::AW, AH = D::AH, HW = D::HW, QH = D::QH;
+    auto sAh = reinterpret_cast<float (*)[AW]>(smf);
+    auto sAl = reinterpret_cast<float (*)[AW]>(smf + AH * AW);
+    auto sHh = reinterpret_cast<float (*)[HW]>(smf + 2 * AH * AW);
+    auto sHl = reinterpret_cast<float (*)[HW]>(smf + 2 * AH * AW + AH * HW);
+    auto sQ = reinterpret_cast<float (*)[HW]>(smf + 2 * AH * AW + 2 * AH * HW);
+    auto sQs = reinterpret_cast<float (*)[TX]>(smf + 2 * AH * AW);   // reuses sHh
     const int tx = threadIdx.x & 63, ty = threadIdx.x >> 6;
-    const int c = blockIdx.z;
-    const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
     const float* Ac = A + size_t(c) * N * N;
     const float* xc = x + size_t(c) * N * N;
 
@@ -487,6 +534,15 @@ __global__ void __launch_bounds__(256) k_diffusion(const float* __restrict__ A,
     });
 }
 
+template <int LOGN>
+__global__ void __launch_bounds__(256) k_diffusion(const float* __restrict__ A,
+                                                    const float* __restrict__ x,
+                                                    float* __restrict__ out) {
+    extern __shared__ __align__(128) float sm_diff[];
+    diffusion_body<LOGN>(A, x, out, blockIdx.z, blockIdx.x * Geo<LOGN>::TX,
+                         blockIdx.y * Geo<LOGN>::TY, sm_diff);
+}
+
 // ---------------------------------------------------------------------------
 // Kernel spectrum packing (set_kernel, mod.rs:207-214): full n x n spectrum
 // [ky][kx] -> Hermitian part, scaled by 1/(2 n^2), kx-major [kx][ky] for
@@ -528,6 +584,9 @@ cudaError_t prepare_size() {
                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   int(G::C2R_SMEM))) != cudaSuccess)
         return e;
+    if ((e = cudaFuncSetAttribute(k_diffusion<LOGN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  int(DiffGeo<LOGN>::SMEM))) != cudaSuccess)
+        return e;
     return cudaFuncSetAttribute(k_col_conv<LOGN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 int(G::COL_SMEM));
 }
@@ -545,8 +604,8 @@ cudaError_t launch_step(const StepArgs& a, int phases, cudaStream_t st) {
         k_row_c2r_growth<LOGN><<<dim3(G::N / G::RB, a.C), G::RT, G::C2R_SMEM, st>>>(
             a.U, a.A, a.tw, a.groups, a.gp, a.temp, a.udbg, float(G::N) * float(G::N));
     if (phases & kPhaseDiffusion)
-        k_diffusion<LOGN><<<dim3(G::N / G::TX, G::N / G::TY, a.C), 256, 0, st>>>(a.A, a.x_in,
-                                                                                 a.x_out);
+        k_diffusion<LOGN><<<dim3(G::N / G::TX, G::N / G::TY, a.C), 256, DiffGeo<LOGN>::SMEM,
+                            st>>>(a.A, a.x_in, a.x_out);
     return cudaGetLastError();
 }
 

@@ -234,3 +234,95 @@ def setup_simulation(config_path, kernels_path, temp=None, stream=None):
     for k in range(cfg["num_kernels"]):
         sim.set_kernel(ks[k], k)
     return sim
+
+
+class GpuMaceLeniaBatch:
+    """Many worlds of uneven grid side, channel and kernel count, stepped
+    together: each phase is one persistent launch over every world's work and
+    each step one CUDA graph.  World w behaves exactly like a
+    :class:`GpuMaceLenia` built from the same parameters."""
+
+    def __init__(self, creatures, stream=None):
+        self._lib = _abi.load()
+        self.creatures = list(creatures)
+        nw = len(self.creatures)
+        n = np.array([cr.n for cr in self.creatures], dtype=np.int32)
+        C = np.array([cr.C for cr in self.creatures], dtype=np.int32)
+        K = np.array([cr.K for cr in self.creatures], dtype=np.int32)
+        cat = lambda name, dt: np.ascontiguousarray(
+            np.concatenate([np.asarray(getattr(cr, name), dtype=dt) for cr in self.creatures]))
+        c0, c1 = cat("c0", np.uint32), cat("c1", np.uint32)
+        mu, sg, w = cat("mu", np.float32), cat("sigma", np.float32), cat("weights", np.float32)
+        temp = np.array([cr.temp for cr in self.creatures], dtype=np.float32)
+        ip = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
+        h = ctypes.c_void_p()
+        check(self._lib.cg_batch_create(nw, ip(n), ip(C), ip(K), uptr(c0), uptr(c1), fptr(mu),
+                                        fptr(sg), fptr(w), fptr(temp),
+                                        ctypes.c_void_p(stream) if stream else None,
+                                        ctypes.byref(h)))
+        self._h = h
+        for i, cr in enumerate(self.creatures):
+            for k in range(cr.K):
+                self.set_kernel(i, k, cr.kspec[k])
+            for c in range(cr.C):
+                a = np.ascontiguousarray(cr.seed[c], dtype=np.float64)
+                check(self._lib.cg_batch_upload_channel(self._h, i, c, dptr(a)))
+
+    def close(self):
+        if getattr(self, "_h", None):
+            check(self._lib.cg_batch_destroy(self._h))
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def set_kernel(self, world, k, spec):
+        a = np.asarray(spec).reshape(-1)
+        inter = np.empty((a.size, 2), dtype=np.float32)
+        inter[:, 0] = a.real
+        inter[:, 1] = a.imag
+        check(self._lib.cg_batch_set_kernel(self._h, int(world), int(k), fptr(inter)))
+
+    def run_steps(self, n):
+        check(self._lib.cg_batch_step(self._h, int(n)))
+
+    def synchronize(self):
+        check(self._lib.cg_batch_synchronize(self._h))
+
+    def state(self, world):
+        cr = self.creatures[world]
+        out = np.empty(cr.C * cr.n * cr.n, dtype=np.float32)
+        check(self._lib.cg_batch_download_channels(self._h, int(world), fptr(out)))
+        return out.reshape(cr.C, cr.n, cr.n)
+
+    def mass_f64(self, world):
+        out = np.zeros(self.creatures[world].C, dtype=np.float64)
+        check(self._lib.cg_batch_mass_f64(self._h, int(world), dptr(out)))
+        return out
+
+    def profile(self, nsteps):
+        """Average device ms per phase [row FFT, column conv, row inverse +
+        growth, diffusion] over nsteps steps."""
+        ms = np.zeros(4, dtype=np.float64)
+        check(self._lib.cg_batch_profile(self._h, int(nsteps), dptr(ms)))
+        return ms
+
+    def stream(self) -> int:
+        p = ctypes.c_void_p()
+        check(self._lib.cg_batch_stream(self._h, ctypes.byref(p)))
+        return p.value or 0
+
+    def info(self):
+        items = (ctypes.c_int * 4)()
+        grid = (ctypes.c_int * 4)()
+        check(self._lib.cg_batch_info(self._h, items, grid))
+        return list(items), list(grid)

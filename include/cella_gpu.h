@@ -155,6 +155,42 @@ int cg_stream(cg_sim* sim, cg_stream_t* out);
 int cg_synchronize(cg_sim* sim);
 
 /* ---------------------------------------------------------------------------
+ * Batched worlds (no reference counterpart beyond the PyTorch model's batch
+ * dimension, train/lenia_org.py:47; here worlds may differ in grid side,
+ * channel and kernel count)
+ * ------------------------------------------------------------------------- */
+
+typedef struct cg_batch cg_batch;
+
+/* n_worlds worlds; world w has grid side n[w] (64..2048), C[w] channels,
+ * K[w] kernels and temp[w].  c0/c1/mu/sigma/weights hold the worlds'
+ * per-kernel arrays back to back (world w starts at sum of K[0..w-1]).
+ * Each step is one CUDA graph: a persistent launch per phase over the work
+ * of every world. */
+int cg_batch_create(int n_worlds, const int* n, const int* C, const int* K,
+                    const uint32_t* c0, const uint32_t* c1, const float* mu,
+                    const float* sigma, const float* weights, const float* temp,
+                    cg_stream_t stream, cg_batch** out);
+int cg_batch_destroy(cg_batch* b);
+/* set_kernel / upload_channel of world `world` (mod.rs:207-226). */
+int cg_batch_set_kernel(cg_batch* b, int world, int k, const float* spec_interleaved);
+int cg_batch_upload_channel(cg_batch* b, int world, int c, const double* data);
+/* nsteps steps of every world (run_steps, mod.rs:229). */
+int cg_batch_step(cg_batch* b, int nsteps);
+int cg_batch_download_channels(cg_batch* b, int world, float* out);
+int cg_batch_mass_f64(cg_batch* b, int world, double* out);
+int cg_batch_synchronize(cg_batch* b);
+/* Average device ms per phase over nsteps steps (advances the state):
+ * [0] row FFT, [1] column convolution, [2] inverse row FFT + growth,
+ * [3] diffusion. */
+int cg_batch_profile(cg_batch* b, int nsteps, double ms[4]);
+/* The batch's stream. */
+int cg_batch_stream(cg_batch* b, cg_stream_t* out);
+/* Work items and persistent grid size per phase (either pointer may be
+ * NULL). */
+int cg_batch_info(cg_batch* b, int* items4, int* grid4);
+
+/* ---------------------------------------------------------------------------
  * File formats (ml-rs/config.rs)
  * ------------------------------------------------------------------------- */
 
