@@ -6,8 +6,9 @@
 // and batches only in its PyTorch model, where every world shares one shape
 // (train/lenia_org.py:47, state (B,C,H,W)).  Here each phase's work (row
 // blocks, column tiles, diffusion tiles of every world and channel) is a list
-// of items; persistent CTAs take items from a counter, one item ahead, and
-// run the same per-size device bodies as the single-world kernels.
+// of items; each phase is one persistent launch per grid size present, whose
+// resident CTAs stride through that size's items and run the same per-size
+// device bodies as the single-world kernels.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -43,138 +44,91 @@ struct WorkItem {
     int world, c, a, b;   // a, b: row/column offsets of the unit
 };
 
-// Size dispatch: one case per supported grid side.  Each case calls a
-// non-inlined per-size item function, so every size gets its own register
-// allocation (inlining all sizes into one loop made the compiler spill the
-// column pass's register-resident spectrum).
-#define CG_SIZE_SWITCH(logn, CALL)      \
-    switch (logn) {                     \
-        case 6: CALL(6); break;         \
-        case 7: CALL(7); break;         \
-        case 8: CALL(8); break;         \
-        case 9: CALL(9); break;         \
-        case 10: CALL(10); break;       \
-        default: CALL(11); break;       \
-    }
 
-template <int L>
-__device__ __noinline__ void item_r2c(const WorldDesc& w, const WorkItem& it, int parity,
-                                      float2* sm) {
-    row_r2c_body<L>(w.state[parity], w.rowspec, w.tw, it.c, it.a, sm);
-}
-template <int L>
-__device__ __noinline__ bool item_col(const WorldDesc& w, const WorkItem& it, float2* sm,
-                                      uint64_t* bar, uint32_t* phase, int* err) {
-    uint32_t ph = *phase;
-    const bool ok = col_conv_body<L>(w.rowspec, w.kspec, w.U, w.tw, w.groups, it.c, it.a, sm, bar,
-                                     ph, err);
-    *phase = ph;
-    return ok;
-}
-template <int L>
-__device__ __noinline__ void item_c2r(const WorldDesc& w, const WorkItem& it, float2* sm) {
-    row_c2r_growth_body<L>(w.U, w.A, w.tw, w.groups, w.gp, w.temp, nullptr, 0.f, it.c, it.a, sm);
-}
-template <int L>
-__device__ __noinline__ void item_diff(const WorldDesc& w, const WorkItem& it, int parity,
-                                       float* sm) {
-    diffusion_body<L>(w.A, w.state[parity], w.state[parity ^ 1], it.c, it.a, it.b, sm);
-}
-
-// Work queue with one item of lookahead: thread 0 claims the next item while
-// the block runs the current one, so the atomic's latency is hidden.
-struct Queue {
-    int* counter;
-    int count;
-    int* slot;   // shared
-    int ahead;   // thread 0 only
-
-    __device__ int first() {
-        if (threadIdx.x == 0) {
-            *slot = atomicAdd(counter, 1);
-            ahead = atomicAdd(counter, 1);
-        }
-        __syncthreads();
-        const int i = *slot;
-        __syncthreads();
-        return i;
-    }
-    __device__ int next() {
-        if (threadIdx.x == 0) {
-            *slot = ahead;
-            ahead = atomicAdd(counter, 1);
-        }
-        __syncthreads();
-        const int i = *slot;
-        __syncthreads();
-        return i;
-    }
-};
-
-__global__ void __launch_bounds__(512) kb_row_r2c(const WorldDesc* __restrict__ worlds,
+// One persistent kernel per phase and grid size: a kernel that served
+// several sizes made the compiler spill the column pass's register-resident
+// spectrum, so each size gets its own instantiation.  Within one size the
+// items cost about the same (sorted by cost, largest first), so each
+// resident CTA takes items blockIdx.x, blockIdx.x + gridDim.x, ...
+template <int LOGN>
+__global__ void __launch_bounds__(512, 2) kb_row_r2c(const WorldDesc* __restrict__ worlds,
                                                    const WorkItem* __restrict__ items, int count,
-                                                   int* counter, int parity) {
+                                                   int parity) {
     extern __shared__ __align__(128) float2 smb_r2c[];
-    __shared__ int slot;
-    Queue q{counter, count, &slot, 0};
-    for (int i = q.first(); i < count; i = q.next()) {
+    for (int i = blockIdx.x; i < count; i += gridDim.x) {
+        __syncthreads();
         const WorkItem it = items[i];
         const WorldDesc& w = worlds[it.world];
-#define CALL(L) item_r2c<L>(w, it, parity, smb_r2c)
-        CG_SIZE_SWITCH(w.logn, CALL)
-#undef CALL
+        row_r2c_body<LOGN>(w.state[parity], w.rowspec, w.tw, it.c, it.a, smb_r2c);
     }
 }
 
+template <int LOGN>
 __global__ void __launch_bounds__(256, 2) kb_col_conv(const WorldDesc* __restrict__ worlds,
                                                        const WorkItem* __restrict__ items,
-                                                       int count, int* counter, int* err) {
+                                                       int count, int* err) {
     extern __shared__ __align__(128) float2 smb_col[];
     __shared__ __align__(8) uint64_t bar;
-    __shared__ int slot;
-    __shared__ uint32_t phase;
     init_tile_barrier(&bar);
-    if (threadIdx.x == 0) phase = 0;
-    __syncthreads();
-    bool ok = true;
-    Queue q{counter, count, &slot, 0};
-    for (int i = q.first(); i < count; i = q.next()) {
-        if (!ok) continue;   // drain the queue without touching memory
+    uint32_t phase = 0;
+    for (int i = blockIdx.x; i < count; i += gridDim.x) {
+        __syncthreads();
         const WorkItem it = items[i];
         const WorldDesc& w = worlds[it.world];
-#define CALL(L) ok = item_col<L>(w, it, smb_col, &bar, &phase, err)
-        CG_SIZE_SWITCH(w.logn, CALL)
-#undef CALL
+        if (!col_conv_body<LOGN>(w.rowspec, w.kspec, w.U, w.tw, w.groups, it.c, it.a, smb_col,
+                                 &bar, phase, err))
+            return;   // a bounded wait timed out (uniform across the block)
     }
 }
 
+template <int LOGN>
 __global__ void __launch_bounds__(512) kb_row_c2r_growth(const WorldDesc* __restrict__ worlds,
                                                           const WorkItem* __restrict__ items,
-                                                          int count, int* counter) {
+                                                          int count) {
     extern __shared__ __align__(128) float2 smb_c2r[];
-    __shared__ int slot;
-    Queue q{counter, count, &slot, 0};
-    for (int i = q.first(); i < count; i = q.next()) {
+    for (int i = blockIdx.x; i < count; i += gridDim.x) {
+        __syncthreads();
         const WorkItem it = items[i];
         const WorldDesc& w = worlds[it.world];
-#define CALL(L) item_c2r<L>(w, it, smb_c2r)
-        CG_SIZE_SWITCH(w.logn, CALL)
-#undef CALL
+        row_c2r_growth_body<LOGN>(w.U, w.A, w.tw, w.groups, w.gp, w.temp, nullptr, 0.f, it.c,
+                                  it.a, smb_c2r);
     }
 }
 
+template <int LOGN>
 __global__ void __launch_bounds__(256) kb_diffusion(const WorldDesc* __restrict__ worlds,
                                                      const WorkItem* __restrict__ items,
-                                                     int count, int* counter, int parity) {
+                                                     int count, int parity) {
     extern __shared__ __align__(128) float smb_diff[];
-    __shared__ int slot;
-    Queue q{counter, count, &slot, 0};
-    for (int i = q.first(); i < count; i = q.next()) {
+    for (int i = blockIdx.x; i < count; i += gridDim.x) {
+        __syncthreads();
         const WorkItem it = items[i];
         const WorldDesc& w = worlds[it.world];
-#define CALL(L) item_diff<L>(w, it, parity, smb_diff)
-        CG_SIZE_SWITCH(w.logn, CALL)
-#undef CALL
+        diffusion_body<LOGN>(w.A, w.state[parity], w.state[parity ^ 1], it.c, it.a, it.b,
+                             smb_diff);
+    }
+}
+
+// The four persistent kernels of one size, as untyped pointers for the
+// occupancy query and the launches.
+struct PhaseFns {
+    const void* fn[4];
+};
+template <int LOGN>
+PhaseFns phase_fns() {
+    return {{reinterpret_cast<const void*>(kb_row_r2c<LOGN>),
+             reinterpret_cast<const void*>(kb_col_conv<LOGN>),
+             reinterpret_cast<const void*>(kb_row_c2r_growth<LOGN>),
+             reinterpret_cast<const void*>(kb_diffusion<LOGN>)}};
+}
+static PhaseFns phase_fns_for(int logn) {
+    switch (logn) {
+        case 6: return phase_fns<6>();
+        case 7: return phase_fns<7>();
+        case 8: return phase_fns<8>();
+        case 9: return phase_fns<9>();
+        case 10: return phase_fns<10>();
+        default: return phase_fns<11>();
     }
 }
 
@@ -232,14 +186,20 @@ struct cg_batch {
         KernelGroups groups{};
         GrowthParams gp{};
     };
+    // All worlds of one grid side: per phase a work list and a persistent
+    // grid.
+    struct SizeClass {
+        int logn = 0;
+        PhaseFns fns{};
+        WorkItem* d_items[4] = {nullptr, nullptr, nullptr, nullptr};
+        int count[4] = {0, 0, 0, 0};
+        int grid[4] = {0, 0, 0, 0};
+        size_t smem[4] = {0, 0, 0, 0};
+    };
     std::vector<World> worlds;
+    std::vector<SizeClass> classes;   // largest grid side first
     std::vector<float2*> tw_by_logn = std::vector<float2*>(kMaxLogN + 1, nullptr);
     WorldDesc* d_worlds = nullptr;
-    WorkItem* d_items[4] = {nullptr, nullptr, nullptr, nullptr};
-    int count[4] = {0, 0, 0, 0};
-    int grid[4] = {0, 0, 0, 0};
-    size_t smem[4] = {0, 0, 0, 0};
-    int* counters = nullptr;   // 4 ints, reset at the start of every step
     int* err = nullptr;
     void* staging = nullptr;
     double* mass_partial = nullptr;
@@ -271,9 +231,9 @@ void batch_release(cg_batch* b) {
         cudaFree(w.A);
     }
     for (auto p : b->tw_by_logn) cudaFree(p);
+    for (auto& sc : b->classes)
+        for (auto p : sc.d_items) cudaFree(p);
     cudaFree(b->d_worlds);
-    for (auto p : b->d_items) cudaFree(p);
-    cudaFree(b->counters);
     cudaFree(b->err);
     cudaFree(b->staging);
     cudaFree(b->mass_partial);
@@ -282,31 +242,30 @@ void batch_release(cg_batch* b) {
     delete b;
 }
 
+// One phase: a persistent launch per size class (largest first).
 cudaError_t launch_phase(cg_batch* b, int phase, int parity, cudaStream_t st) {
-    if (b->count[phase] == 0) return cudaSuccess;
-    int* ctr = b->counters + phase;
-    switch (phase) {
-        case 0:
-            kb_row_r2c<<<b->grid[0], 512, b->smem[0], st>>>(b->d_worlds, b->d_items[0],
-                                                            b->count[0], ctr, parity);
-            break;
-        case 1:
-            kb_col_conv<<<b->grid[1], 256, b->smem[1], st>>>(b->d_worlds, b->d_items[1],
-                                                             b->count[1], ctr, b->err);
-            break;
-        case 2:
-            kb_row_c2r_growth<<<b->grid[2], 512, b->smem[2], st>>>(b->d_worlds, b->d_items[2],
-                                                                   b->count[2], ctr);
-            break;
-        default:
-            kb_diffusion<<<b->grid[3], 256, b->smem[3], st>>>(b->d_worlds, b->d_items[3],
-                                                              b->count[3], ctr, parity);
+    static const unsigned threads[4] = {512, 256, 512, 256};
+    for (size_t i = 0; i < b->classes.size(); ++i) {
+        auto& sc = b->classes[i];
+        if (sc.count[phase] == 0) continue;
+        const WorldDesc* worlds = b->d_worlds;
+        const WorkItem* items = sc.d_items[phase];
+        int count = sc.count[phase];
+        void* args5[4];
+        args5[0] = &worlds;
+        args5[1] = &items;
+        args5[2] = &count;
+        if (phase == 1) args5[3] = &b->err;
+        else args5[3] = &parity;   // (the c2r kernel takes only three)
+        cudaError_t e = cudaLaunchKernel(sc.fns.fn[phase], dim3(sc.grid[phase]), dim3(threads[phase]),
+                                         args5, sc.smem[phase], st);
+        if (e != cudaSuccess) return e;
     }
     return cudaGetLastError();
 }
 
 cudaError_t enqueue_step(cg_batch* b, int parity, cudaStream_t st) {
-    cudaError_t e = cudaMemsetAsync(b->counters, 0, 4 * sizeof(int), st);
+    cudaError_t e = cudaSuccess;
     for (int p = 0; p < 4 && e == cudaSuccess; ++p) e = launch_phase(b, p, parity, st);
     return e;
 }
@@ -436,65 +395,53 @@ int cg_batch_create(int n_worlds, const int* n, const int* C, const int* K, cons
         chk(cudaMemcpy(b->d_worlds, descs.data(), sizeof(WorldDesc) * n_worlds,
                        cudaMemcpyHostToDevice),
             "uploading world descriptors");
-    // work lists, largest grids first so the queues end on small items
-    std::vector<int> order(n_worlds);
-    for (int w = 0; w < n_worlds; ++w) order[w] = w;
-    std::stable_sort(order.begin(), order.end(),
-                     [&](int a, int c) { return b->worlds[a].n > b->worlds[c].n; });
-    std::vector<WorkItem> lists[4];
-    PhaseSmem need{0, 0, 0, 0};
-    for (int w : order) {
-        const auto& W = b->worlds[w];
-        const UnitGeo g = unit_geo_for(W.logn);
-        const PhaseSmem ps = phase_smem_for(W.logn);
-        need.r2c = std::max(need.r2c, ps.r2c);
-        need.col = std::max(need.col, ps.col);
-        need.c2r = std::max(need.c2r, ps.c2r);
-        need.diff = std::max(need.diff, ps.diff);
-        for (int c = 0; c < W.C; ++c)
-            for (int y0 = 0; y0 < W.n; y0 += g.RB) lists[0].push_back({w, c, y0, 0});
-        for (int c = 0; c < W.C; ++c)
-            if (W.groups.in_count[c] > 0)
-                for (int x0 = 0; x0 < W.n / 2; x0 += g.TW) lists[1].push_back({w, c, x0, 0});
-        for (int c = 0; c < W.C; ++c)
-            for (int y0 = 0; y0 < W.n; y0 += g.RB) lists[2].push_back({w, c, y0, 0});
-        for (int c = 0; c < W.C; ++c)
-            for (int y0 = 0; y0 < W.n; y0 += g.TY)
-                for (int x0 = 0; x0 < W.n; x0 += g.TX) lists[3].push_back({w, c, x0, y0});
-    }
-    b->smem[0] = need.r2c;
-    b->smem[1] = need.col;
-    b->smem[2] = need.c2r;
-    b->smem[3] = need.diff;
-    for (int p = 0; p < 4 && rc == CG_OK; ++p) {
-        b->count[p] = int(lists[p].size());
-        if (chk(cudaMalloc(&b->d_items[p], sizeof(WorkItem) * std::max<size_t>(1, lists[p].size())),
-                "cudaMalloc(items)"))
-            chk(cudaMemcpy(b->d_items[p], lists[p].data(), sizeof(WorkItem) * lists[p].size(),
-                           cudaMemcpyHostToDevice),
-                "uploading work lists");
-    }
-    // persistent grids: as many CTAs as can be resident
-    if (rc == CG_OK) {
-        int sms = 0;
+    // size classes, largest first; per class and phase a work list
+    int sms = 0;
+    if (rc == CG_OK)
         chk(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device), "attr");
-        const void* fns[4] = {reinterpret_cast<const void*>(kb_row_r2c),
-                              reinterpret_cast<const void*>(kb_col_conv),
-                              reinterpret_cast<const void*>(kb_row_c2r_growth),
-                              reinterpret_cast<const void*>(kb_diffusion)};
+    for (int logn = kBatchMaxLogN; logn >= kBatchMinLogN && rc == CG_OK; --logn) {
+        std::vector<WorkItem> lists[4];
+        for (int w = 0; w < n_worlds; ++w) {
+            const auto& W = b->worlds[w];
+            if (W.logn != logn) continue;
+            const UnitGeo g = unit_geo_for(logn);
+            for (int c = 0; c < W.C; ++c)
+                for (int y0 = 0; y0 < W.n; y0 += g.RB) lists[0].push_back({w, c, y0, 0});
+            for (int c = 0; c < W.C; ++c)
+                if (W.groups.in_count[c] > 0)
+                    for (int x0 = 0; x0 < W.n / 2; x0 += g.TW) lists[1].push_back({w, c, x0, 0});
+            for (int c = 0; c < W.C; ++c)
+                for (int y0 = 0; y0 < W.n; y0 += g.RB) lists[2].push_back({w, c, y0, 0});
+            for (int c = 0; c < W.C; ++c)
+                for (int y0 = 0; y0 < W.n; y0 += g.TY)
+                    for (int x0 = 0; x0 < W.n; x0 += g.TX) lists[3].push_back({w, c, x0, y0});
+        }
+        if (lists[0].empty()) continue;
+        cg_batch::SizeClass sc;
+        sc.logn = logn;
+        sc.fns = phase_fns_for(logn);
+        const PhaseSmem ps = phase_smem_for(logn);
+        const size_t smem[4] = {ps.r2c, ps.col, ps.c2r, ps.diff};
         const int threads[4] = {512, 256, 512, 256};
         for (int p = 0; p < 4 && rc == CG_OK; ++p) {
-            chk(cudaFuncSetAttribute(fns[p], cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     int(b->smem[p])),
+            sc.count[p] = int(lists[p].size());
+            sc.smem[p] = smem[p];
+            if (chk(cudaMalloc(&sc.d_items[p], sizeof(WorkItem) * std::max<size_t>(1, lists[p].size())),
+                    "cudaMalloc(items)"))
+                chk(cudaMemcpy(sc.d_items[p], lists[p].data(), sizeof(WorkItem) * lists[p].size(),
+                               cudaMemcpyHostToDevice),
+                    "uploading work lists");
+            chk(cudaFuncSetAttribute(sc.fns.fn[p], cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     int(smem[p])),
                 "cudaFuncSetAttribute");
             int per_sm = 0;
-            chk(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fns[p], threads[p],
-                                                              b->smem[p]),
+            chk(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sc.fns.fn[p], threads[p],
+                                                              smem[p]),
                 "occupancy");
-            b->grid[p] = std::max(1, std::min(per_sm * sms, std::max(1, b->count[p])));
+            sc.grid[p] = std::max(1, std::min(per_sm * sms, std::max(1, sc.count[p])));
         }
+        b->classes.push_back(sc);
     }
-    if (rc == CG_OK) chk(cudaMalloc(&b->counters, 4 * sizeof(int)), "cudaMalloc(counters)");
     if (rc == CG_OK) chk(cudaMalloc(&b->err, sizeof(int)), "cudaMalloc(err)");
     if (rc == CG_OK) chk(cudaMemset(b->err, 0, sizeof(int)), "memset(err)");
     if (rc == CG_OK) chk(cudaMalloc(&b->staging, sizeof(double) * b->max_px), "cudaMalloc(staging)");
@@ -625,7 +572,6 @@ int cg_batch_profile(cg_batch* b, int nsteps, double ms[4]) {
     if (nsteps < 1 || nsteps > 1024) return fail(CG_ERR_ARG, "nsteps %d outside [1, 1024]", nsteps);
     double acc[4] = {0, 0, 0, 0};
     for (int i = 0; i < nsteps; ++i) {
-        BCHECK(cudaMemsetAsync(b->counters, 0, 4 * sizeof(int), b->stream), "memset");
         BCHECK(cudaEventRecord(b->ev[0], b->stream), "cudaEventRecord");
         for (int p = 0; p < 4; ++p) {
             BCHECK(launch_phase(b, p, b->cur, b->stream), "launching a phase");
@@ -652,8 +598,13 @@ int cg_batch_stream(cg_batch* b, cg_stream_t* out) {
 int cg_batch_info(cg_batch* b, int* items4, int* grid4) {
     if (!b) return fail(CG_ERR_ARG, "cg_batch_info: NULL handle");
     for (int p = 0; p < 4; ++p) {
-        if (items4) items4[p] = b->count[p];
-        if (grid4) grid4[p] = b->grid[p];
+        int items = 0, grid = 0;
+        for (auto& sc : b->classes) {
+            items += sc.count[p];
+            grid = std::max(grid, sc.grid[p]);
+        }
+        if (items4) items4[p] = items;
+        if (grid4) grid4[p] = grid;
     }
     return CG_OK;
 }

@@ -40,8 +40,10 @@ struct Geo {
     static constexpr size_t R2C_SMEM = size_t(RB) * RP * sizeof(float2);
     static constexpr size_t C2R_SMEM = 2 * R2C_SMEM;    // double-buffered input
     // Column kernel: TW columns per CTA, CT threads; a padded work buffer
-    // and an unpadded staging tile that bulk copies fill.
-    static constexpr int TW = 2;
+    // and an unpadded staging tile that bulk copies fill.  TW = 4096/N keeps
+    // 256 butterflies per radix-16 pass (one per thread) at every size.
+    static constexpr int TW0 = 4096 / N;
+    static constexpr int TW = TW0 < 2 ? 2 : (TW0 > M ? M : TW0);
     static constexpr int CT = 256;
     static constexpr int CP = padded_len(N) + 1;
     static constexpr size_t COL_SMEM = (size_t(TW) * CP + size_t(TW) * N) * sizeof(float2);
