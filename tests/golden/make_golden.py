@@ -11,8 +11,10 @@ over ``fft_kernel``.  Kernel k of the orchestrator API (input c0[k], output
 c1[k]) sits at ``fft_kernel[0, c0[k], c1[k]]`` — dim 1 is the channel that is
 transformed and summed over (lenia_org.py:131-134, diff_lenia_org.py:50).
 
-Two runs per fixture: float64 (the pin for the FP64 oracle) and float32 (the
-reference's own precision).  ``pyperlin`` (used only for random initial
+Two runs per trajectory fixture: float64 (the pin for the FP64 oracle) and
+float32 (the reference's own precision).  The grad_*.npz fixtures hold
+gradients of MSE(x_T, seed shifted by (+16, +8) px) from the model's own
+autograd in float64.  ``pyperlin`` (used only for random initial
 states, lenia_org.py:63-66) is replaced by an empty stub module because the
 state is always given.
 """
@@ -77,6 +79,51 @@ def run_reference(DL, cr, steps, dtype):
     return np.stack(states), aff1, w_used
 
 
+def reference_gradients(DL, cr, T, target):
+    """Gradients of MSE(x_T, target) through the reference model's own
+    autograd, w.r.t. the seed, mu, sigma and the (normalised) weights, which
+    are swapped for leaf tensors after construction (all float64)."""
+    import torch
+    C, n = cr.C, cr.n
+    dt = torch.float64
+    mu = np.zeros((1, C, C))
+    sg = np.ones((1, C, C))
+    w = np.zeros((1, C, C))
+    kf = torch.zeros((1, C, C, n, n), dtype=torch.complex128)
+    for k in range(cr.K):
+        i, o = int(cr.c0[k]), int(cr.c1[k])
+        mu[0, i, o] = cr.mu[k]
+        sg[0, i, o] = cr.sigma[k]
+        w[0, i, o] = cr.weights[k]
+        kf[0, i, o] = torch.from_numpy(cr.kspec[k].astype(np.complex128))
+    params = {"k_size": 5, "mu": torch.from_numpy(mu), "sigma": torch.from_numpy(sg),
+              "beta": torch.zeros((1, C, C, 3), dtype=dt), "mu_k": torch.zeros((1, C, C, 3), dtype=dt),
+              "sigma_k": torch.ones((1, C, C, 3), dtype=dt), "weights": torch.from_numpy(w)}
+    m = DL(size=(1, n, n), dt=0.2, num_channels=C, params=params,
+           state_init=torch.from_numpy(cr.seed[None]).to(dt), device="cpu")
+    seed_l = torch.from_numpy(cr.seed[None]).to(dt).requires_grad_(True)
+    mu_l = torch.from_numpy(mu).requires_grad_(True)
+    sg_l = torch.from_numpy(sg).requires_grad_(True)
+    w_l = torch.from_numpy(w).requires_grad_(True)
+    m.state, m.mu, m.sigma, m.weights = seed_l, mu_l, sg_l, w_l
+    m.fft_kernel = kf
+    m.temp = cr.temp
+    for _ in range(T):
+        m.step()
+    loss = torch.mean((m.state[0] - torch.from_numpy(target)) ** 2)
+    g = torch.autograd.grad(loss, [seed_l, mu_l, sg_l, w_l])
+    pick = lambda a: np.array([a[0, int(cr.c0[k]), int(cr.c1[k])] for k in range(cr.K)])
+    return (float(loss), g[0][0].numpy(), pick(g[1].numpy()), pick(g[2].numpy()),
+            pick(g[3].numpy()))
+
+
+GRAD_CASES = [
+    # name, n, C, T, temp, radius, rng seed
+    ("grad_c3k9_n32", 32, 3, 4, 1.0, (3.0, 7.0), 21),
+    ("grad_c2k4_n64", 64, 2, 3, 1.4, (4.0, 12.0), 22),
+]
+
+
 CASES = [
     # name, n, C, steps, temp, radius, rng seed
     ("c3k9_n32", 32, 3, 4, 1.0, (3.0, 7.0), 11),
@@ -102,6 +149,19 @@ def main(ref_root):
             states_f64=s64, aff1_f64=a64, states_f32=s32.astype(np.float32),
             aff1_f32=a32.astype(np.float32))
         print(f"wrote {path}: steps={steps}, mass0={cr.seed.sum(axis=(1, 2))}")
+    for name, n, C, T, temp, radius, seed in GRAD_CASES:
+        cr = make_creature(n, C, seed=seed, radius=radius, temp=temp, seed_box=n // 2)
+        target = np.roll(cr.seed, (8, 16), axis=(1, 2))
+        loss, gs, gm, gsg, gw = reference_gradients(DL, cr, T, target)
+        path = os.path.join(HERE, f"{name}.npz")
+        np.savez_compressed(
+            path, n=n, C=C, K=cr.K, T=T, temp=temp, seed=cr.seed, kspec=cr.kspec,
+            c0=cr.c0, c1=cr.c1, mu=cr.mu, sigma=cr.sigma, weights=cr.weights,
+            ring_radius=cr.ring_radius,
+            ring_w_flat=np.concatenate([np.asarray(b) for b in cr.ring_weights]),
+            ring_w_len=np.array([len(b) for b in cr.ring_weights]),
+            target=target, loss=loss, g_seed=gs, g_mu=gm, g_sigma=gsg, g_weights=gw)
+        print(f"wrote {path}: loss={loss:.6e}")
 
 
 if __name__ == "__main__":
