@@ -55,6 +55,13 @@ SIGNATURES = {
     "cg_destroy": ([_P], _I),
     "cg_set_kernel": ([_P, _I, _FP], _I),
     "cg_upload_channel": ([_P, _I, _DP], _I),
+    "cg_set_kernel_device": ([_P, _I, _P], _I),
+    "cg_set_params": ([_P, _FP, _FP, _FP, _F], _I),
+    "cg_step_from": ([_P, _P, _P], _I),
+    "cg_step_backward": ([_P, _P, _P, _P, _P, _P], _I),
+    "cg_kernel_grad_spatial": ([_P, _P, _P], _I),
+    "cg_unroll": ([_P, _P, _I, _I, _P, _P], _I),
+    "cg_unroll_backward": ([_P, _P, _I, _I, _P, _P, _P, _P, _P, _P], _I),
     "cg_upload_channel_f32": ([_P, _I, _FP], _I),
     "cg_iterate": ([_P], _I),
     "cg_step": ([_P, _I], _I),

@@ -54,6 +54,39 @@ struct StepArgs {
     GrowthParams gp;
 };
 
+// Per-kernel constants of the backward pass.
+struct AdjointParams {
+    int cout[kMaxK];       // c1[k]: the channel kernel k's growth feeds
+    float mu[kMaxK];
+    float w[kMaxK];
+    float inv_s2[kMaxK];   // 1 / sigma^2
+    float inv_s3[kMaxK];   // 1 / sigma^3
+};
+
+// Everything one backward step's launches need (adjoint.cuh).  Buffers of
+// the step (rowspec, U, A) are reused as scratch; x and ybar are read,
+// xbar and abar written; pgrad[3K] (d/dmu, d/dsigma, d/dw) and, if given,
+// kgrad[K][n/2][n] are accumulated.
+struct BwdArgs {
+    int C, K;
+    float temp;
+    const float* x;
+    const float* ybar;
+    float* xbar;
+    float* abar;
+    float2* rowspec;
+    const float2* kspec;
+    float2* U;
+    float* A;
+    const float2* tw;
+    double* pgrad;
+    float2* kgrad;
+    int* err;
+    KernelGroups groups;
+    GrowthParams gp;
+    AdjointParams ap;
+};
+
 // Phase bits for launch_step (timed_iterate splits the step into phases).
 enum : int {
     kPhaseRowFwd = 1,
@@ -68,12 +101,18 @@ typedef cudaError_t (*launch_step_fn)(const StepArgs&, int phases, cudaStream_t)
 typedef cudaError_t (*pack_kernel_fn)(const float2* full, float2* out, cudaStream_t);
 typedef cudaError_t (*prepare_fn)();
 typedef int (*twiddle_count_fn)();
+typedef cudaError_t (*launch_bwd_fn)(const BwdArgs&, cudaStream_t);
+typedef cudaError_t (*kgrad_final_fn)(float2* kgrad, float* hbar, int K, const float2* tw,
+                                      cudaStream_t);
 
 struct SizeOps {
     launch_step_fn step;
     pack_kernel_fn pack;
     prepare_fn prepare;
     twiddle_count_fn twiddle_count;   // float2 entries of the twiddle buffer
+    launch_bwd_fn backward;
+    kgrad_final_fn kgrad_final;
+    prepare_fn prepare_backward;
 };
 
 // Fill the twiddle buffer of an n-point grid (host side, double precision).

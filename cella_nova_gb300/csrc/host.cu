@@ -10,6 +10,7 @@
 // ping-pong parity, captured once at creation.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -184,6 +185,10 @@ struct cg_sim {
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     KernelGroups groups{};
     GrowthParams gp{};
+    AdjointParams ap{};
+    float* abar = nullptr;          // backward scratch, allocated on first use
+    float* utmp[2] = {nullptr, nullptr};   // cg_unroll scratch states
+    bool bwd_ready = false;
 
     size_t px() const { return size_t(n) * n; }
 
@@ -227,6 +232,9 @@ void release(cg_sim* s) {
     cudaFree(s->mass_partial);
     cudaFree(s->mass_out);
     cudaFree(s->err);
+    cudaFree(s->abar);
+    cudaFree(s->utmp[0]);
+    cudaFree(s->utmp[1]);
     if (s->own_stream && s->stream) cudaStreamDestroy(s->stream);
     delete s;
 }
@@ -280,6 +288,58 @@ int check_device_error(cg_sim* s) {
         if (rc_ != CG_OK) return rc_;                  \
     } while (0)
 
+void build_adjoint_params(cg_sim* s) {
+    for (int k = 0; k < s->K; ++k) {
+        const double sg = double(s->sigma[k]);
+        s->ap.cout[k] = int(s->c1[k]);
+        s->ap.mu[k] = s->mu[k];
+        s->ap.w[k] = s->w[k];
+        s->ap.inv_s2[k] = float(1.0 / (sg * sg));
+        s->ap.inv_s3[k] = float(1.0 / (sg * sg * sg));
+    }
+}
+
+int recapture(cg_sim* s) {
+    for (auto& g : s->graph)
+        if (g) {
+            cudaGraphExecDestroy(g);
+            g = nullptr;
+        }
+    return capture_graphs(s);
+}
+
+int ensure_backward(cg_sim* s) {
+    if (s->bwd_ready) return CG_OK;
+    CG_CHECK(s->ops->prepare_backward(), "configuring backward kernels");
+    CG_CHECK(cudaMalloc(&s->abar, sizeof(float) * s->C * s->px()), "cudaMalloc(abar)");
+    s->bwd_ready = true;
+    return CG_OK;
+}
+
+BwdArgs bwd_args(cg_sim* s, const float* x, const float* ybar, float* xbar, double* pgrad,
+                 float2* kgrad) {
+    BwdArgs a{};
+    a.C = s->C;
+    a.K = s->K;
+    a.temp = s->temp;
+    a.x = x;
+    a.ybar = ybar;
+    a.xbar = xbar;
+    a.abar = s->abar;
+    a.rowspec = s->rowspec;
+    a.kspec = s->kspec;
+    a.U = s->U;
+    a.A = s->A;
+    a.tw = s->tw;
+    a.pgrad = pgrad;
+    a.kgrad = kgrad;
+    a.err = s->err;
+    a.groups = s->groups;
+    a.gp = s->gp;
+    a.ap = s->ap;
+    return a;
+}
+
 }  // namespace
 
 extern "C" {
@@ -312,6 +372,7 @@ int cg_create(int n, int C, int K, const uint32_t* c0, const uint32_t* c1, const
     s->ops = size_ops(logn);
 
     build_groups(C, K, c0, c1, mu, sigma, weights, &s->groups, &s->gp);
+    build_adjoint_params(s);
 
     int rc = CG_OK;
     auto chk = [&](cudaError_t e, const char* what) {
@@ -378,6 +439,16 @@ int cg_set_kernel(cg_sim* s, int k, const float* spec) {
              "uploading kernel spectrum");
     CG_CHECK(s->ops->pack(static_cast<const float2*>(s->staging), s->kspec + size_t(k) * (half + s->n),
                           s->stream),
+             "packing kernel spectrum");
+    return CG_OK;
+}
+
+int cg_set_kernel_device(cg_sim* s, int k, const float* dev_spec) {
+    if (!s || !dev_spec) return fail(CG_ERR_ARG, "cg_set_kernel_device: NULL argument");
+    if (k < 0 || k >= s->K) return fail(CG_ERR_ARG, "kernel index %d outside [0, %d)", k, s->K);
+    const size_t half = size_t(s->n / 2) * s->n;
+    CG_CHECK(s->ops->pack(reinterpret_cast<const float2*>(dev_spec),
+                          s->kspec + size_t(k) * (half + s->n), s->stream),
              "packing kernel spectrum");
     return CG_OK;
 }
@@ -553,6 +624,110 @@ int cg_channel_ptr(cg_sim* s, float** p) {
 int cg_stream(cg_sim* s, cg_stream_t* out) {
     if (!s || !out) return fail(CG_ERR_ARG, "cg_stream: NULL argument");
     *out = s->stream;
+    return CG_OK;
+}
+
+int cg_set_params(cg_sim* s, const float* mu, const float* sigma, const float* weights,
+                  float temp) {
+    if (!s) return fail(CG_ERR_ARG, "cg_set_params: NULL handle");
+    int logn = 0;
+    int rc = validate_world(s->n, s->C, s->K, s->c0.data(), s->c1.data(), mu, sigma, weights,
+                            temp, &logn);
+    if (rc != CG_OK) return rc;
+    CG_CHECK(cudaStreamSynchronize(s->stream), "cudaStreamSynchronize");
+    s->mu.assign(mu, mu + s->K);
+    s->sigma.assign(sigma, sigma + s->K);
+    s->w.assign(weights, weights + s->K);
+    s->temp = temp;
+    build_groups(s->C, s->K, s->c0.data(), s->c1.data(), mu, sigma, weights, &s->groups, &s->gp);
+    build_adjoint_params(s);
+    return recapture(s);
+}
+
+int cg_step_from(cg_sim* s, const float* x_in, float* x_out) {
+    if (!s || !x_in || !x_out) return fail(CG_ERR_ARG, "cg_step_from: NULL argument");
+    if (x_in == x_out) return fail(CG_ERR_ARG, "cg_step_from: input and output must differ");
+    StepArgs a = s->args(s->cur, nullptr);
+    a.x_in = x_in;
+    a.x_out = x_out;
+    CG_CHECK(s->ops->step(a, kPhaseAll, s->stream), "launching a step");
+    return CG_OK;
+}
+
+int cg_step_backward(cg_sim* s, const float* x, const float* ybar, float* xbar, double* pgrad,
+                     float* kgrad) {
+    if (!s || !x || !ybar || !xbar || !pgrad)
+        return fail(CG_ERR_ARG, "cg_step_backward: NULL argument");
+    if (xbar == ybar || xbar == x)
+        return fail(CG_ERR_ARG, "cg_step_backward: xbar must not alias x or ybar");
+    int rc = ensure_backward(s);
+    if (rc != CG_OK) return rc;
+    CG_CHECK(s->ops->backward(bwd_args(s, x, ybar, xbar, pgrad, reinterpret_cast<float2*>(kgrad)),
+                              s->stream),
+             "launching a backward step");
+    return CG_OK;
+}
+
+int cg_kernel_grad_spatial(cg_sim* s, float* kgrad, float* hbar) {
+    if (!s || !kgrad || !hbar) return fail(CG_ERR_ARG, "cg_kernel_grad_spatial: NULL argument");
+    int rc = ensure_backward(s);
+    if (rc != CG_OK) return rc;
+    CG_CHECK(s->ops->kgrad_final(reinterpret_cast<float2*>(kgrad), hbar, s->K, s->tw, s->stream),
+             "finishing the kernel gradient");
+    return CG_OK;
+}
+
+int cg_unroll(cg_sim* s, const float* x0, int T, int every, float* ckpt, float* xT) {
+    if (!s || !x0 || !ckpt || !xT) return fail(CG_ERR_ARG, "cg_unroll: NULL argument");
+    if (T < 1 || every < 1) return fail(CG_ERR_ARG, "cg_unroll: T=%d, every=%d", T, every);
+    const size_t bytes = sizeof(float) * s->C * s->px();
+    const size_t plane = size_t(s->C) * s->px();
+    for (auto& p : s->utmp)
+        if (!p) CG_CHECK(cudaMalloc(&p, bytes), "cudaMalloc(unroll scratch)");
+    // checkpoint j holds x_{j*every}, j = 0 .. (T-1)/every
+    CG_CHECK(cudaMemcpyAsync(ckpt, x0, bytes, cudaMemcpyDeviceToDevice, s->stream), "checkpoint");
+    const float* cur = x0;
+    for (int t = 0; t < T; ++t) {
+        float* nxt;
+        if (t + 1 == T) nxt = xT;
+        else if ((t + 1) % every == 0) nxt = ckpt + plane * size_t((t + 1) / every);
+        else nxt = s->utmp[(t + 1) & 1];
+        int rc = cg_step_from(s, cur, nxt);
+        if (rc != CG_OK) return rc;
+        cur = nxt;
+    }
+    return CG_OK;
+}
+
+int cg_unroll_backward(cg_sim* s, const float* ckpt, int T, int every, const float* gT, float* g0,
+                       double* pgrad, float* kgrad, float* seg, float* gtmp) {
+    if (!s || !ckpt || !gT || !g0 || !pgrad || !seg || !gtmp)
+        return fail(CG_ERR_ARG, "cg_unroll_backward: NULL argument");
+    if (T < 1 || every < 1) return fail(CG_ERR_ARG, "cg_unroll_backward: T=%d, every=%d", T, every);
+    const size_t bytes = sizeof(float) * s->C * s->px();
+    const size_t plane = size_t(s->C) * s->px();
+    // gradient ping-pong between g0 and gtmp, arranged to end in g0
+    float* gb[2] = {(T % 2 == 0) ? g0 : gtmp, (T % 2 == 0) ? gtmp : g0};
+    CG_CHECK(cudaMemcpyAsync(gb[0], gT, bytes, cudaMemcpyDeviceToDevice, s->stream), "gradient");
+    int which = 0;
+    const int nseg = (T + every - 1) / every;
+    for (int j = nseg - 1; j >= 0; --j) {
+        const int t0 = j * every, t1 = std::min(T, t0 + every);
+        // recompute x_{t0} .. x_{t1-1} into seg
+        CG_CHECK(cudaMemcpyAsync(seg, ckpt + plane * size_t(j), bytes, cudaMemcpyDeviceToDevice,
+                                 s->stream),
+                 "segment");
+        for (int t = t0; t + 1 < t1; ++t) {
+            int rc = cg_step_from(s, seg + plane * size_t(t - t0), seg + plane * size_t(t - t0 + 1));
+            if (rc != CG_OK) return rc;
+        }
+        for (int t = t1 - 1; t >= t0; --t) {
+            int rc = cg_step_backward(s, seg + plane * size_t(t - t0), gb[which], gb[which ^ 1],
+                                      pgrad, kgrad);
+            if (rc != CG_OK) return rc;
+            which ^= 1;
+        }
+    }
     return CG_OK;
 }
 

@@ -1,3 +1,3 @@
 // Step kernels for grid side 2048.
-#include "step_kernels.cuh"
+#include "adjoint.cuh"
 CG_DEFINE_SIZE_OPS(11)

@@ -1,4 +1,4 @@
 // Step kernels for grid sides 512 and 1024.
-#include "step_kernels.cuh"
+#include "adjoint.cuh"
 CG_DEFINE_SIZE_OPS(9)
 CG_DEFINE_SIZE_OPS(10)

@@ -67,6 +67,10 @@ struct Geo {
 // grid (N/RB, C), block RT.
 // ---------------------------------------------------------------------------
 template <int LOGN>
+__device__ __forceinline__ void r2c_finish(float2* sm, const float2* __restrict__ tw,
+                                           float2* __restrict__ dst);
+
+template <int LOGN>
 __device__ __forceinline__ void row_r2c_body(const float* __restrict__ state,
                                              float2* __restrict__ rowspec,
                                              const float2* __restrict__ tw, int c, int y0,
@@ -78,7 +82,16 @@ __device__ __forceinline__ void row_r2c_body(const float* __restrict__ state,
     auto smld = [&](int s, int i, int, int) { return sm[s * G::RP + pidx(i)]; };
     auto smst = [&](int s, int i, float2 v, int, int) { sm[s * G::RP + pidx(i)] = v; };
     FftPasses<G::M, 1, false, G::RT, G::RB>::run(ld0, smld, smst, smst, tw + G::TW_ROW);
+    r2c_finish<LOGN>(sm, tw, rowspec + size_t(c) * G::M * G::N + y0);
+}
 
+// Even/odd split of RB transformed rows in shared memory (X[k] from Z[k],
+// Z[M-k]; X[0], X[M] packed in slot 0), then the kx-major transposed store
+// of the RB rows to dst[kx * N + s].
+template <int LOGN>
+__device__ __forceinline__ void r2c_finish(float2* sm, const float2* __restrict__ tw,
+                                           float2* __restrict__ dst) {
+    using G = Geo<LOGN>;
     constexpr int H = G::M / 2;
     for (int item = threadIdx.x; item < G::RB * (H + 1); item += G::RT) {
         const int s = item / (H + 1), k = item % (H + 1);
@@ -98,7 +111,6 @@ __device__ __forceinline__ void row_r2c_body(const float* __restrict__ state,
     }
     __syncthreads();
 
-    float2* dst = rowspec + size_t(c) * G::M * G::N + y0;
     for (int item = threadIdx.x; item < G::RB * G::M; item += G::RT) {
         const int s = item % G::RB, kx = item / G::RB;
         dst[size_t(kx) * G::N + s] = sm[s * G::RP + pidx(kx)];
@@ -626,9 +638,12 @@ cudaError_t launch_pack(const float2* full, float2* out, cudaStream_t st) {
 
 }  // namespace cg
 
-#define CG_DEFINE_SIZE_OPS(LOGN)                                                        \
-    namespace cg {                                                                      \
-    extern const SizeOps size_ops_l##LOGN;                                              \
-    const SizeOps size_ops_l##LOGN = {launch_step<LOGN>, launch_pack<LOGN>,             \
-                                      prepare_size<LOGN>, twiddle_count<LOGN>};         \
+// Per-size operation table (needs adjoint.cuh included before expansion).
+#define CG_DEFINE_SIZE_OPS(LOGN)                                                          \
+    namespace cg {                                                                        \
+    extern const SizeOps size_ops_l##LOGN;                                                \
+    const SizeOps size_ops_l##LOGN = {launch_step<LOGN>,      launch_pack<LOGN>,          \
+                                      prepare_size<LOGN>,     twiddle_count<LOGN>,        \
+                                      launch_backward<LOGN>,  launch_kgrad_final<LOGN>,   \
+                                      prepare_backward<LOGN>};                            \
     }

@@ -73,6 +73,10 @@ int cg_destroy(cg_sim* sim);
  * spectrum, interleaved (re, im) f32, row-major, origin at [0,0]. */
 int cg_set_kernel(cg_sim* sim, int k, const float* spec_interleaved);
 
+/* set_kernel from DEVICE memory: kernel k's full n*n complex spectrum,
+ * interleaved (re, im) f32, already on the GPU (no host round trip). */
+int cg_set_kernel_device(cg_sim* sim, int k, const float* dev_spec_interleaved);
+
 /* GpuMaceLenia::upload_channel, mod.rs:217-226: channel c from n*n doubles,
  * rounded to f32 (mod.rs:220 casts with `as f32`, round-to-nearest). */
 int cg_upload_channel(cg_sim* sim, int c, const double* data);
@@ -153,6 +157,44 @@ int cg_stream(cg_sim* sim, cg_stream_t* out);
 
 /* Device-side synchronisation of the handle's stream. */
 int cg_synchronize(cg_sim* sim);
+
+/* ---------------------------------------------------------------------------
+ * Differentiation (no counterpart in the Rust orchestrator; the reference
+ * differentiates its PyTorch model, train/diff_lenia_org.py, with autograd).
+ * All array arguments here are DEVICE pointers on the handle's device; work
+ * is enqueued on the handle's stream.
+ * ------------------------------------------------------------------------- */
+
+/* Replace mu/sigma/weights (K each) and temp; the step graphs are
+ * re-captured.  Same checks as cg_create. */
+int cg_set_params(cg_sim* sim, const float* mu, const float* sigma, const float* weights,
+                  float temp);
+
+/* One step from x_in to x_out (C*n*n f32 each, distinct). */
+int cg_step_from(cg_sim* sim, const float* x_in, float* x_out);
+
+/* Vector-Jacobian product of one step at state x: given ybar = dL/dx_next,
+ * writes xbar = dL/dx and ACCUMULATES pgrad[3K] (double: dL/dmu, dL/dsigma,
+ * dL/dweights) and, if kgrad is not NULL, kgrad (K*(n/2)*n complex f32, the
+ * packed kernel-gradient spectra; finish with cg_kernel_grad_spatial).
+ * xbar must not alias x or ybar. */
+int cg_step_backward(cg_sim* sim, const float* x, const float* ybar, float* xbar,
+                     double* pgrad, float* kgrad);
+
+/* hbar[K][n][n] = dL/dh_k for the spatial kernels h_k = Re IFFT(K_k), from
+ * the accumulated kgrad (which this overwrites). */
+int cg_kernel_grad_spatial(cg_sim* sim, float* kgrad, float* hbar);
+
+/* T steps from x0 to xT, storing x_{j*every} in ckpt[j], j = 0..(T-1)/every
+ * (ckpt holds (T-1)/every + 1 states). */
+int cg_unroll(cg_sim* sim, const float* x0, int T, int every, float* ckpt, float* xT);
+
+/* Gradients of an unroll stored by cg_unroll: from gT = dL/dx_T to
+ * g0 = dL/dx_0, recomputing each segment of `every` states from its
+ * checkpoint into seg (every*C*n*n f32); gtmp is one C*n*n scratch state.
+ * pgrad / kgrad accumulate as in cg_step_backward. */
+int cg_unroll_backward(cg_sim* sim, const float* ckpt, int T, int every, const float* gT,
+                       float* g0, double* pgrad, float* kgrad, float* seg, float* gtmp);
 
 /* ---------------------------------------------------------------------------
  * Batched worlds (no reference counterpart beyond the PyTorch model's batch
