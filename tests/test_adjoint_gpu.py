@@ -60,7 +60,7 @@ def test_single_step_vjp_matches_fp64():
     w.close()
 
 
-@pytest.mark.parametrize("n,C,T,every", [(64, 3, 6, 4), (128, 2, 9, 4)])
+@pytest.mark.parametrize("n,C,T,every", [(64, 3, 6, 4), (128, 2, 9, 4), (128, 3, 64, 8)])
 def test_unroll_gradients_match_fp64(n, C, T, every):
     cr = make_creature(n, C, seed=50 + n, radius=(n / 16, n / 6), seed_box=n // 2, temp=1.0)
     target = AR.shifted_target(cr.seed)
@@ -69,11 +69,13 @@ def test_unroll_gradients_match_fp64(n, C, T, every):
     xT = m(T, every)
     loss = torch.mean((xT - torch.tensor(target, dtype=torch.float32, device="cuda")) ** 2)
     loss.backward()
-    errs = {"loss": abs(float(loss) - ref["loss"]) / ref["loss"],
+    errs = {"loss": abs(float(loss.detach()) - ref["loss"]) / ref["loss"],
             "seed": rel(m.seed.grad.cpu(), ref["seed"]), "mu": rel(m.mu.grad.cpu(), ref["mu"]),
             "sigma": rel(m.sigma.grad.cpu(), ref["sigma"]),
             "weights": rel(m.weights.grad.cpu(), ref["weights"]),
-            "ring": max(rel(b.grad.cpu(), rb) for b, rb in zip(m.ring_weights, ref["ring_weights"]))}
+            # jointly: a one-ring kernel is invariant to its weight (gradient 0)
+            "ring": rel(np.concatenate([b.grad.cpu().numpy() for b in m.ring_weights]),
+                        np.concatenate(ref["ring_weights"]))}
     print(errs)
     assert max(errs.values()) < 2e-3, errs
 
