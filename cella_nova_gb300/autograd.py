@@ -40,7 +40,10 @@ class LeniaWorld:
         self.K = len(self.c0)
         self.temp = float(temp)
         with torch.cuda.device(self.device):
-            stream = torch.cuda.current_stream(self.device).cuda_stream
+            # bind to torch's current stream; its default stream is the legacy
+            # stream, handle 0, which the C ABI would read as "own stream",
+            # so pass cudaStreamLegacy (1) instead
+            stream = torch.cuda.current_stream(self.device).cuda_stream or 1
             one = np.ones(self.K, np.float32)
             h = ctypes.c_void_p()
             check(self.lib.cg_create(self.n, self.C, self.K, uptr(self.c0), uptr(self.c1),

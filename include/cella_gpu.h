@@ -46,7 +46,10 @@ typedef enum {
 } cg_status;
 
 typedef struct cg_sim cg_sim;
-typedef void* cg_stream_t; /* a cudaStream_t; NULL = the library's own stream */
+/* A cudaStream_t.  NULL = the library creates its own (non-blocking)
+ * stream; to run on the legacy default stream pass cudaStreamLegacy
+ * ((cg_stream_t)1). */
+typedef void* cg_stream_t;
 
 /* Message of the last failure on this thread ("" if none). */
 const char* cg_last_error(void);
