@@ -421,6 +421,72 @@ def run_batched(args):
     return 0
 
 
+def run_grad(args):
+    """Differentiable unroll: one 1024^2 creature, C=3, K=9, T=64 steps,
+    checkpoints every 8; loss = MSE(x_T, seed shifted by (+16, +8) px);
+    gradients for the seed, mu, sigma, weights and ring weights through the
+    adjoint kernels.  fwd+bwd cell-updates/s = n^2 T / (forward + backward)."""
+    import torch
+    world, rank, local, dist = dist_setup(args.gpus)
+    torch.cuda.set_device(local)
+    from cella_nova_gb300.autograd import DiffusionLeniaGPU
+    from cella_nova_gb300.creature import make_creature
+    n, C, T, every = 1024, 3, 64, 8
+    cr = make_creature(n, C, seed=1024 + rank, temp=1.0, device=torch.device("cuda", local))
+    target = torch.tensor(np.roll(cr.seed, (8, 16), axis=(1, 2)), dtype=torch.float32,
+                          device="cuda")
+    m = DiffusionLeniaGPU(cr)
+
+    def iteration():
+        m.zero_grad(set_to_none=True)
+        xT = m(T, every)
+        loss = torch.mean((xT - target) ** 2)
+        loss.backward()
+        return loss
+
+    for _ in range(max(args.warmup, 3)):
+        iteration()
+    torch.cuda.synchronize()
+    barrier(dist, world)
+    iters = max(1, min(args.steps, 20))
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    f_ms = b_ms = 0.0
+    for _ in range(iters):
+        m.zero_grad(set_to_none=True)
+        ev[0].record()
+        xT = m(T, every)
+        loss = torch.mean((xT - target) ** 2)
+        ev[1].record()
+        loss.backward()
+        ev[2].record()
+        ev[2].synchronize()
+        f_ms += ev[0].elapsed_time(ev[1])
+        b_ms += ev[1].elapsed_time(ev[2])
+    f_ms, b_ms = f_ms / iters, b_ms / iters
+    tot = max_over_ranks(f_ms + b_ms, dist, world)
+    line = {
+        "metric": "cell-updates/s (fwd+bwd, differentiable unroll 1024^2, C=3, K=9, T=64, "
+                  "checkpoints every 8)",
+        "value": world * n * n * T / (tot / 1e3), "unit": UNIT, "n_gpus": world,
+        "steps": iters, "warmup": max(args.warmup, 3), "ms_per_step": tot,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": "1 creature 1024^2, 3 channels, 9 kernels, T=64, checkpoint every "
+                               "8 (backward recomputes each segment), loss MSE vs seed shifted "
+                               "(+16,+8) px; grads: seed, mu, sigma, weights, ring weights",
+                   "step_unit": "one forward+backward iteration of the unroll"},
+        "forward_ms": f_ms, "backward_ms": b_ms,
+        "forward_cell_updates_per_s": n * n * T / (f_ms / 1e3),
+        "gpu_launches": T * 4 + T * 9 + (T - (T + every - 1) // every) * 4,
+        "loss": float(loss.detach()),
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -429,12 +495,14 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--config", default="plain", choices=["plain", "batched"])
+    ap.add_argument("--config", default="plain", choices=["plain", "batched", "grad"])
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
     if args.config == "batched":
         return run_batched(args)
+    if args.config == "grad":
+        return run_grad(args)
     return run_ours(args)
 
 
