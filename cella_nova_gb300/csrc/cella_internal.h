@@ -102,6 +102,7 @@ typedef cudaError_t (*pack_kernel_fn)(const float2* full, float2* out, cudaStrea
 typedef cudaError_t (*prepare_fn)();
 typedef int (*twiddle_count_fn)();
 typedef cudaError_t (*launch_bwd_fn)(const BwdArgs&, cudaStream_t);
+typedef cudaError_t (*launch_step_channel_fn)(const StepArgs&, int phases, int c, cudaStream_t);
 typedef cudaError_t (*kgrad_final_fn)(float2* kgrad, float* hbar, int K, const float2* tw,
                                       cudaStream_t);
 
@@ -113,6 +114,7 @@ struct SizeOps {
     launch_bwd_fn backward;
     kgrad_final_fn kgrad_final;
     prepare_fn prepare_backward;
+    launch_step_channel_fn step_channel;   // phases of one channel
 };
 
 // Fill the twiddle buffer of an n-point grid (host side, double precision).

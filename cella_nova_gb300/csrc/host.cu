@@ -181,7 +181,8 @@ struct cg_sim {
     double* mass_partial = nullptr;
     double* mass_out = nullptr;
     int* err = nullptr;   // device error word written by bounded waits
-    cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};     // one step, per parity
+    cudaGraphExec_t graph8[2] = {nullptr, nullptr};    // kStepsPerGraph steps, per parity
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     KernelGroups groups{};
     GrowthParams gp{};
@@ -219,6 +220,8 @@ void release(cg_sim* s) {
     cudaSetDevice(s->device);
     for (auto& g : s->graph)
         if (g) cudaGraphExecDestroy(g);
+    for (auto& g : s->graph8)
+        if (g) cudaGraphExecDestroy(g);
     for (auto& e : s->ev)
         if (e) cudaEventDestroy(e);
     cudaFree(s->state[0]);
@@ -239,25 +242,73 @@ void release(cg_sim* s) {
     delete s;
 }
 
-int capture_graphs(cg_sim* s) {
-    cudaStream_t cap;
-    CG_CHECK(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking), "cudaStreamCreate(capture)");
-    for (int p = 0; p < 2; ++p) {
-        cudaGraph_t g = nullptr;
-        cudaError_t e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
-        if (e == cudaSuccess) {
-            cudaError_t le = s->ops->step(s->args(p, nullptr), kPhaseAll, cap);
-            e = cudaStreamEndCapture(cap, &g);
-            if (le != cudaSuccess) e = le;
-        }
-        if (e == cudaSuccess) e = cudaGraphInstantiate(&s->graph[p], g, 0);
-        if (g) cudaGraphDestroy(g);
-        if (e != cudaSuccess) {
-            cudaStreamDestroy(cap);
-            return cuda_fail(e, "capturing the step graph");
-        }
+constexpr int kStepsPerGraph = 8;
+
+// Capture `nsteps` steps starting at ping-pong parity p0 as one graph whose
+// launches are per channel, on one stream per channel, so that independent
+// channels overlap (one channel's diffusion runs in another's tail).  Only
+// two dependencies cross channels: the inverse row pass of step t needs every
+// channel's column pass of step t (the products U of all input channels), and
+// the column pass of step t+1 overwrites U, which every inverse row pass of
+// step t reads.  Everything else is per channel and in stream order.
+cudaError_t capture_steps(cg_sim* s, int p0, int nsteps, cudaGraphExec_t* out) {
+    const int C = s->C;
+    std::vector<cudaStream_t> st(C, nullptr);
+    std::vector<cudaEvent_t> ecol(C, nullptr), ec2r(C, nullptr);
+    cudaEvent_t fork = nullptr;
+    cudaError_t e = cudaEventCreateWithFlags(&fork, cudaEventDisableTiming);
+    for (int c = 0; c < C && e == cudaSuccess; ++c) {
+        e = cudaStreamCreateWithFlags(&st[c], cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ecol[c], cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ec2r[c], cudaEventDisableTiming);
     }
-    cudaStreamDestroy(cap);
+    cudaGraph_t g = nullptr;
+    if (e == cudaSuccess) e = cudaStreamBeginCapture(st[0], cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+        cudaError_t le = cudaEventRecord(fork, st[0]);
+        for (int c = 1; c < C && le == cudaSuccess; ++c) le = cudaStreamWaitEvent(st[c], fork, 0);
+        for (int t = 0; t < nsteps && le == cudaSuccess; ++t) {
+            const StepArgs a = s->args(p0 ^ (t & 1), nullptr);
+            for (int c = 0; c < C && le == cudaSuccess; ++c) {
+                le = s->ops->step_channel(a, kPhaseRowFwd, c, st[c]);
+                for (int c2 = 0; t > 0 && c2 < C && le == cudaSuccess; ++c2)
+                    le = cudaStreamWaitEvent(st[c], ec2r[c2], 0);
+                if (le == cudaSuccess) le = s->ops->step_channel(a, kPhaseColConv, c, st[c]);
+                if (le == cudaSuccess) le = cudaEventRecord(ecol[c], st[c]);
+            }
+            for (int c = 0; c < C && le == cudaSuccess; ++c) {
+                for (int c2 = 0; c2 < C && le == cudaSuccess; ++c2)
+                    if (c2 != c) le = cudaStreamWaitEvent(st[c], ecol[c2], 0);
+                if (le == cudaSuccess) le = s->ops->step_channel(a, kPhaseGrowth, c, st[c]);
+                if (le == cudaSuccess) le = cudaEventRecord(ec2r[c], st[c]);
+                if (le == cudaSuccess) le = s->ops->step_channel(a, kPhaseDiffusion, c, st[c]);
+            }
+        }
+        // join every channel stream back into the origin stream
+        for (int c = 1; c < C && le == cudaSuccess; ++c) {
+            le = cudaEventRecord(ecol[c], st[c]);
+            if (le == cudaSuccess) le = cudaStreamWaitEvent(st[0], ecol[c], 0);
+        }
+        e = cudaStreamEndCapture(st[0], &g);
+        if (le != cudaSuccess) e = le;
+    }
+    if (e == cudaSuccess) e = cudaGraphInstantiate(out, g, 0);
+    if (g) cudaGraphDestroy(g);
+    for (int c = 0; c < C; ++c) {
+        if (st[c]) cudaStreamDestroy(st[c]);
+        if (ecol[c]) cudaEventDestroy(ecol[c]);
+        if (ec2r[c]) cudaEventDestroy(ec2r[c]);
+    }
+    if (fork) cudaEventDestroy(fork);
+    return e;
+}
+
+int capture_graphs(cg_sim* s) {
+    for (int p = 0; p < 2; ++p) {
+        cudaError_t e = capture_steps(s, p, 1, &s->graph[p]);
+        if (e == cudaSuccess) e = capture_steps(s, p, kStepsPerGraph, &s->graph8[p]);
+        if (e != cudaSuccess) return cuda_fail(e, "capturing the step graph");
+    }
     return CG_OK;
 }
 
@@ -300,11 +351,12 @@ void build_adjoint_params(cg_sim* s) {
 }
 
 int recapture(cg_sim* s) {
-    for (auto& g : s->graph)
-        if (g) {
-            cudaGraphExecDestroy(g);
-            g = nullptr;
-        }
+    for (auto* set : {s->graph, s->graph8})
+        for (int p = 0; p < 2; ++p)
+            if (set[p]) {
+                cudaGraphExecDestroy(set[p]);
+                set[p] = nullptr;
+            }
     return capture_graphs(s);
 }
 
@@ -477,7 +529,12 @@ int cg_upload_channel_f32(cg_sim* s, int c, const float* data) {
 int cg_step(cg_sim* s, int nsteps) {
     if (!s) return fail(CG_ERR_ARG, "cg_step: NULL handle");
     if (nsteps < 0) return fail(CG_ERR_ARG, "negative step count %d", nsteps);
-    for (int i = 0; i < nsteps; ++i) {
+    int left = nsteps;
+    while (left >= kStepsPerGraph) {   // an even count: the parity is unchanged
+        CG_CHECK(cudaGraphLaunch(s->graph8[s->cur], s->stream), "cudaGraphLaunch");
+        left -= kStepsPerGraph;
+    }
+    for (; left > 0; --left) {
         CG_CHECK(cudaGraphLaunch(s->graph[s->cur], s->stream), "cudaGraphLaunch");
         s->cur ^= 1;
     }

@@ -120,9 +120,10 @@ __device__ __forceinline__ void r2c_finish(float2* sm, const float2* __restrict_
 template <int LOGN>
 __global__ void __launch_bounds__(512) k_row_r2c(const float* __restrict__ state,
                                                   float2* __restrict__ rowspec,
-                                                  const float2* __restrict__ tw) {
+                                                  const float2* __restrict__ tw, int cbase) {
     extern __shared__ __align__(128) float2 sm_r2c[];
-    row_r2c_body<LOGN>(state, rowspec, tw, blockIdx.y, blockIdx.x * Geo<LOGN>::RB, sm_r2c);
+    row_r2c_body<LOGN>(state, rowspec, tw, blockIdx.y + cbase, blockIdx.x * Geo<LOGN>::RB,
+                       sm_r2c);
 }
 
 // Run the first pass of a transform, then `hook()`, then the rest.
@@ -271,14 +272,15 @@ __global__ void __launch_bounds__(256, 2) k_col_conv(const float2* __restrict__ 
                                                       float2* __restrict__ U,
                                                       const float2* __restrict__ tw,
                                                       const __grid_constant__ KernelGroups groups,
-                                                      int* err) {
+                                                      int* err, int cbase) {
     extern __shared__ __align__(128) float2 sm_col[];
     __shared__ __align__(8) uint64_t bar;
-    if (groups.in_count[blockIdx.y] == 0) return;
+    const int c = blockIdx.y + cbase;
+    if (groups.in_count[c] == 0) return;
     init_tile_barrier(&bar);
     uint32_t phase = 0;
-    col_conv_body<LOGN>(rowspec, kspec, U, tw, groups, blockIdx.y, blockIdx.x * Geo<LOGN>::TW,
-                        sm_col, &bar, phase, err);
+    col_conv_body<LOGN>(rowspec, kspec, U, tw, groups, c, blockIdx.x * Geo<LOGN>::TW, sm_col,
+                        &bar, phase, err);
 }
 
 // ---------------------------------------------------------------------------
@@ -394,9 +396,9 @@ __global__ void __launch_bounds__(512) k_row_c2r_growth(const float2* __restrict
                                                          const __grid_constant__ KernelGroups groups,
                                                          const __grid_constant__ GrowthParams gp,
                                                          float temp, float* __restrict__ udbg,
-                                                         float udbg_scale) {
+                                                         float udbg_scale, int cbase) {
     extern __shared__ __align__(128) float2 sm_c2r[];
-    row_c2r_growth_body<LOGN>(U, A, tw, groups, gp, temp, udbg, udbg_scale, blockIdx.y,
+    row_c2r_growth_body<LOGN>(U, A, tw, groups, gp, temp, udbg, udbg_scale, blockIdx.y + cbase,
                               blockIdx.x * Geo<LOGN>::RB, sm_c2r);
 }
 
@@ -551,9 +553,9 @@ __device__ __forceinline__ void diffusion_body(const float* __restrict__ A,
 template <int LOGN>
 __global__ void __launch_bounds__(256) k_diffusion(const float* __restrict__ A,
                                                     const float* __restrict__ x,
-                                                    float* __restrict__ out) {
+                                                    float* __restrict__ out, int cbase) {
     extern __shared__ __align__(128) float sm_diff[];
-    diffusion_body<LOGN>(A, x, out, blockIdx.z, blockIdx.x * Geo<LOGN>::TX,
+    diffusion_body<LOGN>(A, x, out, blockIdx.z + cbase, blockIdx.x * Geo<LOGN>::TX,
                          blockIdx.y * Geo<LOGN>::TY, sm_diff);
 }
 
@@ -605,22 +607,37 @@ cudaError_t prepare_size() {
                                 int(G::COL_SMEM));
 }
 
+// Launch the given phases for channels [c_lo, c_hi) (r2c/col: the channels
+// read; c2r/diffusion: the channels written).
+template <int LOGN>
+cudaError_t launch_step_range(const StepArgs& a, int phases, int c_lo, int c_hi,
+                              cudaStream_t st) {
+    using G = Geo<LOGN>;
+    const int nc = c_hi - c_lo;
+    if (nc <= 0) return cudaSuccess;
+    if (phases & kPhaseRowFwd)
+        k_row_r2c<LOGN><<<dim3(G::N / G::RB, nc), G::RT, G::R2C_SMEM, st>>>(a.x_in, a.rowspec,
+                                                                           a.tw, c_lo);
+    if (phases & kPhaseColConv)
+        k_col_conv<LOGN><<<dim3(G::M / G::TW, nc), G::CT, G::COL_SMEM, st>>>(
+            a.rowspec, a.kspec, a.U, a.tw, a.groups, a.err, c_lo);
+    if (phases & kPhaseGrowth)
+        k_row_c2r_growth<LOGN><<<dim3(G::N / G::RB, nc), G::RT, G::C2R_SMEM, st>>>(
+            a.U, a.A, a.tw, a.groups, a.gp, a.temp, a.udbg, float(G::N) * float(G::N), c_lo);
+    if (phases & kPhaseDiffusion)
+        k_diffusion<LOGN><<<dim3(G::N / G::TX, G::N / G::TY, nc), 256, DiffGeo<LOGN>::SMEM,
+                            st>>>(a.A, a.x_in, a.x_out, c_lo);
+    return cudaGetLastError();
+}
+
 template <int LOGN>
 cudaError_t launch_step(const StepArgs& a, int phases, cudaStream_t st) {
-    using G = Geo<LOGN>;
-    if (phases & kPhaseRowFwd)
-        k_row_r2c<LOGN><<<dim3(G::N / G::RB, a.C), G::RT, G::R2C_SMEM, st>>>(a.x_in, a.rowspec,
-                                                                            a.tw);
-    if (phases & kPhaseColConv)
-        k_col_conv<LOGN><<<dim3(G::M / G::TW, a.C), G::CT, G::COL_SMEM, st>>>(
-            a.rowspec, a.kspec, a.U, a.tw, a.groups, a.err);
-    if (phases & kPhaseGrowth)
-        k_row_c2r_growth<LOGN><<<dim3(G::N / G::RB, a.C), G::RT, G::C2R_SMEM, st>>>(
-            a.U, a.A, a.tw, a.groups, a.gp, a.temp, a.udbg, float(G::N) * float(G::N));
-    if (phases & kPhaseDiffusion)
-        k_diffusion<LOGN><<<dim3(G::N / G::TX, G::N / G::TY, a.C), 256, DiffGeo<LOGN>::SMEM,
-                            st>>>(a.A, a.x_in, a.x_out);
-    return cudaGetLastError();
+    return launch_step_range<LOGN>(a, phases, 0, a.C, st);
+}
+
+template <int LOGN>
+cudaError_t launch_step_channel(const StepArgs& a, int phases, int c, cudaStream_t st) {
+    return launch_step_range<LOGN>(a, phases, c, c + 1, st);
 }
 
 template <int LOGN>
@@ -645,5 +662,5 @@ cudaError_t launch_pack(const float2* full, float2* out, cudaStream_t st) {
     const SizeOps size_ops_l##LOGN = {launch_step<LOGN>,      launch_pack<LOGN>,          \
                                       prepare_size<LOGN>,     twiddle_count<LOGN>,        \
                                       launch_backward<LOGN>,  launch_kgrad_final<LOGN>,   \
-                                      prepare_backward<LOGN>};                            \
+                                      prepare_backward<LOGN>, launch_step_channel<LOGN>}; \
     }

@@ -102,17 +102,20 @@ def test_conv_buffer_and_affinity_match_oracle():
     assert np.abs(aff - A).max() / np.abs(A).max() < 1e-5
 
 
-def test_graph_steps_equal_timed_and_stream_steps():
+@pytest.mark.parametrize("nsteps", [4, 9, 17])
+def test_graph_steps_equal_timed_and_stream_steps(nsteps):
+    """Per-channel pipelined graphs (8 steps and 1 step) against one launch
+    per phase, step by step."""
     cr = make_creature(128, 3, seed=9, radius=(8, 20), seed_box=64)
     with GpuMaceLenia.from_creature(cr) as a, GpuMaceLenia.from_creature(cr) as b, \
             GpuMaceLenia.from_creature(cr) as c:
-        a.run_steps(4)
-        for _ in range(4):
+        a.run_steps(nsteps)
+        for _ in range(nsteps):
             ms = b.timed_iterate()
             assert ms.shape == (4,) and ms[3] == 0.0 and (ms[:3] >= 0).all()
         import torch
         s = torch.cuda.Stream()
-        for _ in range(4):
+        for _ in range(nsteps):
             c.iterate_on(s.cuda_stream)
         s.synchronize()
         np.testing.assert_array_equal(a.state(), b.state())
