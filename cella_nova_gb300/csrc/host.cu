@@ -174,7 +174,7 @@ struct cg_sim {
     int cur = 0;
     float2* rowspec = nullptr;
     float2* kspec = nullptr;
-    float2* U = nullptr;
+    float2* U = nullptr;       // two [K][n/2][n] buffers, one per ping-pong parity
     float* A = nullptr;
     float2* tw = nullptr;
     void* staging = nullptr;
@@ -202,7 +202,7 @@ struct cg_sim {
         a.x_out = state[from ^ 1];
         a.rowspec = rowspec;
         a.kspec = kspec;
-        a.U = U;
+        a.U = U + size_t(from) * K * (size_t(n / 2) * n);
         a.A = A;
         a.tw = tw;
         a.udbg = udbg;
@@ -249,18 +249,22 @@ constexpr int kStepsPerGraph = 8;
 // channels overlap (one channel's diffusion runs in another's tail).  Only
 // two dependencies cross channels: the inverse row pass of step t needs every
 // channel's column pass of step t (the products U of all input channels), and
-// the column pass of step t+1 overwrites U, which every inverse row pass of
-// step t reads.  Everything else is per channel and in stream order.
+// the column pass of step t overwrites the U buffer of its parity, which every
+// inverse row pass of step t-2 read.  Everything else is per channel and in
+// stream order.
 cudaError_t capture_steps(cg_sim* s, int p0, int nsteps, cudaGraphExec_t* out) {
     const int C = s->C;
     std::vector<cudaStream_t> st(C, nullptr);
-    std::vector<cudaEvent_t> ecol(C, nullptr), ec2r(C, nullptr);
+    std::vector<cudaEvent_t> ecol(C, nullptr);
+    std::vector<cudaEvent_t> ec2r[2] = {std::vector<cudaEvent_t>(C, nullptr),
+                                        std::vector<cudaEvent_t>(C, nullptr)};
     cudaEvent_t fork = nullptr;
     cudaError_t e = cudaEventCreateWithFlags(&fork, cudaEventDisableTiming);
     for (int c = 0; c < C && e == cudaSuccess; ++c) {
         e = cudaStreamCreateWithFlags(&st[c], cudaStreamNonBlocking);
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ecol[c], cudaEventDisableTiming);
-        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ec2r[c], cudaEventDisableTiming);
+        for (int q = 0; q < 2 && e == cudaSuccess; ++q)
+            e = cudaEventCreateWithFlags(&ec2r[q][c], cudaEventDisableTiming);
     }
     cudaGraph_t g = nullptr;
     if (e == cudaSuccess) e = cudaStreamBeginCapture(st[0], cudaStreamCaptureModeThreadLocal);
@@ -271,8 +275,11 @@ cudaError_t capture_steps(cg_sim* s, int p0, int nsteps, cudaGraphExec_t* out) {
             const StepArgs a = s->args(p0 ^ (t & 1), nullptr);
             for (int c = 0; c < C && le == cudaSuccess; ++c) {
                 le = s->ops->step_channel(a, kPhaseRowFwd, c, st[c]);
-                for (int c2 = 0; t > 0 && c2 < C && le == cudaSuccess; ++c2)
-                    le = cudaStreamWaitEvent(st[c], ec2r[c2], 0);
+                // U alternates with the parity, so the column pass of step t
+                // only has to wait for the inverse row passes of step t-2,
+                // which read the same buffer
+                for (int c2 = 0; t > 1 && c2 < C && le == cudaSuccess; ++c2)
+                    le = cudaStreamWaitEvent(st[c], ec2r[t & 1][c2], 0);   // step t-2
                 if (le == cudaSuccess) le = s->ops->step_channel(a, kPhaseColConv, c, st[c]);
                 if (le == cudaSuccess) le = cudaEventRecord(ecol[c], st[c]);
             }
@@ -280,7 +287,7 @@ cudaError_t capture_steps(cg_sim* s, int p0, int nsteps, cudaGraphExec_t* out) {
                 for (int c2 = 0; c2 < C && le == cudaSuccess; ++c2)
                     if (c2 != c) le = cudaStreamWaitEvent(st[c], ecol[c2], 0);
                 if (le == cudaSuccess) le = s->ops->step_channel(a, kPhaseGrowth, c, st[c]);
-                if (le == cudaSuccess) le = cudaEventRecord(ec2r[c], st[c]);
+                if (le == cudaSuccess) le = cudaEventRecord(ec2r[t & 1][c], st[c]);
                 if (le == cudaSuccess) le = s->ops->step_channel(a, kPhaseDiffusion, c, st[c]);
             }
         }
@@ -297,7 +304,8 @@ cudaError_t capture_steps(cg_sim* s, int p0, int nsteps, cudaGraphExec_t* out) {
     for (int c = 0; c < C; ++c) {
         if (st[c]) cudaStreamDestroy(st[c]);
         if (ecol[c]) cudaEventDestroy(ecol[c]);
-        if (ec2r[c]) cudaEventDestroy(ec2r[c]);
+        for (int q = 0; q < 2; ++q)
+            if (ec2r[q][c]) cudaEventDestroy(ec2r[q][c]);
     }
     if (fork) cudaEventDestroy(fork);
     return e;
@@ -448,7 +456,7 @@ int cg_create(int n, int C, int K, const uint32_t* c0, const uint32_t* c1, const
     if (rc == CG_OK) chk(cudaMalloc(&s->rowspec, sizeof(float2) * C * half), "cudaMalloc(rowspec)");
     if (rc == CG_OK)
         chk(cudaMalloc(&s->kspec, sizeof(float2) * K * (half + n)), "cudaMalloc(kspec)");
-    if (rc == CG_OK) chk(cudaMalloc(&s->U, sizeof(float2) * K * half), "cudaMalloc(U)");
+    if (rc == CG_OK) chk(cudaMalloc(&s->U, 2 * sizeof(float2) * K * half), "cudaMalloc(U)");
     if (rc == CG_OK) chk(cudaMalloc(&s->A, sizeof(float) * C * px), "cudaMalloc(A)");
     if (rc == CG_OK)
         chk(cudaMalloc(&s->tw, sizeof(float2) * s->ops->twiddle_count()), "cudaMalloc(twiddles)");
