@@ -35,7 +35,7 @@ N_GRID, C_CH, K_KER = 2048, 3, 9
 METRIC = "cell-updates/s (DiffusionLenia fwd step, 2048^2, C=3, K=9)"
 UNIT = "cell-updates/s"
 WORKLOAD = "DiffusionLenia 2048x2048, 3 channels, 9 kernels (all pairs), 1 creature, " \
-           "1 CUDA graph per step"
+           "8 steps per CUDA graph (per-channel launches on forked streams)"
 
 
 def bytes_per_px(C, K):
