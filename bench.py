@@ -223,6 +223,10 @@ def run_ours(args):
     cr = make_creature(N_GRID, C_CH, seed=2048 + rank, temp=1.0)
     sim = GpuMaceLenia.from_creature(cr)
     px = N_GRID * N_GRID
+    tuned = None
+    if not args.no_autotune:
+        chosen, tms = sim.autotune(reps=10)
+        tuned = {"variants": chosen, "ms": np.round(tms, 4).tolist()}
     stream = torch.cuda.ExternalStream(sim.stream())
     sampler = ClockSampler(local)
     sampler.start()
@@ -289,6 +293,7 @@ def run_ours(args):
         "e2e": e2e,
         "gpu_launches": 4 * args.steps,
         "clocks": clocks,
+        "autotune": tuned,
     }
     if cpu is not None:
         line["cpu_baseline"] = cpu
@@ -495,6 +500,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--config", default="plain", choices=["plain", "batched", "grad"])
     args = ap.parse_args()
     if args.impl == "reference":

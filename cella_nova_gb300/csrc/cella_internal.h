@@ -29,6 +29,11 @@ struct GrowthParams {
     float wsum[kMaxC];
 };
 
+// CTA-shape variant of each phase (0 = default); the autotuner picks them.
+struct Variants {
+    int r2c = 0, col = 0, c2r = 0, diff = 0;
+};
+
 // Everything one step's launches need.  Planar layouts, all device pointers:
 //   x_in, x_out : [C][n][n] f32 state (ping-pong)
 //   rowspec     : [C][n/2][n] complex — row spectra, transposed (kx-major)
@@ -52,6 +57,7 @@ struct StepArgs {
     int* err;      // device error word (bounded waits that timed out)
     KernelGroups groups;
     GrowthParams gp;
+    Variants var;
 };
 
 // Per-kernel constants of the backward pass.

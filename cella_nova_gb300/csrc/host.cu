@@ -187,6 +187,7 @@ struct cg_sim {
     KernelGroups groups{};
     GrowthParams gp{};
     AdjointParams ap{};
+    Variants var{};
     float* abar = nullptr;          // backward scratch, allocated on first use
     float* utmp[2] = {nullptr, nullptr};   // cg_unroll scratch states
     bool bwd_ready = false;
@@ -209,6 +210,7 @@ struct cg_sim {
         a.err = err;
         a.groups = groups;
         a.gp = gp;
+        a.var = var;
         return a;
     }
 };
@@ -794,6 +796,69 @@ int cg_unroll_backward(cg_sim* s, const float* ckpt, int T, int every, const flo
         }
     }
     return CG_OK;
+}
+
+int cg_set_variants(cg_sim* s, const int v[4]) {
+    if (!s || !v) return fail(CG_ERR_ARG, "cg_set_variants: NULL argument");
+    for (int p = 0; p < 4; ++p)
+        if (v[p] < 0 || v[p] > 2) return fail(CG_ERR_ARG, "variant %d of phase %d outside [0, 2]", v[p], p);
+    CG_CHECK(cudaStreamSynchronize(s->stream), "cudaStreamSynchronize");
+    s->var.r2c = v[0];
+    s->var.col = v[1];
+    s->var.c2r = v[2];
+    s->var.diff = v[3];
+    return recapture(s);
+}
+
+int cg_get_variants(cg_sim* s, int v[4]) {
+    if (!s || !v) return fail(CG_ERR_ARG, "cg_get_variants: NULL argument");
+    v[0] = s->var.r2c;
+    v[1] = s->var.col;
+    v[2] = s->var.c2r;
+    v[3] = s->var.diff;
+    return CG_OK;
+}
+
+int cg_autotune(cg_sim* s, int reps, double ms_out[12], int chosen[4]) {
+    if (!s) return fail(CG_ERR_ARG, "cg_autotune: NULL handle");
+    if (reps < 1 || reps > 1000) return fail(CG_ERR_ARG, "cg_autotune: reps %d outside [1, 1000]", reps);
+    CG_CHECK(cudaStreamSynchronize(s->stream), "cudaStreamSynchronize");
+    const int phases[4] = {kPhaseRowFwd, kPhaseColConv, kPhaseGrowth, kPhaseDiffusion};
+    double ms[4][3];
+    int best[4];
+    // Every phase reads the current state or the scratch the previous phase
+    // wrote; running them in order on the live handle leaves the state
+    // untouched (diffusion writes the spare ping-pong buffer only).
+    for (int p = 0; p < 4; ++p) {
+        best[p] = 0;
+        for (int v = 0; v < 3; ++v) {
+            Variants var = s->var;
+            int* slot[4] = {&var.r2c, &var.col, &var.c2r, &var.diff};
+            *slot[p] = v;
+            StepArgs a = s->args(s->cur, nullptr);
+            a.var = var;
+            for (int q = 0; q < p; ++q)   // inputs of phase p
+                CG_CHECK(s->ops->step(a, phases[q], s->stream), "autotune prologue");
+            CG_CHECK(s->ops->step(a, phases[p], s->stream), "autotune warm-up");
+            CG_CHECK(cudaEventRecord(s->ev[0], s->stream), "cudaEventRecord");
+            for (int r = 0; r < reps; ++r)
+                CG_CHECK(s->ops->step(a, phases[p], s->stream), "autotune launch");
+            CG_CHECK(cudaEventRecord(s->ev[1], s->stream), "cudaEventRecord");
+            CG_CHECK(cudaEventSynchronize(s->ev[1]), "cudaEventSynchronize");
+            float t = 0.f;
+            CG_CHECK(cudaEventElapsedTime(&t, s->ev[0], s->ev[1]), "cudaEventElapsedTime");
+            ms[p][v] = double(t) / reps;
+            if (ms[p][v] < ms[p][best[p]]) best[p] = v;
+        }
+    }
+    int rc = check_device_error(s);
+    if (rc != CG_OK) return rc;
+    if (ms_out)
+        for (int p = 0; p < 4; ++p)
+            for (int v = 0; v < 3; ++v) ms_out[p * 3 + v] = ms[p][v];
+    if (chosen)
+        for (int p = 0; p < 4; ++p) chosen[p] = best[p];
+    return cg_set_variants(s, best);
 }
 
 int cg_synchronize(cg_sim* s) {

@@ -26,25 +26,34 @@
 
 namespace cg {
 
-template <int LOGN>
+// Geometry of one grid size.  V selects a variant of the CTA shapes (the
+// autotuner times them): row kernels V=1 halve the rows per CTA and the
+// threads; the column kernel V=1 halves and V=2 doubles the columns and the
+// threads per CTA (work per thread is unchanged); diffusion V=1/V=2 use
+// 16 / 64 tile rows instead of 32.  Layouts in memory do not depend on V.
+template <int LOGN, int V = 0>
 struct Geo {
     static constexpr int N = 1 << LOGN;
     static constexpr int M = N / 2;
     // Row kernels: RB rows per CTA, RT threads.  The row pitch RP keeps the
     // kx-major transposes conflict-free: odd for RB >= 16 (a half-warp reads
-    // 16 rows of one column), 2 mod 16 for RB = 8 (8 rows x 2 columns).
+    // 16 rows of one column), 2 mod 16 for RB = 8 (8 rows x 2 columns),
+    // 4 mod 16 for RB = 4.
     static constexpr int RB0 = 8192 / M;
-    static constexpr int RB = RB0 < 8 ? 8 : (RB0 > N ? N : RB0);
-    static constexpr int RT = 512;
-    static constexpr int RP = padded_len(M) + (RB >= 16 ? 1 : 2);
+    static constexpr int RB1 = RB0 < 8 ? 8 : (RB0 > N ? N : RB0);
+    static constexpr int RB = (V == 1 && RB1 > 4) ? RB1 / 2 : RB1;
+    static constexpr int RT = (V == 1) ? 256 : 512;
+    static constexpr int RP = padded_len(M) + (RB >= 16 ? 1 : (RB == 8 ? 2 : 4));
     static constexpr size_t R2C_SMEM = size_t(RB) * RP * sizeof(float2);
     static constexpr size_t C2R_SMEM = 2 * R2C_SMEM;    // double-buffered input
     // Column kernel: TW columns per CTA, CT threads; a padded work buffer
     // and an unpadded staging tile that bulk copies fill.  TW = 4096/N keeps
     // 256 butterflies per radix-16 pass (one per thread) at every size.
     static constexpr int TW0 = 4096 / N;
-    static constexpr int TW = TW0 < 2 ? 2 : (TW0 > M ? M : TW0);
-    static constexpr int CT = 256;
+    static constexpr int TW1 = TW0 < 2 ? 2 : (TW0 > M ? M : TW0);
+    static constexpr int TW = (V == 1) ? (TW1 > 1 ? TW1 / 2 : 1)
+                                       : (V == 2 ? (2 * TW1 > M ? M : 2 * TW1) : TW1);
+    static constexpr int CT = (V == 1) ? 128 : (V == 2 ? 512 : 256);
     static constexpr int CP = padded_len(N) + 1;
     static constexpr size_t COL_SMEM = (size_t(TW) * CP + size_t(TW) * N) * sizeof(float2);
     // Twiddle buffer: W_N^m (m < N), then the pass tables of the column
@@ -55,7 +64,8 @@ struct Geo {
     static constexpr int TW_TOTAL = TW_ROW + tw_size(M, false);
     // Diffusion tile.
     static constexpr int TX = N < 64 ? N : 64;
-    static constexpr int TY = N < 32 ? N : 32;
+    static constexpr int TY0 = (V == 1) ? 16 : (V == 2 ? 64 : 32);
+    static constexpr int TY = N < TY0 ? N : TY0;
 };
 
 // ---------------------------------------------------------------------------
@@ -66,32 +76,32 @@ struct Geo {
 // X[M] are real and share slot 0.  Output scale: 2 x rfft.
 // grid (N/RB, C), block RT.
 // ---------------------------------------------------------------------------
-template <int LOGN>
+template <int LOGN, int V = 0>
 __device__ __forceinline__ void r2c_finish(float2* sm, const float2* __restrict__ tw,
                                            float2* __restrict__ dst);
 
-template <int LOGN>
+template <int LOGN, int V = 0>
 __device__ __forceinline__ void row_r2c_body(const float* __restrict__ state,
                                              float2* __restrict__ rowspec,
                                              const float2* __restrict__ tw, int c, int y0,
                                              float2* sm) {
-    using G = Geo<LOGN>;
+    using G = Geo<LOGN, V>;
     const float2* src =
         reinterpret_cast<const float2*>(state + (size_t(c) * G::N + y0) * G::N);
     auto ld0 = [&](int s, int i, int, int) { return __ldg(&src[size_t(s) * G::M + i]); };
     auto smld = [&](int s, int i, int, int) { return sm[s * G::RP + pidx(i)]; };
     auto smst = [&](int s, int i, float2 v, int, int) { sm[s * G::RP + pidx(i)] = v; };
     FftPasses<G::M, 1, false, G::RT, G::RB>::run(ld0, smld, smst, smst, tw + G::TW_ROW);
-    r2c_finish<LOGN>(sm, tw, rowspec + size_t(c) * G::M * G::N + y0);
+    r2c_finish<LOGN, V>(sm, tw, rowspec + size_t(c) * G::M * G::N + y0);
 }
 
 // Even/odd split of RB transformed rows in shared memory (X[k] from Z[k],
 // Z[M-k]; X[0], X[M] packed in slot 0), then the kx-major transposed store
 // of the RB rows to dst[kx * N + s].
-template <int LOGN>
+template <int LOGN, int V>
 __device__ __forceinline__ void r2c_finish(float2* sm, const float2* __restrict__ tw,
                                            float2* __restrict__ dst) {
-    using G = Geo<LOGN>;
+    using G = Geo<LOGN, V>;
     constexpr int H = G::M / 2;
     for (int item = threadIdx.x; item < G::RB * (H + 1); item += G::RT) {
         const int s = item / (H + 1), k = item % (H + 1);
@@ -117,13 +127,14 @@ __device__ __forceinline__ void r2c_finish(float2* sm, const float2* __restrict_
     }
 }
 
-template <int LOGN>
-__global__ void __launch_bounds__(512) k_row_r2c(const float* __restrict__ state,
-                                                  float2* __restrict__ rowspec,
-                                                  const float2* __restrict__ tw, int cbase) {
+template <int LOGN, int V = 0>
+__global__ void __launch_bounds__(Geo<LOGN, V>::RT, 512 / Geo<LOGN, V>::RT) k_row_r2c(const float* __restrict__ state,
+                                                               float2* __restrict__ rowspec,
+                                                               const float2* __restrict__ tw,
+                                                               int cbase) {
     extern __shared__ __align__(128) float2 sm_r2c[];
-    row_r2c_body<LOGN>(state, rowspec, tw, blockIdx.y + cbase, blockIdx.x * Geo<LOGN>::RB,
-                       sm_r2c);
+    row_r2c_body<LOGN, V>(state, rowspec, tw, blockIdx.y + cbase,
+                          blockIdx.x * Geo<LOGN, V>::RB, sm_r2c);
 }
 
 // Run the first pass of a transform, then `hook()`, then the rest.
@@ -166,7 +177,7 @@ __device__ __forceinline__ void fft_with_hook(LD& ld, SMLD& smld, SMST& smst, ST
 // Returns false if a bounded wait timed out (the error word is set).  `bar`
 // is an initialised mbarrier owned by the caller and `phase` counts its
 // completed phases, so one CTA can run many tiles back to back.
-template <int LOGN>
+template <int LOGN, int V = 0>
 __device__ __forceinline__ bool col_conv_body(const float2* __restrict__ rowspec,
                                               const float2* __restrict__ kspec,
                                               float2* __restrict__ U,
@@ -174,7 +185,7 @@ __device__ __forceinline__ bool col_conv_body(const float2* __restrict__ rowspec
                                               const KernelGroups& groups, int c, int kx0,
                                               float2* sm, uint64_t* barp, uint32_t& phase,
                                               int* err) {
-    using G = Geo<LOGN>;
+    using G = Geo<LOGN, V>;
     constexpr int N = G::N, M = G::M, TW = G::TW, T = G::CT;
     const int cnt = groups.in_count[c];
     if (cnt == 0) return true;
@@ -266,21 +277,19 @@ __device__ __forceinline__ void init_tile_barrier(uint64_t* bar) {
     __syncthreads();
 }
 
-template <int LOGN>
-__global__ void __launch_bounds__(256, 2) k_col_conv(const float2* __restrict__ rowspec,
-                                                      const float2* __restrict__ kspec,
-                                                      float2* __restrict__ U,
-                                                      const float2* __restrict__ tw,
-                                                      const __grid_constant__ KernelGroups groups,
-                                                      int* err, int cbase) {
+template <int LOGN, int V = 0>
+__global__ void __launch_bounds__(Geo<LOGN, V>::CT, 512 / Geo<LOGN, V>::CT)
+    k_col_conv(const float2* __restrict__ rowspec, const float2* __restrict__ kspec,
+               float2* __restrict__ U, const float2* __restrict__ tw,
+               const __grid_constant__ KernelGroups groups, int* err, int cbase) {
     extern __shared__ __align__(128) float2 sm_col[];
     __shared__ __align__(8) uint64_t bar;
     const int c = blockIdx.y + cbase;
     if (groups.in_count[c] == 0) return;
     init_tile_barrier(&bar);
     uint32_t phase = 0;
-    col_conv_body<LOGN>(rowspec, kspec, U, tw, groups, c, blockIdx.x * Geo<LOGN>::TW, sm_col,
-                        &bar, phase, err);
+    col_conv_body<LOGN, V>(rowspec, kspec, U, tw, groups, c, blockIdx.x * Geo<LOGN, V>::TW,
+                           sm_col, &bar, phase, err);
 }
 
 // ---------------------------------------------------------------------------
@@ -298,7 +307,7 @@ __global__ void __launch_bounds__(256, 2) k_col_conv(const float2* __restrict__ 
 // into the second buffer while the current one is transformed.
 // grid (N/RB, C), block RT.
 // ---------------------------------------------------------------------------
-template <int LOGN>
+template <int LOGN, int V = 0>
 __device__ __forceinline__ void row_c2r_growth_body(const float2* __restrict__ U,
                                                     float* __restrict__ A,
                                                     const float2* __restrict__ tw,
@@ -306,7 +315,7 @@ __device__ __forceinline__ void row_c2r_growth_body(const float2* __restrict__ U
                                                     const GrowthParams& gp, float temp,
                                                     float* __restrict__ udbg, float udbg_scale,
                                                     int c, int y0, float2* sm) {
-    using G = Geo<LOGN>;
+    using G = Geo<LOGN, V>;
     constexpr int RL = last_radix(G::M);
     constexpr int JL = G::M / RL;
     constexpr int ITEMS = G::RB * JL;
@@ -389,8 +398,8 @@ __device__ __forceinline__ void row_c2r_growth_body(const float2* __restrict__ U
     }
 }
 
-template <int LOGN>
-__global__ void __launch_bounds__(512) k_row_c2r_growth(const float2* __restrict__ U,
+template <int LOGN, int V = 0>
+__global__ void __launch_bounds__(Geo<LOGN, V>::RT, 512 / Geo<LOGN, V>::RT) k_row_c2r_growth(const float2* __restrict__ U,
                                                          float* __restrict__ A,
                                                          const float2* __restrict__ tw,
                                                          const __grid_constant__ KernelGroups groups,
@@ -398,8 +407,8 @@ __global__ void __launch_bounds__(512) k_row_c2r_growth(const float2* __restrict
                                                          float temp, float* __restrict__ udbg,
                                                          float udbg_scale, int cbase) {
     extern __shared__ __align__(128) float2 sm_c2r[];
-    row_c2r_growth_body<LOGN>(U, A, tw, groups, gp, temp, udbg, udbg_scale, blockIdx.y + cbase,
-                              blockIdx.x * Geo<LOGN>::RB, sm_c2r);
+    row_c2r_growth_body<LOGN, V>(U, A, tw, groups, gp, temp, udbg, udbg_scale,
+                                 blockIdx.y + cbase, blockIdx.x * Geo<LOGN, V>::RB, sm_c2r);
 }
 
 // ---------------------------------------------------------------------------
@@ -439,20 +448,20 @@ __device__ __forceinline__ void for_tile(F fn) {
     }
 }
 
-template <int LOGN>
+template <int LOGN, int V = 0>
 struct DiffGeo {
-    static constexpr int TX = Geo<LOGN>::TX, TY = Geo<LOGN>::TY;
+    static constexpr int TX = Geo<LOGN, V>::TX, TY = Geo<LOGN, V>::TY;
     static constexpr int AW = TX + 4, AH = TY + 4, HW = TX + 2, QH = TY + 2;
     static constexpr size_t SMEM = size_t(2 * AH * AW + 2 * AH * HW + QH * HW) * sizeof(float);
 };
 
-template <int LOGN>
+template <int LOGN, int V = 0>
 __device__ __forceinline__ void diffusion_body(const float* __restrict__ A,
                                                const float* __restrict__ x,
                                                float* __restrict__ out, int c, int x0, int y0,
                                                float* smf) {
-    using G = Geo<LOGN>;
-    using D = DiffGeo<LOGN>;
+    using G = Geo<LOGN, V>;
+    using D = DiffGeo<LOGN, V>;
     constexpr int N = G::N, TX = G::TX, TY = G::TY;
     constexpr int AW = D::AW, AH = D::AH, HW = D::HW, QH = D::QH;
     auto sAh = reinterpret_cast<float (*)[AW]>(smf);
@@ -550,13 +559,13 @@ __device__ __forceinline__ void diffusion_body(const float* __restrict__ A,
     });
 }
 
-template <int LOGN>
+template <int LOGN, int V = 0>
 __global__ void __launch_bounds__(256) k_diffusion(const float* __restrict__ A,
                                                     const float* __restrict__ x,
                                                     float* __restrict__ out, int cbase) {
     extern __shared__ __align__(128) float sm_diff[];
-    diffusion_body<LOGN>(A, x, out, blockIdx.z + cbase, blockIdx.x * Geo<LOGN>::TX,
-                         blockIdx.y * Geo<LOGN>::TY, sm_diff);
+    diffusion_body<LOGN, V>(A, x, out, blockIdx.z + cbase, blockIdx.x * Geo<LOGN, V>::TX,
+                            blockIdx.y * Geo<LOGN, V>::TY, sm_diff);
 }
 
 // ---------------------------------------------------------------------------
@@ -589,44 +598,78 @@ __global__ void k_pack_kernel(const float2* __restrict__ full, float2* __restric
 // ---------------------------------------------------------------------------
 // Host-side launchers for one grid size.
 // ---------------------------------------------------------------------------
-template <int LOGN>
-cudaError_t prepare_size() {
-    using G = Geo<LOGN>;
+template <int LOGN, int V>
+cudaError_t prepare_variant() {
+    using G = Geo<LOGN, V>;
     cudaError_t e;
-    if ((e = cudaFuncSetAttribute(k_row_r2c<LOGN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    if ((e = cudaFuncSetAttribute(k_row_r2c<LOGN, V>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   int(G::R2C_SMEM))) != cudaSuccess)
         return e;
-    if ((e = cudaFuncSetAttribute(k_row_c2r_growth<LOGN>,
+    if ((e = cudaFuncSetAttribute(k_row_c2r_growth<LOGN, V>,
                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   int(G::C2R_SMEM))) != cudaSuccess)
         return e;
-    if ((e = cudaFuncSetAttribute(k_diffusion<LOGN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  int(DiffGeo<LOGN>::SMEM))) != cudaSuccess)
+    if ((e = cudaFuncSetAttribute(k_diffusion<LOGN, V>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  int(DiffGeo<LOGN, V>::SMEM))) != cudaSuccess)
         return e;
-    return cudaFuncSetAttribute(k_col_conv<LOGN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    return cudaFuncSetAttribute(k_col_conv<LOGN, V>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 int(G::COL_SMEM));
 }
 
-// Launch the given phases for channels [c_lo, c_hi) (r2c/col: the channels
-// read; c2r/diffusion: the channels written).
+template <int LOGN>
+cudaError_t prepare_size() {
+    cudaError_t e = prepare_variant<LOGN, 0>();
+    if (e == cudaSuccess) e = prepare_variant<LOGN, 1>();
+    if (e == cudaSuccess) e = prepare_variant<LOGN, 2>();
+    return e;
+}
+
+// One phase for channels [c_lo, c_lo + nc) (r2c/col: the channels read;
+// c2r/diffusion: the channels written) in variant V.
+template <int LOGN, int V>
+void launch_r2c(const StepArgs& a, int c_lo, int nc, cudaStream_t st) {
+    using G = Geo<LOGN, V>;
+    k_row_r2c<LOGN, V><<<dim3(G::N / G::RB, nc), G::RT, G::R2C_SMEM, st>>>(a.x_in, a.rowspec,
+                                                                          a.tw, c_lo);
+}
+template <int LOGN, int V>
+void launch_col(const StepArgs& a, int c_lo, int nc, cudaStream_t st) {
+    using G = Geo<LOGN, V>;
+    k_col_conv<LOGN, V><<<dim3(G::M / G::TW, nc), G::CT, G::COL_SMEM, st>>>(
+        a.rowspec, a.kspec, a.U, a.tw, a.groups, a.err, c_lo);
+}
+template <int LOGN, int V>
+void launch_c2r(const StepArgs& a, int c_lo, int nc, cudaStream_t st) {
+    using G = Geo<LOGN, V>;
+    k_row_c2r_growth<LOGN, V><<<dim3(G::N / G::RB, nc), G::RT, G::C2R_SMEM, st>>>(
+        a.U, a.A, a.tw, a.groups, a.gp, a.temp, a.udbg, float(G::N) * float(G::N), c_lo);
+}
+template <int LOGN, int V>
+void launch_diff(const StepArgs& a, int c_lo, int nc, cudaStream_t st) {
+    using G = Geo<LOGN, V>;
+    k_diffusion<LOGN, V><<<dim3(G::N / G::TX, G::N / G::TY, nc), 256, DiffGeo<LOGN, V>::SMEM,
+                           st>>>(a.A, a.x_in, a.x_out, c_lo);
+}
+
+#define CG_VARIANT_SWITCH(v, FN, ...)            \
+    switch (v) {                                  \
+        case 1: FN<LOGN, 1>(__VA_ARGS__); break;  \
+        case 2: FN<LOGN, 2>(__VA_ARGS__); break;  \
+        default: FN<LOGN, 0>(__VA_ARGS__); break; \
+    }
+
+// The given phases for channels [c_lo, c_hi), each in the variant a.var
+// names.
 template <int LOGN>
 cudaError_t launch_step_range(const StepArgs& a, int phases, int c_lo, int c_hi,
                               cudaStream_t st) {
-    using G = Geo<LOGN>;
     const int nc = c_hi - c_lo;
     if (nc <= 0) return cudaSuccess;
-    if (phases & kPhaseRowFwd)
-        k_row_r2c<LOGN><<<dim3(G::N / G::RB, nc), G::RT, G::R2C_SMEM, st>>>(a.x_in, a.rowspec,
-                                                                           a.tw, c_lo);
-    if (phases & kPhaseColConv)
-        k_col_conv<LOGN><<<dim3(G::M / G::TW, nc), G::CT, G::COL_SMEM, st>>>(
-            a.rowspec, a.kspec, a.U, a.tw, a.groups, a.err, c_lo);
-    if (phases & kPhaseGrowth)
-        k_row_c2r_growth<LOGN><<<dim3(G::N / G::RB, nc), G::RT, G::C2R_SMEM, st>>>(
-            a.U, a.A, a.tw, a.groups, a.gp, a.temp, a.udbg, float(G::N) * float(G::N), c_lo);
-    if (phases & kPhaseDiffusion)
-        k_diffusion<LOGN><<<dim3(G::N / G::TX, G::N / G::TY, nc), 256, DiffGeo<LOGN>::SMEM,
-                            st>>>(a.A, a.x_in, a.x_out, c_lo);
+    if (phases & kPhaseRowFwd) { CG_VARIANT_SWITCH(a.var.r2c, launch_r2c, a, c_lo, nc, st) }
+    if (phases & kPhaseColConv) { CG_VARIANT_SWITCH(a.var.col, launch_col, a, c_lo, nc, st) }
+    if (phases & kPhaseGrowth) { CG_VARIANT_SWITCH(a.var.c2r, launch_c2r, a, c_lo, nc, st) }
+    if (phases & kPhaseDiffusion) { CG_VARIANT_SWITCH(a.var.diff, launch_diff, a, c_lo, nc, st) }
     return cudaGetLastError();
 }
 

@@ -127,6 +127,23 @@ class GpuMaceLenia:
         check(self._lib.cg_profile_kernels(self._h, int(nsteps), dptr(ms)))
         return ms
 
+    def autotune(self, reps=10):
+        """Time every CTA-shape variant of every phase, keep the fastest.
+        Returns (chosen[4], ms[4][3])."""
+        ms = np.zeros(12, dtype=np.float64)
+        ch = (ctypes.c_int * 4)()
+        check(self._lib.cg_autotune(self._h, int(reps), dptr(ms), ch))
+        return list(ch), ms.reshape(4, 3)
+
+    def set_variants(self, v):
+        arr = (ctypes.c_int * 4)(*[int(x) for x in v])
+        check(self._lib.cg_set_variants(self._h, arr))
+
+    def variants(self):
+        arr = (ctypes.c_int * 4)()
+        check(self._lib.cg_get_variants(self._h, arr))
+        return list(arr)
+
     def synchronize(self):
         check(self._lib.cg_synchronize(self._h))
 

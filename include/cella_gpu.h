@@ -119,6 +119,20 @@ int cg_download_affinity(cg_sim* sim, float* out);
  * copy (always 0: the state is ping-ponged, no copy exists). */
 int cg_timed_iterate(cg_sim* sim, double ms[4]);
 
+/* Autotuner (no reference counterpart).  Each phase has three CTA-shape
+ * variants (rows per CTA and threads for the row FFTs, columns per CTA and
+ * threads for the column pass, tile rows for diffusion); they give
+ * bit-identical results.  cg_autotune times every variant of every phase
+ * `reps` times on the live handle (the state is not advanced), keeps the
+ * fastest per phase and re-captures the step graphs.  ms_out[12]
+ * (phase-major: [row FFT v0..v2, column v0..v2, inverse row + growth
+ * v0..v2, diffusion v0..v2]) and chosen[4] may be NULL. */
+int cg_autotune(cg_sim* sim, int reps, double ms_out[12], int chosen[4]);
+/* Set / read the variant of each phase ([row FFT, column, inverse row +
+ * growth, diffusion], each 0..2); setting re-captures the graphs. */
+int cg_set_variants(cg_sim* sim, const int v[4]);
+int cg_get_variants(cg_sim* sim, int v[4]);
+
 /* Per-kernel device time, averaged over nsteps steps (1..1024) launched
  * one kernel at a time with CUDA events between them (no reference
  * counterpart; a finer split of timed_iterate, mod.rs:469-540).  Advances

@@ -176,3 +176,31 @@ def test_kernel_reupload_and_zero_kernel():
         sim.set_kernel(cr.kspec[0], 0)
         conv = sim.download_conv_buffer().reshape(cr.K, 64, 64)
         assert np.abs(conv[0]).max() > 0.0
+
+
+@pytest.mark.parametrize("n", [64, 256, 1024])
+def test_variants_bit_identical_and_autotune(n):
+    """Every CTA-shape variant of every phase computes the same bits, so the
+    autotuner's choice never changes results."""
+    cr = make_creature(n, 3, seed=70 + n, radius=(max(2.0, n / 16), max(4.0, n / 6)),
+                       seed_box=n // 2)
+    with GpuMaceLenia.from_creature(cr) as sim:
+        assert sim.variants() == [0, 0, 0, 0]
+        sim.run_steps(3)
+        ref = sim.state()
+    for p in range(4):
+        for v in (1, 2):
+            var = [0, 0, 0, 0]
+            var[p] = v
+            with GpuMaceLenia.from_creature(cr) as sim:
+                sim.set_variants(var)
+                sim.run_steps(3)
+                np.testing.assert_array_equal(sim.state(), ref, err_msg=str(var))
+    with GpuMaceLenia.from_creature(cr) as sim:
+        x0 = sim.state()
+        chosen, ms = sim.autotune(reps=3)
+        np.testing.assert_array_equal(sim.state(), x0)    # tuning does not step
+        assert all(0 <= c <= 2 for c in chosen) and ms.shape == (4, 3) and (ms > 0).all()
+        assert sim.variants() == chosen
+        sim.run_steps(3)
+        np.testing.assert_array_equal(sim.state(), ref)
