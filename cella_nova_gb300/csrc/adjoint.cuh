@@ -235,7 +235,7 @@ __device__ __forceinline__ bool col_conv_adj_body(float2* __restrict__ rowspec,
     using G = Geo<LOGN>;
     constexpr int N = G::N, M = G::M, TW = G::TW, T = G::CT;
     float2* W = sm;
-    float2* KS = sm + TW * G::CP;
+    float2* KS = sm + G::KSOFF;
     uint64_t& bar = *barp;
     const int cnt = groups.in_count[c], base = groups.in_start[c];
     float2* dst = rowspec + (size_t(c) * M + kx0) * N;

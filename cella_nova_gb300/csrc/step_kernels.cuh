@@ -55,7 +55,10 @@ struct Geo {
                                        : (V == 2 ? (2 * TW1 > M ? M : 2 * TW1) : TW1);
     static constexpr int CT = (V == 1) ? 128 : (V == 2 ? 512 : 256);
     static constexpr int CP = padded_len(N) + 1;
-    static constexpr size_t COL_SMEM = (size_t(TW) * CP + size_t(TW) * N) * sizeof(float2);
+    // the staging tile is a bulk-copy (TMA) destination: 16-byte aligned
+    static constexpr int KSOFF = (TW * CP + 1) & ~1;
+    static_assert((KSOFF * sizeof(float2)) % 16 == 0, "bulk-copy destination alignment");
+    static constexpr size_t COL_SMEM = (size_t(KSOFF) + size_t(TW) * N) * sizeof(float2);
     // Twiddle buffer: W_N^m (m < N), then the pass tables of the column
     // forward plan, the column inverse plan and the row plan.
     static constexpr int TW_COL_FWD = N;
@@ -190,7 +193,7 @@ __device__ __forceinline__ bool col_conv_body(const float2* __restrict__ rowspec
     const int cnt = groups.in_count[c];
     if (cnt == 0) return true;
     float2* W = sm;
-    float2* KS = sm + TW * G::CP;
+    float2* KS = sm + G::KSOFF;
     uint64_t& bar = *barp;
     const int base = groups.in_start[c];
     constexpr uint32_t kTileBytes = uint32_t(TW) * N * sizeof(float2);
