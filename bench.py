@@ -291,7 +291,9 @@ def run_ours(args):
         "kernel_ms": {"row_r2c": kms[0], "col_conv": kms[1], "row_c2r_growth": kms[2],
                       "diffusion": kms[3]},
         "e2e": e2e,
-        "gpu_launches": 4 * args.steps,
+        # per step one launch per phase (4) per channel (the graphs run the
+        # channels on forked streams)
+        "gpu_launches": 4 * C_CH * args.steps,
         "clocks": clocks,
         "autotune": tuned,
     }
@@ -416,7 +418,8 @@ def run_batched(args):
         "phase_ms": {"row_r2c": phase_ms[0], "col_conv": phase_ms[1],
                      "row_c2r_growth": phase_ms[2], "diffusion": phase_ms[3]},
         "work_items": items, "persistent_grid": grid,
-        "gpu_launches": 4 * args.steps, "clocks": clocks,
+        # one persistent launch per phase per grid size
+        "gpu_launches": 4 * len({cr.n for cr in crs}) * args.steps, "clocks": clocks,
         "setup_s": {"generate": gen_s},
     }
     if rank == 0:
@@ -482,7 +485,10 @@ def run_grad(args):
                    "step_unit": "one forward+backward iteration of the unroll"},
         "forward_ms": f_ms, "backward_ms": b_ms,
         "forward_cell_updates_per_s": n * n * T / (f_ms / 1e3),
-        "gpu_launches": T * 4 + T * 9 + (T - (T + every - 1) // every) * 4,
+        # forward 4 per step; backward per step 3 recomputed phases + 5 adjoint
+        # kernels; each segment re-runs its steps but the first; 2 final
+        # kernel-gradient launches
+        "gpu_launches": T * 4 + T * 8 + (T - (T + every - 1) // every) * 4 + 2,
         "loss": float(loss.detach()),
     }
     if rank == 0:
