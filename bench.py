@@ -60,7 +60,7 @@ def peaks():
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+    """nvidia-smi clocks and throttle reasons sampled every 100 ms."""
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
@@ -75,7 +75,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "100"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except OSError:
             self.proc = None
@@ -102,8 +102,10 @@ class ClockSampler:
         if not rows:
             rows = [r for _, r in self.rows]
         if not rows:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"],
-                    "samples": 0}
+            why = ("nvidia-smi printed no sample (the run may be shorter than its start-up)"
+                   if self.proc else "nvidia-smi unavailable")
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0,
+                    "note": why}
         sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
         mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
@@ -501,7 +503,10 @@ def run_grad(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=1000)
+    # default: 4000 steps for the plain 2048^2 step (a timed region near one
+    # second, ~10 clock samples), 500 for the batched forward, 20 iterations
+    # of the differentiable unroll
+    ap.add_argument("--steps", type=int, default=None)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -509,6 +514,10 @@ def main():
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--config", default="plain", choices=["plain", "batched", "grad"])
     args = ap.parse_args()
+    if args.steps is None:
+        args.steps = {"plain": 4000, "batched": 500, "grad": 20}[args.config]
+        if args.impl == "reference":
+            args.steps = 1000
     if args.impl == "reference":
         return run_reference(args)
     if args.config == "batched":
