@@ -57,6 +57,12 @@ SIGNATURES = {
     "cg_upload_channel": ([_P, _I, _DP], _I),
     "cg_set_kernel_device": ([_P, _I, _P], _I),
     "cg_set_params": ([_P, _FP, _FP, _FP, _F], _I),
+    "cg_set_params_device": ([_P, _P, _P, _P], _I),
+    "cg_iterate_and_render": ([_P], _I),
+    "cg_render": ([_P], _I),
+    "cg_download_render": ([_P, ctypes.POINTER(ctypes.c_uint8)], _I),
+    "cg_download_render_packed": ([_P, _UP], _I),
+    "cg_render_ptr": ([_P, ctypes.POINTER(_P)], _I),
     "cg_step_from": ([_P, _P, _P], _I),
     "cg_step_backward": ([_P, _P, _P, _P, _P, _P], _I),
     "cg_kernel_grad_spatial": ([_P, _P, _P], _I),
@@ -93,6 +99,8 @@ SIGNATURES = {
     "cg_batch_info": ([_P, ctypes.POINTER(_I), ctypes.POINTER(_I)], _I),
     "cg_load_config_json": ([ctypes.c_char_p, ctypes.POINTER(cg_config)], _I),
     "cg_free_config": ([ctypes.POINTER(cg_config)], None),
+    "cg_load_config_bin": ([ctypes.c_char_p, ctypes.POINTER(cg_config)], _I),
+    "cg_save_config_bin": ([ctypes.c_char_p, ctypes.POINTER(cg_config)], _I),
     "cg_load_kernels_bin": ([ctypes.c_char_p, _I, _I, _FP], _I),
     "cg_kernels_bin_size": ([ctypes.c_char_p, _I, ctypes.POINTER(_I)], _I),
 }

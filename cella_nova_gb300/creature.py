@@ -25,6 +25,7 @@ r >= 1; the kernel is normalised to sum 1 and transformed in float64.
 from __future__ import annotations
 
 import json
+import struct
 import os
 from dataclasses import dataclass, field
 
@@ -194,6 +195,24 @@ def write_seed_json(path: str, cr: Creature) -> None:
     os.makedirs(os.path.dirname(os.path.abspath(path)), exist_ok=True)
     with open(path, "w") as f:
         json.dump(data, f)
+
+
+def write_seed_bin(path: str, cr: Creature) -> None:
+    """The binary twin of the seed JSON (magic CNSEED01; layout in
+    include/cella_gpu.h): the JSON's fields, c0/c1 in the JSON's order."""
+    K = cr.K
+    parts = [b"CNSEED01", struct.pack("<IIIf", cr.n, cr.C, K, float(cr.temp)),
+             np.asarray(cr.c1, dtype="<u4").tobytes(),    # JSON c0 (output)
+             np.asarray(cr.c0, dtype="<u4").tobytes(),    # JSON c1 (input)
+             np.asarray(cr.mu, dtype="<f4").tobytes(),
+             np.asarray(cr.sigma, dtype="<f4").tobytes(),
+             np.asarray(cr.weights, dtype="<f4").tobytes()]
+    head = b"".join(parts)
+    head += b"\0" * (-len(head) % 8)
+    os.makedirs(os.path.dirname(os.path.abspath(path)), exist_ok=True)
+    with open(path, "wb") as f:
+        f.write(head)
+        f.write(np.ascontiguousarray(cr.seed, dtype="<f8").tobytes())
 
 
 def write_creature(root: str, name: str, cr: Creature) -> tuple[str, str]:

@@ -209,12 +209,12 @@ template <int LOGN>
 __global__ void __launch_bounds__(512) k_growth_bwd(float2* __restrict__ U,
                                                      const float* __restrict__ abar,
                                                      const float2* __restrict__ tw,
-                                                     const __grid_constant__ AdjointParams ap,
+                                                     const AdjointParams* __restrict__ app,
                                                      double* __restrict__ pgrad, int K) {
     extern __shared__ __align__(128) float2 sm_gbwd[];
     __shared__ double red[16];
     const int k = blockIdx.y;
-    growth_bwd_body<LOGN>(U, abar, tw, ap, k, ap.cout[k], blockIdx.x * Geo<LOGN>::RB, pgrad, K,
+    growth_bwd_body<LOGN>(U, abar, tw, *app, k, app->cout[k], blockIdx.x * Geo<LOGN>::RB, pgrad, K,
                           sm_gbwd, red);
 }
 

@@ -55,8 +55,9 @@ struct StepArgs {
     const float2* tw;
     float* udbg;   // optional [K][n][n] f32: Re(conv) before the 1/n^2 scale
     int* err;      // device error word (bounded waits that timed out)
+    unsigned char* render;   // optional packed 0x00RRGGBB words, written by the diffusion
     KernelGroups groups;
-    GrowthParams gp;
+    const GrowthParams* gp;   // device-resident: updated without re-capturing graphs
     Variants var;
 };
 
@@ -89,6 +90,12 @@ struct BwdArgs {
     float2* kgrad;
     int* err;
     KernelGroups groups;
+    const GrowthParams* gp;   // device-resident
+    const AdjointParams* ap;  // device-resident
+};
+
+// The per-world parameter block the kernels read from device memory.
+struct DeviceParams {
     GrowthParams gp;
     AdjointParams ap;
 };
@@ -145,6 +152,10 @@ const SizeOps* size_ops(int logn);
 cudaError_t launch_f64_to_f32(const double* in, float* out, size_t count, cudaStream_t s);
 cudaError_t launch_mass_f64(const float* x, int C, size_t px, double* partial, int nblocks,
                             double* out, cudaStream_t s);
+cudaError_t launch_render(const float* x, int C, size_t px, unsigned* out, cudaStream_t s);
+cudaError_t launch_rgb24(const unsigned* in, unsigned char* out, size_t px, cudaStream_t s);
+cudaError_t launch_fold_params(const float* mu, const float* sigma, const float* w, int C, int K,
+                               const KernelGroups& g, DeviceParams* p, cudaStream_t s);
 constexpr int kMassBlocks = 296;   // 2 per SM on a 148/152-SM part
 
 }  // namespace cg

@@ -4,6 +4,22 @@
 //                       train/generate_kernel_json.py:195-215)
 //   kernels/{name}_{n}.bin  (config.rs:49-125; generate_kernel_json.py:182-192)
 //
+// and a binary twin of the seed format (no reference counterpart), which
+// holds exactly the fields of the JSON so a conversion either way is
+// lossless.  All little-endian:
+//
+//   offset 0   8 bytes  magic "CNSEED01"
+//          8   u32      seed_size n
+//         12   u32      num_channels C
+//         16   u32      num_kernels K
+//         20   f32      temp
+//         24   u32[K]   the JSON "c0" field (output channel; swapped on load
+//                       as config.rs:40 swaps the JSON fields)
+//              u32[K]   the JSON "c1" field (input channel)
+//              f32[K]   growth_mu, then growth_sigma, then growth_weights
+//              zero padding to a multiple of 8 bytes
+//              f64[C][n][n]  seed_channels
+//
 // A small JSON reader of its own (objects, arrays, numbers, strings,
 // literals) is enough for the seed format; unknown keys are skipped, as
 // serde does for SimConfig.  Failures return a status instead of panicking
@@ -154,6 +170,41 @@ bool read_file(const char* path, std::vector<char>& buf) {
     buf[got] = '\0';
     buf.resize(got + 1);
     return got == size_t(sz);
+}
+
+constexpr char kSeedMagic[8] = {'C', 'N', 'S', 'E', 'E', 'D', '0', '1'};
+
+size_t seed_bin_header(int K) {
+    const size_t h = 24 + size_t(K) * 4 * 5;
+    return (h + 7) & ~size_t(7);
+}
+
+uint32_t get_u32(const unsigned char* b) {
+    return uint32_t(b[0]) | (uint32_t(b[1]) << 8) | (uint32_t(b[2]) << 16) | (uint32_t(b[3]) << 24);
+}
+
+float get_f32(const unsigned char* b) {
+    const uint32_t u = get_u32(b);
+    float v;
+    std::memcpy(&v, &u, 4);
+    return v;
+}
+
+double get_f64(const unsigned char* b) {
+    const uint64_t u = uint64_t(get_u32(b)) | (uint64_t(get_u32(b + 4)) << 32);
+    double v;
+    std::memcpy(&v, &u, 8);
+    return v;
+}
+
+void put_u32(std::vector<unsigned char>& o, uint32_t u) {
+    for (int i = 0; i < 4; ++i) o.push_back(static_cast<unsigned char>(u >> (8 * i)));
+}
+
+void put_f32(std::vector<unsigned char>& o, float v) {
+    uint32_t u;
+    std::memcpy(&u, &v, 4);
+    put_u32(o, u);
 }
 
 template <class T>
@@ -345,6 +396,98 @@ int cg_load_kernels_bin(const char* path, int K, int target, float* out) {
                 dst[2 * di + 1] = rd(si, 1);
             }
     }
+    return CG_OK;
+}
+
+int cg_load_config_bin(const char* path, cg_config* out) {
+    using cg::fail;
+    if (!path || !out) return fail(CG_ERR_ARG, "cg_load_config_bin: NULL argument");
+    std::memset(out, 0, sizeof(*out));
+    std::vector<char> raw;
+    if (!read_file(path, raw)) return fail(CG_ERR_IO, "cannot read seed file %s", path);
+    const size_t size = raw.size() - 1;   // read_file appends a NUL
+    const auto* b = reinterpret_cast<const unsigned char*>(raw.data());
+    if (size < 24 || std::memcmp(b, kSeedMagic, 8) != 0)
+        return fail(CG_ERR_FORMAT, "%s: not a binary seed file (magic CNSEED01)", path);
+    const uint32_t n = get_u32(b + 8), C = get_u32(b + 12), K = get_u32(b + 16);
+    if (n < 1 || n > 65536 || C < 1 || C > 4096 || K < 1 || K > 65536)
+        return fail(CG_ERR_FORMAT, "%s: implausible sizes n=%u C=%u K=%u", path, n, C, K);
+    const size_t px = size_t(n) * n, head = seed_bin_header(int(K));
+    if (size != head + 8 * size_t(C) * px)
+        return fail(CG_ERR_FORMAT, "%s: %zu bytes, expected %zu for n=%u C=%u K=%u", path, size,
+                    head + 8 * size_t(C) * px, n, C, K);
+    const unsigned char* pk = b + 24;
+    for (uint32_t k = 0; k < 2 * K; ++k)
+        if (get_u32(pk + 4 * k) >= C)
+            return fail(CG_ERR_FORMAT, "%s: kernel %u channel index outside [0, %u)", path, k % K, C);
+    out->seed_size = int(n);
+    out->num_channels = int(C);
+    out->num_kernels = int(K);
+    out->temp = get_f32(b + 20);
+    out->seed_channels = static_cast<double*>(std::malloc(sizeof(double) * C * px));
+    out->c0 = static_cast<uint32_t*>(std::malloc(sizeof(uint32_t) * K));
+    out->c1 = static_cast<uint32_t*>(std::malloc(sizeof(uint32_t) * K));
+    out->growth_mu = static_cast<float*>(std::malloc(sizeof(float) * K));
+    out->growth_sigma = static_cast<float*>(std::malloc(sizeof(float) * K));
+    out->growth_weights = static_cast<float*>(std::malloc(sizeof(float) * K));
+    if (!out->seed_channels || !out->c0 || !out->c1 || !out->growth_mu || !out->growth_sigma ||
+        !out->growth_weights) {
+        cg_free_config(out);
+        return fail(CG_ERR_OOM, "cg_load_config_bin: host allocation failed");
+    }
+    for (uint32_t k = 0; k < K; ++k) {
+        out->c1[k] = get_u32(pk + 4 * k);             // JSON c0: output channel
+        out->c0[k] = get_u32(pk + 4 * (K + k));       // JSON c1: input channel
+        out->growth_mu[k] = get_f32(pk + 4 * (2 * K + k));
+        out->growth_sigma[k] = get_f32(pk + 4 * (3 * K + k));
+        out->growth_weights[k] = get_f32(pk + 4 * (4 * K + k));
+    }
+    const unsigned char* ps = b + head;
+    for (size_t i = 0; i < size_t(C) * px; ++i) out->seed_channels[i] = get_f64(ps + 8 * i);
+    return CG_OK;
+}
+
+int cg_save_config_bin(const char* path, const cg_config* cfg) {
+    using cg::fail;
+    if (!path || !cfg || !cfg->seed_channels || !cfg->c0 || !cfg->c1 || !cfg->growth_mu ||
+        !cfg->growth_sigma || !cfg->growth_weights)
+        return fail(CG_ERR_ARG, "cg_save_config_bin: NULL argument");
+    const int n = cfg->seed_size, C = cfg->num_channels, K = cfg->num_kernels;
+    if (n < 1 || C < 1 || K < 1) return fail(CG_ERR_ARG, "cg_save_config_bin: empty config");
+    for (int k = 0; k < K; ++k)
+        if (cfg->c0[k] >= uint32_t(C) || cfg->c1[k] >= uint32_t(C))
+            return fail(CG_ERR_ARG, "kernel %d channel index outside [0, %d)", k, C);
+    std::vector<unsigned char> o;
+    o.reserve(seed_bin_header(K));
+    o.insert(o.end(), kSeedMagic, kSeedMagic + 8);
+    put_u32(o, uint32_t(n));
+    put_u32(o, uint32_t(C));
+    put_u32(o, uint32_t(K));
+    put_f32(o, cfg->temp);
+    for (int k = 0; k < K; ++k) put_u32(o, cfg->c1[k]);   // JSON c0
+    for (int k = 0; k < K; ++k) put_u32(o, cfg->c0[k]);   // JSON c1
+    for (int k = 0; k < K; ++k) put_f32(o, cfg->growth_mu[k]);
+    for (int k = 0; k < K; ++k) put_f32(o, cfg->growth_sigma[k]);
+    for (int k = 0; k < K; ++k) put_f32(o, cfg->growth_weights[k]);
+    o.resize(seed_bin_header(K), 0);
+    FILE* f = std::fopen(path, "wb");
+    if (!f) return fail(CG_ERR_IO, "cannot write seed file %s", path);
+    bool ok = std::fwrite(o.data(), 1, o.size(), f) == o.size();
+    // the seed in chunks, little-endian
+    const size_t total = size_t(C) * n * n;
+    std::vector<unsigned char> chunk;
+    for (size_t i = 0; ok && i < total; i += 65536) {
+        const size_t m = total - i < 65536 ? total - i : 65536;
+        chunk.resize(8 * m);
+        for (size_t j = 0; j < m; ++j) {
+            uint64_t u;
+            std::memcpy(&u, &cfg->seed_channels[i + j], 8);
+            for (int q = 0; q < 8; ++q) chunk[8 * j + q] = static_cast<unsigned char>(u >> (8 * q));
+        }
+        ok = std::fwrite(chunk.data(), 1, chunk.size(), f) == chunk.size();
+    }
+    if (std::fclose(f) != 0) ok = false;
+    if (!ok) return fail(CG_ERR_IO, "writing seed file %s failed", path);
     return CG_OK;
 }
 

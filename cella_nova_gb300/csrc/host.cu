@@ -183,10 +183,13 @@ struct cg_sim {
     int* err = nullptr;   // device error word written by bounded waits
     cudaGraphExec_t graph[2] = {nullptr, nullptr};     // one step, per parity
     cudaGraphExec_t graph8[2] = {nullptr, nullptr};    // kStepsPerGraph steps, per parity
+    cudaGraphExec_t graphR[2] = {nullptr, nullptr};    // one step that also renders
+    unsigned* render = nullptr;   // [n][n] packed 0x00RRGGBB
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     KernelGroups groups{};
-    GrowthParams gp{};
+    GrowthParams gp{};          // host copies of the folded parameters
     AdjointParams ap{};
+    DeviceParams* dparams = nullptr;   // the copies the kernels read
     Variants var{};
     float* abar = nullptr;          // backward scratch, allocated on first use
     float* utmp[2] = {nullptr, nullptr};   // cg_unroll scratch states
@@ -209,7 +212,7 @@ struct cg_sim {
         a.udbg = udbg;
         a.err = err;
         a.groups = groups;
-        a.gp = gp;
+        a.gp = &dparams->gp;
         a.var = var;
         return a;
     }
@@ -224,6 +227,8 @@ void release(cg_sim* s) {
         if (g) cudaGraphExecDestroy(g);
     for (auto& g : s->graph8)
         if (g) cudaGraphExecDestroy(g);
+    for (auto& g : s->graphR)
+        if (g) cudaGraphExecDestroy(g);
     for (auto& e : s->ev)
         if (e) cudaEventDestroy(e);
     cudaFree(s->state[0]);
@@ -237,6 +242,8 @@ void release(cg_sim* s) {
     cudaFree(s->mass_partial);
     cudaFree(s->mass_out);
     cudaFree(s->err);
+    cudaFree(s->dparams);
+    cudaFree(s->render);
     cudaFree(s->abar);
     cudaFree(s->utmp[0]);
     cudaFree(s->utmp[1]);
@@ -254,7 +261,9 @@ constexpr int kStepsPerGraph = 8;
 // the column pass of step t overwrites the U buffer of its parity, which every
 // inverse row pass of step t-2 read.  Everything else is per channel and in
 // stream order.
-cudaError_t capture_steps(cg_sim* s, int p0, int nsteps, cudaGraphExec_t* out) {
+// nsteps steps from parity p0 into one graph; with render, the last step's
+// diffusion kernels also write the render buffer.
+cudaError_t capture_steps(cg_sim* s, int p0, int nsteps, bool render, cudaGraphExec_t* out) {
     const int C = s->C;
     std::vector<cudaStream_t> st(C, nullptr);
     std::vector<cudaEvent_t> ecol(C, nullptr);
@@ -274,7 +283,8 @@ cudaError_t capture_steps(cg_sim* s, int p0, int nsteps, cudaGraphExec_t* out) {
         cudaError_t le = cudaEventRecord(fork, st[0]);
         for (int c = 1; c < C && le == cudaSuccess; ++c) le = cudaStreamWaitEvent(st[c], fork, 0);
         for (int t = 0; t < nsteps && le == cudaSuccess; ++t) {
-            const StepArgs a = s->args(p0 ^ (t & 1), nullptr);
+            StepArgs a = s->args(p0 ^ (t & 1), nullptr);
+            if (render && t == nsteps - 1) a.render = reinterpret_cast<unsigned char*>(s->render);
             for (int c = 0; c < C && le == cudaSuccess; ++c) {
                 le = s->ops->step_channel(a, kPhaseRowFwd, c, st[c]);
                 // U alternates with the parity, so the column pass of step t
@@ -315,8 +325,9 @@ cudaError_t capture_steps(cg_sim* s, int p0, int nsteps, cudaGraphExec_t* out) {
 
 int capture_graphs(cg_sim* s) {
     for (int p = 0; p < 2; ++p) {
-        cudaError_t e = capture_steps(s, p, 1, &s->graph[p]);
-        if (e == cudaSuccess) e = capture_steps(s, p, kStepsPerGraph, &s->graph8[p]);
+        cudaError_t e = capture_steps(s, p, 1, false, &s->graph[p]);
+        if (e == cudaSuccess) e = capture_steps(s, p, kStepsPerGraph, false, &s->graph8[p]);
+        if (e == cudaSuccess) e = capture_steps(s, p, 1, true, &s->graphR[p]);
         if (e != cudaSuccess) return cuda_fail(e, "capturing the step graph");
     }
     return CG_OK;
@@ -360,8 +371,19 @@ void build_adjoint_params(cg_sim* s) {
     }
 }
 
+// Enqueue the folded parameters (host copies) for the kernels, in stream
+// order: steps already enqueued keep the old values.
+int upload_params(cg_sim* s) {
+    DeviceParams h;
+    h.gp = s->gp;
+    h.ap = s->ap;
+    CG_CHECK(cudaMemcpyAsync(s->dparams, &h, sizeof(h), cudaMemcpyHostToDevice, s->stream),
+             "uploading growth parameters");
+    return CG_OK;
+}
+
 int recapture(cg_sim* s) {
-    for (auto* set : {s->graph, s->graph8})
+    for (auto* set : {s->graph, s->graph8, s->graphR})
         for (int p = 0; p < 2; ++p)
             if (set[p]) {
                 cudaGraphExecDestroy(set[p]);
@@ -397,8 +419,8 @@ BwdArgs bwd_args(cg_sim* s, const float* x, const float* ybar, float* xbar, doub
     a.kgrad = kgrad;
     a.err = s->err;
     a.groups = s->groups;
-    a.gp = s->gp;
-    a.ap = s->ap;
+    a.gp = &s->dparams->gp;
+    a.ap = &s->dparams->ap;
     return a;
 }
 
@@ -468,6 +490,10 @@ int cg_create(int n, int C, int K, const uint32_t* c0, const uint32_t* c1, const
     if (rc == CG_OK) chk(cudaMalloc(&s->mass_out, sizeof(double) * C), "cudaMalloc(mass)");
     if (rc == CG_OK) chk(cudaMalloc(&s->err, sizeof(int)), "cudaMalloc(err)");
     if (rc == CG_OK) chk(cudaMemset(s->err, 0, sizeof(int)), "memset(err)");
+    if (rc == CG_OK) chk(cudaMalloc(&s->dparams, sizeof(DeviceParams)), "cudaMalloc(params)");
+    if (rc == CG_OK) chk(cudaMalloc(&s->render, sizeof(unsigned) * px), "cudaMalloc(render)");
+    if (rc == CG_OK) chk(cudaMemsetAsync(s->render, 0, sizeof(unsigned) * px, s->stream), "memset");
+    if (rc == CG_OK) rc = upload_params(s);
     for (int i = 0; i < 4 && rc == CG_OK; ++i) chk(cudaEventCreate(&s->ev[i]), "cudaEventCreate");
     if (rc == CG_OK) chk(cudaMemsetAsync(s->state[0], 0, sizeof(float) * C * px, s->stream), "memset");
     if (rc == CG_OK) chk(cudaMemsetAsync(s->state[1], 0, sizeof(float) * C * px, s->stream), "memset");
@@ -552,6 +578,47 @@ int cg_step(cg_sim* s, int nsteps) {
 }
 
 int cg_iterate(cg_sim* s) { return cg_step(s, 1); }
+
+int cg_iterate_and_render(cg_sim* s) {
+    if (!s) return fail(CG_ERR_ARG, "cg_iterate_and_render: NULL handle");
+    CG_CHECK(cudaGraphLaunch(s->graphR[s->cur], s->stream), "cudaGraphLaunch");
+    s->cur ^= 1;
+    return CG_OK;
+}
+
+int cg_render(cg_sim* s) {
+    if (!s) return fail(CG_ERR_ARG, "cg_render: NULL handle");
+    CG_CHECK(launch_render(s->state[s->cur], s->C, s->px(), s->render, s->stream),
+             "launching render");
+    return CG_OK;
+}
+
+int cg_download_render(cg_sim* s, uint8_t* rgb24) {
+    if (!s || !rgb24) return fail(CG_ERR_ARG, "cg_download_render: NULL argument");
+    auto* bytes = static_cast<unsigned char*>(s->staging);   // 8 B per pixel, 3 used
+    CG_CHECK(launch_rgb24(s->render, bytes, s->px(), s->stream), "launching RGB24 conversion");
+    CG_CHECK(cudaMemcpyAsync(rgb24, bytes, 3 * s->px(), cudaMemcpyDeviceToHost, s->stream),
+             "downloading render");
+    CG_CHECK(cudaStreamSynchronize(s->stream), "cudaStreamSynchronize");
+    CG_SYNC_CHECK(s);
+    return CG_OK;
+}
+
+int cg_download_render_packed(cg_sim* s, uint32_t* out) {
+    if (!s || !out) return fail(CG_ERR_ARG, "cg_download_render_packed: NULL argument");
+    CG_CHECK(cudaMemcpyAsync(out, s->render, sizeof(uint32_t) * s->px(), cudaMemcpyDeviceToHost,
+                             s->stream),
+             "downloading render");
+    CG_CHECK(cudaStreamSynchronize(s->stream), "cudaStreamSynchronize");
+    CG_SYNC_CHECK(s);
+    return CG_OK;
+}
+
+int cg_render_ptr(cg_sim* s, const uint32_t** out) {
+    if (!s || !out) return fail(CG_ERR_ARG, "cg_render_ptr: NULL argument");
+    *out = s->render;
+    return CG_OK;
+}
 
 int cg_iterate_on(cg_sim* s, cg_stream_t stream) {
     if (!s) return fail(CG_ERR_ARG, "cg_iterate_on: NULL handle");
@@ -701,14 +768,27 @@ int cg_set_params(cg_sim* s, const float* mu, const float* sigma, const float* w
     int rc = validate_world(s->n, s->C, s->K, s->c0.data(), s->c1.data(), mu, sigma, weights,
                             temp, &logn);
     if (rc != CG_OK) return rc;
-    CG_CHECK(cudaStreamSynchronize(s->stream), "cudaStreamSynchronize");
     s->mu.assign(mu, mu + s->K);
     s->sigma.assign(sigma, sigma + s->K);
     s->w.assign(weights, weights + s->K);
-    s->temp = temp;
     build_groups(s->C, s->K, s->c0.data(), s->c1.data(), mu, sigma, weights, &s->groups, &s->gp);
     build_adjoint_params(s);
+    rc = upload_params(s);
+    if (rc != CG_OK || temp == s->temp) return rc;
+    // temp is a launch argument of the captured graphs
+    CG_CHECK(cudaStreamSynchronize(s->stream), "cudaStreamSynchronize");
+    s->temp = temp;
     return recapture(s);
+}
+
+int cg_set_params_device(cg_sim* s, const float* dev_mu, const float* dev_sigma,
+                         const float* dev_weights) {
+    if (!s || !dev_mu || !dev_sigma || !dev_weights)
+        return fail(CG_ERR_ARG, "cg_set_params_device: NULL argument");
+    CG_CHECK(launch_fold_params(dev_mu, dev_sigma, dev_weights, s->C, s->K, s->groups, s->dparams,
+                                s->stream),
+             "launching parameter folding");
+    return CG_OK;
 }
 
 int cg_step_from(cg_sim* s, const float* x_in, float* x_out) {

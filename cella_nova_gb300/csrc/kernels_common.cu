@@ -4,6 +4,7 @@
 
 #include "cella_gpu.h"
 #include "cella_internal.h"
+#include "render.cuh"
 
 namespace cg {
 
@@ -70,6 +71,83 @@ cudaError_t launch_mass_f64(const float* x, int C, size_t px, double* partial, i
                             double* out, cudaStream_t s) {
     k_mass_partial<<<dim3(nblocks, C), 256, 0, s>>>(x, px, partial);
     k_mass_final<<<C, 256, 0, s>>>(partial, nblocks, out);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Render the current state on its own (RenderPhase::run, render.rs:143-153):
+// one packed 0x00RRGGBB word per pixel from channels 0..2, the same levels the
+// diffusion epilogue writes.
+// ---------------------------------------------------------------------------
+__global__ void k_render(const float* __restrict__ x, int C, size_t px,
+                         unsigned* __restrict__ out) {
+    for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < px;
+         i += size_t(gridDim.x) * blockDim.x) {
+        unsigned v = render_level(__ldg(&x[i])) << 16;
+        if (C > 1) v |= render_level(__ldg(&x[px + i])) << 8;
+        if (C > 2) v |= render_level(__ldg(&x[2 * px + i]));
+        out[i] = v;
+    }
+}
+
+// download_render's conversion (mod.rs:322-329): packed words -> RGB24 bytes.
+__global__ void k_rgb24(const unsigned* __restrict__ in, unsigned char* __restrict__ out,
+                        size_t px) {
+    for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < px;
+         i += size_t(gridDim.x) * blockDim.x) {
+        const unsigned v = __ldg(&in[i]);
+        out[3 * i] = static_cast<unsigned char>(v >> 16);
+        out[3 * i + 1] = static_cast<unsigned char>(v >> 8);
+        out[3 * i + 2] = static_cast<unsigned char>(v);
+    }
+}
+
+static int grid_for(size_t count) {
+    return int((count + 255) / 256 < 4096 ? (count + 255) / 256 : 4096);
+}
+
+cudaError_t launch_render(const float* x, int C, size_t px, unsigned* out, cudaStream_t s) {
+    k_render<<<grid_for(px), 256, 0, s>>>(x, C, px, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_rgb24(const unsigned* in, unsigned char* out, size_t px, cudaStream_t s) {
+    k_rgb24<<<grid_for(px), 256, 0, s>>>(in, out, px);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// The growth-parameter folding of build_groups / build_adjoint_params, on the
+// device, so parameters produced on the device (an optimiser step) reach the
+// kernels without a host round trip.  Same formulas and summation order as
+// the host, hence the same bits.  c1 (AdjointParams::cout) is left as is.
+// ---------------------------------------------------------------------------
+__global__ void k_fold_params(const float* __restrict__ mu, const float* __restrict__ sigma,
+                              const float* __restrict__ w, int C, int K,
+                              const __grid_constant__ KernelGroups g,
+                              DeviceParams* __restrict__ p) {
+    const int t = threadIdx.x;
+    if (t < K) {
+        const float m = mu[t], wk = w[t];
+        const double sg = double(sigma[t]);
+        p->gp.mu[t] = m;
+        p->gp.c2[t] = float(-1.4426950408889634 / (2.0 * sg * sg));
+        p->gp.w2[t] = 2.0f * wk;
+        p->ap.mu[t] = m;
+        p->ap.w[t] = wk;
+        p->ap.inv_s2[t] = float(1.0 / (sg * sg));
+        p->ap.inv_s3[t] = float(1.0 / (sg * sg * sg));
+    }
+    if (t < C) {
+        float ws = 0.f;
+        for (int i = 0; i < g.out_count[t]; ++i) ws += w[g.out_idx[g.out_start[t] + i]];
+        p->gp.wsum[t] = ws;
+    }
+}
+
+cudaError_t launch_fold_params(const float* mu, const float* sigma, const float* w, int C, int K,
+                               const KernelGroups& g, DeviceParams* p, cudaStream_t s) {
+    k_fold_params<<<1, 64, 0, s>>>(mu, sigma, w, C, K, g, p);
     return cudaGetLastError();
 }
 

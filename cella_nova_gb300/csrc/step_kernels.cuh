@@ -23,6 +23,7 @@
 #include "cella_internal.h"
 #include "async_copy.cuh"
 #include "fft.cuh"
+#include "render.cuh"
 
 namespace cg {
 
@@ -406,11 +407,11 @@ __global__ void __launch_bounds__(Geo<LOGN, V>::RT, 512 / Geo<LOGN, V>::RT) k_ro
                                                          float* __restrict__ A,
                                                          const float2* __restrict__ tw,
                                                          const __grid_constant__ KernelGroups groups,
-                                                         const __grid_constant__ GrowthParams gp,
+                                                         const GrowthParams* __restrict__ gp,
                                                          float temp, float* __restrict__ udbg,
                                                          float udbg_scale, int cbase) {
     extern __shared__ __align__(128) float2 sm_c2r[];
-    row_c2r_growth_body<LOGN, V>(U, A, tw, groups, gp, temp, udbg, udbg_scale,
+    row_c2r_growth_body<LOGN, V>(U, A, tw, groups, *gp, temp, udbg, udbg_scale,
                                  blockIdx.y + cbase, blockIdx.x * Geo<LOGN, V>::RB, sm_c2r);
 }
 
@@ -462,7 +463,8 @@ template <int LOGN, int V = 0>
 __device__ __forceinline__ void diffusion_body(const float* __restrict__ A,
                                                const float* __restrict__ x,
                                                float* __restrict__ out, int c, int x0, int y0,
-                                               float* smf) {
+                                               float* smf, unsigned char* render = nullptr,
+                                               int nch = 0) {
     using G = Geo<LOGN, V>;
     using D = DiffGeo<LOGN, V>;
     constexpr int N = G::N, TX = G::TX, TY = G::TY;
@@ -556,19 +558,24 @@ __device__ __forceinline__ void diffusion_body(const float* __restrict__ A,
     for_tile<QH, TX>([&](int r, int q) { sQs[r][q] = sQ[r][q] + sQ[r][q + 1] + sQ[r][q + 2]; });
     __syncthreads();
     float* oc = out + size_t(c) * N * N;
+    const bool draw = render != nullptr && c < 3;
     for_tile<TY, TX>([&](int r, int q) {
         const float a = sAh[r + 2][q + 2] + sAl[r + 2][q + 2];
-        oc[size_t(y0 + r) * N + x0 + q] = a * ((sQs[r][q] + sQs[r + 1][q]) + sQs[r + 2][q]);
+        const size_t p = size_t(y0 + r) * N + x0 + q;
+        const float v = a * ((sQs[r][q] + sQs[r + 1][q]) + sQs[r + 2][q]);
+        oc[p] = v;
+        if (draw) render_store(render, nch, c, p, v);
     });
 }
 
 template <int LOGN, int V = 0>
 __global__ void __launch_bounds__(256) k_diffusion(const float* __restrict__ A,
                                                     const float* __restrict__ x,
-                                                    float* __restrict__ out, int cbase) {
+                                                    float* __restrict__ out, int cbase,
+                                                    unsigned char* __restrict__ render, int nch) {
     extern __shared__ __align__(128) float sm_diff[];
     diffusion_body<LOGN, V>(A, x, out, blockIdx.z + cbase, blockIdx.x * Geo<LOGN, V>::TX,
-                            blockIdx.y * Geo<LOGN, V>::TY, sm_diff);
+                            blockIdx.y * Geo<LOGN, V>::TY, sm_diff, render, nch);
 }
 
 // ---------------------------------------------------------------------------
@@ -652,7 +659,7 @@ template <int LOGN, int V>
 void launch_diff(const StepArgs& a, int c_lo, int nc, cudaStream_t st) {
     using G = Geo<LOGN, V>;
     k_diffusion<LOGN, V><<<dim3(G::N / G::TX, G::N / G::TY, nc), 256, DiffGeo<LOGN, V>::SMEM,
-                           st>>>(a.A, a.x_in, a.x_out, c_lo);
+                           st>>>(a.A, a.x_in, a.x_out, c_lo, a.render, a.C);
 }
 
 #define CG_VARIANT_SWITCH(v, FN, ...)            \

@@ -114,6 +114,49 @@ class GpuMaceLenia:
         """iterate_with_encoder (mod.rs:435): enqueue on a caller stream."""
         check(self._lib.cg_iterate_on(self._h, ctypes.c_void_p(stream)))
 
+    def set_params(self, mu, sigma, weights, temp=None):
+        """Replace growth mu/sigma/weights (K each) and temp; takes effect for
+        work enqueued afterwards."""
+        t = self.temp if temp is None else float(temp)
+        mu, sg, w = (np.ascontiguousarray(v, dtype=np.float32) for v in (mu, sigma, weights))
+        check(self._lib.cg_set_params(self._h, fptr(mu), fptr(sg), fptr(w), ctypes.c_float(t)))
+        self.temp = t
+
+    def set_params_device(self, mu_ptr: int, sigma_ptr: int, weights_ptr: int):
+        """The same from device arrays (K float32 each), folded on the device
+        in stream order."""
+        check(self._lib.cg_set_params_device(self._h, ctypes.c_void_p(mu_ptr),
+                                             ctypes.c_void_p(sigma_ptr),
+                                             ctypes.c_void_p(weights_ptr)))
+
+    def iterate_and_render(self):
+        """iterate_and_render (mod.rs:390): one step whose diffusion also
+        writes the packed 0x00RRGGBB render buffer."""
+        check(self._lib.cg_iterate_and_render(self._h))
+
+    def render(self):
+        """RenderPhase::run (render.rs:143): render the current state."""
+        check(self._lib.cg_render(self._h))
+
+    def download_render(self):
+        """download_render (mod.rs:302): RGB24 bytes, shape (n, n, 3)."""
+        out = np.empty(self.total_elements * 3, dtype=np.uint8)
+        check(self._lib.cg_download_render(
+            self._h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8))))
+        return out.reshape(self.n, self.n, 3)
+
+    def download_render_packed(self):
+        """The packed render words, shape (n, n) uint32."""
+        out = np.empty(self.total_elements, dtype=np.uint32)
+        check(self._lib.cg_download_render_packed(self._h, uptr(out)))
+        return out.reshape(self.n, self.n)
+
+    def render_ptr(self) -> int:
+        """Device address of the render buffer (n*n uint32)."""
+        p = ctypes.c_void_p()
+        check(self._lib.cg_render_ptr(self._h, ctypes.byref(p)))
+        return p.value
+
     def timed_iterate(self):
         """[conv, growth, diffusion, copy] device ms for one step (mod.rs:469)."""
         ms = np.zeros(4, dtype=np.float64)
@@ -206,11 +249,24 @@ class GpuMaceLenia:
 # File formats (ml-rs/config.rs) through the C ABI
 # ---------------------------------------------------------------------------
 
+SEED_MAGIC = b"CNSEED01"
+
+
+def is_seed_bin(path) -> bool:
+    try:
+        with open(path, "rb") as f:
+            return f.read(8) == SEED_MAGIC
+    except OSError:
+        return False   # the JSON loader reports the unreadable file
+
+
 def load_config(path):
-    """load_config (config.rs:32-47) -> dict in orchestrator order (c0 = input)."""
+    """load_config (config.rs:32-47) -> dict in orchestrator order (c0 = input).
+    Reads seed/{name}.json or its binary twin (magic CNSEED01)."""
     lib = _abi.load()
     cfg = _abi.cg_config()
-    check(lib.cg_load_config_json(str(path).encode(), ctypes.byref(cfg)))
+    loader = lib.cg_load_config_bin if is_seed_bin(path) else lib.cg_load_config_json
+    check(loader(str(path).encode(), ctypes.byref(cfg)))
     try:
         n, C, K = cfg.seed_size, cfg.num_channels, cfg.num_kernels
         seed = np.ctypeslib.as_array(cfg.seed_channels, shape=(C * n * n,)).copy()
@@ -227,6 +283,21 @@ def load_config(path):
     finally:
         lib.cg_free_config(ctypes.byref(cfg))
     return out
+
+
+def save_config_bin(path, cfg):
+    """Write a config dict (orchestrator order, as load_config returns it) as
+    a binary seed file."""
+    lib = _abi.load()
+    K, C, n = int(cfg["num_kernels"]), int(cfg["num_channels"]), int(cfg["seed_size"])
+    seed = np.ascontiguousarray(cfg["seed_channels"], dtype=np.float64).reshape(C * n * n)
+    arrs = {k: np.ascontiguousarray(cfg[k], dtype=np.uint32) for k in ("c0", "c1")}
+    arrs.update({k: np.ascontiguousarray(cfg[k], dtype=np.float32)
+                 for k in ("growth_mu", "growth_sigma", "growth_weights")})
+    c = _abi.cg_config(n, C, K, dptr(seed), uptr(arrs["c0"]), uptr(arrs["c1"]),
+                       fptr(arrs["growth_mu"]), fptr(arrs["growth_sigma"]),
+                       fptr(arrs["growth_weights"]), float(cfg.get("temp", 1.0)))
+    check(lib.cg_save_config_bin(str(path).encode(), ctypes.byref(c)))
 
 
 def load_kernels(path, num_kernels, target_size):

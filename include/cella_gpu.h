@@ -99,6 +99,29 @@ int cg_step(cg_sim* sim, int nsteps);
  * the caller's stream instead of the handle's. */
 int cg_iterate_on(cg_sim* sim, cg_stream_t stream);
 
+/* GpuMaceLenia::iterate_and_render, mod.rs:390-431: one step whose diffusion
+ * kernels also write the render buffer (render_main, compute_1024.wgsl:
+ * 428-443): per pixel the packed word 0x00RRGGBB with R, G, B =
+ * u32(sqrt(clamp(1.5 c, 0, 1)) * 255) of channels 0, 1, 2 (0 for channels the
+ * world lacks).  Enqueued. */
+int cg_iterate_and_render(cg_sim* sim);
+
+/* RenderPhase::run, render.rs:143-153: render the current state without
+ * stepping.  Enqueued. */
+int cg_render(cg_sim* sim);
+
+/* GpuMaceLenia::download_render, mod.rs:302-335: blocking copy of the render
+ * buffer as RGB24 bytes (3*n*n, row-major, R first).  The buffer holds zeros
+ * until the first render. */
+int cg_download_render(cg_sim* sim, uint8_t* rgb24);
+
+/* The packed render words themselves (n*n uint32_t), blocking. */
+int cg_download_render_packed(cg_sim* sim, uint32_t* out);
+
+/* Device address of the render buffer (n*n uint32_t, owned by the handle),
+ * for a consumer on the GPU; valid until cg_destroy. */
+int cg_render_ptr(cg_sim* sim, const uint32_t** dev_ptr);
+
 /* GpuMaceLenia::download_all_channels, mod.rs:236-263: blocking copy of the
  * C*n*n f32 state, channel-major. */
 int cg_download_channels(cg_sim* sim, float* out);
@@ -178,14 +201,22 @@ int cg_synchronize(cg_sim* sim);
 /* ---------------------------------------------------------------------------
  * Differentiation (no counterpart in the Rust orchestrator; the reference
  * differentiates its PyTorch model, train/diff_lenia_org.py, with autograd).
- * All array arguments here are DEVICE pointers on the handle's device; work
- * is enqueued on the handle's stream.
+ * Array arguments here are DEVICE pointers on the handle's device, except
+ * those of cg_set_params; work is enqueued on the handle's stream.
  * ------------------------------------------------------------------------- */
 
-/* Replace mu/sigma/weights (K each) and temp; the step graphs are
- * re-captured.  Same checks as cg_create. */
+/* Replace mu/sigma/weights (K each, HOST arrays) and temp.  Same checks as
+ * cg_create.  The parameters reach the kernels through a device-resident
+ * block, updated in stream order (work enqueued earlier keeps the old
+ * values); only a change of temp re-captures the step graphs. */
 int cg_set_params(cg_sim* sim, const float* mu, const float* sigma, const float* weights,
                   float temp);
+
+/* The same from DEVICE arrays, folded on the device by one kernel enqueued on
+ * the handle's stream (capturable in a CUDA graph, e.g. after an optimiser
+ * step).  No checks: the values are used as given. */
+int cg_set_params_device(cg_sim* sim, const float* dev_mu, const float* dev_sigma,
+                         const float* dev_weights);
 
 /* One step from x_in to x_out (C*n*n f32 each, distinct). */
 int cg_step_from(cg_sim* sim, const float* x_in, float* x_out);
@@ -269,6 +300,18 @@ typedef struct {
 /* load_config, config.rs:32-47. */
 int cg_load_config_json(const char* path, cg_config* out);
 void cg_free_config(cg_config* cfg);
+
+/* Binary twin of seed/{name}.json (no reference counterpart; it replaces the
+ * ~12.6 M numbers of JSON text a 2048^2 three-channel seed takes with raw
+ * little-endian values).  The file holds exactly the JSON's fields,
+ * c0/c1 in the JSON's order, so JSON -> binary -> cg_config gives the same
+ * cg_config as the JSON itself:
+ *   "CNSEED01", u32 n, u32 C, u32 K, f32 temp, u32 c0_json[K], u32 c1_json[K],
+ *   f32 mu[K], f32 sigma[K], f32 weights[K], zero padding to 8 bytes,
+ *   f64 seed[C][n][n]. */
+int cg_load_config_bin(const char* path, cg_config* out);
+/* Write cfg (orchestrator c0/c1 order, as the loaders return it). */
+int cg_save_config_bin(const char* path, const cg_config* cfg);
 
 /* load_kernels, config.rs:56-125: K spectra resampled to target_n (spectral
  * zero-padding when the file holds a smaller grid, config.rs:81-116).

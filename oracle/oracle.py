@@ -16,6 +16,9 @@ Contents
 * ``load_config_np`` / ``load_kernels_np``: restatement of
   ml-rs/config.rs:32-125 (JSON seed format with the c0/c1 swap, .bin kernel
   spectra with the spectral zero-padding resample).
+* ``render_np`` / ``rgb24_np``: restatement of render_main
+  (ml-rs/shaders/compute_1024.wgsl:428-443) and of download_render's byte
+  conversion (ml-rs/orchestrator/mod.rs:322-329).
 
 The oracle is pinned by tests/test_oracle.py against golden vectors that the
 reference's own PyTorch model (train/diff_lenia_org.py) produced
@@ -194,3 +197,30 @@ def load_kernels_np(path, K, target):
         big[pad:pad + src, pad:pad + src] = centered
         out[k] = np.roll(big, (hd, hd), axis=(0, 1))
     return out
+
+
+def render_np(state):
+    """Packed 0x00RRGGBB words (n, n) uint32 from channels 0, 1, 2 of an f32
+    state: level = u32(sqrt(clamp(1.5 c, 0, 1)) * 255), all in float32
+    (compute_1024.wgsl:428-443).  Channels the state lacks give 0; a NaN
+    clamps to 0 (fmax/fmin semantics)."""
+    st = np.asarray(state, dtype=np.float32)
+
+    def level(c):
+        v = np.fmin(np.fmax(c * np.float32(1.5), np.float32(0.0)), np.float32(1.0))
+        return (np.sqrt(v) * np.float32(255.0)).astype(np.uint32)
+
+    out = level(st[0]) << np.uint32(16)
+    if st.shape[0] > 1:
+        out |= level(st[1]) << np.uint32(8)
+    if st.shape[0] > 2:
+        out |= level(st[2])
+    return out
+
+
+def rgb24_np(packed):
+    """download_render's conversion (mod.rs:322-329): (n, n) words -> (n, n, 3)
+    bytes R, G, B."""
+    p = np.asarray(packed, dtype=np.uint32)
+    return np.stack([(p >> 16) & 255, (p >> 8) & 255, p & 255], axis=-1).astype(np.uint8)
+

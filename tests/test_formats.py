@@ -112,3 +112,62 @@ def test_malformed_json(tmp_path):
     with pytest.raises(CellaError, match="FORMAT"):
         load_config(str(p))
     assert os.path.exists(p)
+
+
+# -- binary twin of the seed JSON ---------------------------------------------
+
+def _same_config(a, b):
+    for key in ("seed_size", "num_channels", "num_kernels"):
+        assert a[key] == b[key], key
+    for key in ("seed_channels", "c0", "c1", "growth_mu", "growth_sigma", "growth_weights"):
+        np.testing.assert_array_equal(a[key], b[key], err_msg=key)
+    assert a["temp"] == b["temp"]
+
+
+def test_seed_bin_round_trip_equals_json(creature_files, tmp_path):
+    from cella_nova_gb300.orchestrator import save_config_bin
+    cr, js, _ = creature_files
+    from_json = load_config(js)
+    path = tmp_path / "crit.seedbin"
+    save_config_bin(path, from_json)
+    _same_config(load_config(path), from_json)
+    # bit-exact f64 seeds, JSON-order channel fields
+    raw = path.read_bytes()
+    assert raw[:8] == b"CNSEED01"
+    assert len(raw) == 24 + 5 * 4 * cr.K + 4 + 8 * cr.C * cr.n * cr.n   # 9 kernels: 4 pad bytes
+
+
+def test_seed_bin_python_writer_matches_c_writer(creature_files, tmp_path):
+    from cella_nova_gb300.creature import write_seed_bin
+    from cella_nova_gb300.orchestrator import save_config_bin
+    cr, js, _ = creature_files
+    a, b = tmp_path / "py.seedbin", tmp_path / "c.seedbin"
+    write_seed_bin(str(a), cr)
+    save_config_bin(b, load_config(js))
+    assert a.read_bytes() == b.read_bytes()
+
+
+def test_seed_bin_rejects_bad_files(creature_files, tmp_path):
+    from cella_nova_gb300.creature import write_seed_bin
+    cr, _, _ = creature_files
+    good = tmp_path / "g.seedbin"
+    write_seed_bin(str(good), cr)
+    raw = good.read_bytes()
+    cases = {
+        "truncated": raw[:-8],
+        "index": raw[:24] + (7).to_bytes(4, "little") + raw[28:],   # channel 7 of 3
+    }
+    for name, data in cases.items():
+        p = tmp_path / f"{name}.seedbin"
+        p.write_bytes(data)
+        with pytest.raises(CellaError) as e:
+            load_config(p)
+        assert e.value.code == -6, name     # CG_ERR_FORMAT
+
+
+def test_setup_simulation_accepts_seed_bin(creature_files, tmp_path):
+    from cella_nova_gb300.creature import write_seed_bin
+    cr, js, _ = creature_files
+    p = tmp_path / "s.seedbin"
+    write_seed_bin(str(p), cr)
+    _same_config(load_config(p), load_config(js))

@@ -1,0 +1,82 @@
+"""Render (iterate_and_render, render, download_render) and the
+device-resident growth parameters, through the C ABI."""
+import numpy as np
+import pytest
+
+from cella_nova_gb300 import GpuMaceLenia
+from cella_nova_gb300.creature import make_creature
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("n,C", [(64, 1), (64, 2), (128, 3), (64, 4), (256, 3)])
+def test_iterate_and_render_matches_oracle_render(n, C):
+    cr = make_creature(n, C, seed=30 + C, radius=(max(2.0, n / 16), max(4.0, n / 6)),
+                       seed_box=n // 2)
+    with GpuMaceLenia.from_creature(cr) as a, GpuMaceLenia.from_creature(cr) as b:
+        assert (a.download_render_packed() == 0).all()      # zeros until the first render
+        for _ in range(3):
+            a.iterate_and_render()
+            b.iterate()
+            x = a.state()
+            np.testing.assert_array_equal(x, b.state())    # rendering does not change the step
+            packed = a.download_render_packed()
+            np.testing.assert_array_equal(packed, O.render_np(x))
+        np.testing.assert_array_equal(a.download_render(), O.rgb24_np(packed))
+        # the standalone render of the same state gives the same words
+        b.render()
+        np.testing.assert_array_equal(b.download_render_packed(), packed)
+        # graph steps afterwards leave the render buffer alone
+        a.run_steps(9)
+        np.testing.assert_array_equal(a.download_render_packed(), packed)
+
+
+def test_render_saturates_and_clamps():
+    n, C = 64, 3
+    cr = make_creature(n, C, seed=5, radius=(4, 10), seed_box=32)
+    with GpuMaceLenia.from_creature(cr) as sim:
+        x = np.zeros((C, n, n), np.float64)
+        x[0, :, : n // 2] = 5.0
+        x[1] = np.linspace(-1, 1, n * n).reshape(n, n)
+        x[2, n // 2:] = 0.3
+        sim.upload_state(x)
+        sim.render()
+        got = sim.download_render_packed()
+        np.testing.assert_array_equal(got, O.render_np(x.astype(np.float32)))
+
+
+def test_set_params_takes_effect_without_changing_other_steps():
+    """New parameters reach the captured graphs (device-resident block): a
+    world whose parameters were replaced steps exactly like a world created
+    with them."""
+    cr = make_creature(128, 3, seed=40, radius=(8, 20), seed_box=64)
+    cr2 = make_creature(128, 3, seed=41, radius=(8, 20), seed_box=64)
+    with GpuMaceLenia.from_creature(cr) as a:
+        a.run_steps(2)
+        x = a.state()
+        a.set_params(cr2.mu, cr2.sigma, cr2.weights, cr.temp)
+        a.run_steps(9)
+        got = a.state()
+    with GpuMaceLenia((128, 128), 3, cr.K, cr.c0, cr.c1, cr2.mu, cr2.sigma, cr2.weights,
+                      cr.temp) as b:
+        for k in range(cr.K):
+            b.set_kernel(cr.kspec[k], k)
+        b.upload_state(x)
+        b.run_steps(9)
+        np.testing.assert_array_equal(got, b.state())
+
+
+def test_set_params_device_equals_host_folding():
+    import torch
+    cr = make_creature(128, 3, seed=42, radius=(8, 20), seed_box=64)
+    cr2 = make_creature(128, 3, seed=43, radius=(8, 20), seed_box=64)
+    dev = [torch.tensor(np.asarray(v, np.float32), device="cuda")
+           for v in (cr2.mu, cr2.sigma, cr2.weights)]
+    torch.cuda.synchronize()
+    with GpuMaceLenia.from_creature(cr) as a, GpuMaceLenia.from_creature(cr) as b:
+        a.set_params(cr2.mu, cr2.sigma, cr2.weights, cr.temp)
+        b.set_params_device(*[t.data_ptr() for t in dev])
+        a.run_steps(5)
+        b.run_steps(5)
+        np.testing.assert_array_equal(a.state(), b.state())
