@@ -40,6 +40,13 @@ class cg_config(ctypes.Structure):
     ]
 
 
+class cg_ring_spec(ctypes.Structure):
+    _fields_ = [("family", ctypes.c_int), ("rings", ctypes.c_int), ("radius", ctypes.c_float),
+                ("width", ctypes.c_float)]
+
+
+RING_SHELL, RING_GAUSS, MAX_RINGS = 0, 1, 8
+
 _P = ctypes.c_void_p
 _I = ctypes.c_int
 _F = ctypes.c_float
@@ -58,6 +65,8 @@ SIGNATURES = {
     "cg_set_kernel_device": ([_P, _I, _P], _I),
     "cg_set_params": ([_P, _FP, _FP, _FP, _F], _I),
     "cg_set_params_device": ([_P, _P, _P, _P], _I),
+    "cg_build_ring_kernels": ([_P, _P, _P], _I),
+    "cg_ring_weight_grad": ([_P, _P, _P, _P, _P], _I),
     "cg_iterate_and_render": ([_P], _I),
     "cg_render": ([_P], _I),
     "cg_download_render": ([_P, ctypes.POINTER(ctypes.c_uint8)], _I),

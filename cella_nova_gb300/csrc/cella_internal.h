@@ -94,6 +94,16 @@ struct BwdArgs {
     const AdjointParams* ap;  // device-resident
 };
 
+// Ring-kernel descriptors for the on-GPU kernel builder (kernels_common.cu).
+constexpr int kMaxRings = 8;
+constexpr int kRingBlocks = 64;   // blocks per kernel in the builder's sums
+struct RingSet {
+    int family[kMaxK];    // 0: Lenia shells exp(4 - 1/(t(1-t))), 1: sigmoid-gated Gaussian ring
+    int rings[kMaxK];     // shells per kernel (family 0), 1 for family 1
+    float radius[kMaxK];  // px: R (family 0), global_r * radius (family 1)
+    float width[kMaxK];   // family 1: ring width (in units of radius)
+};
+
 // The per-world parameter block the kernels read from device memory.
 struct DeviceParams {
     GrowthParams gp;
@@ -116,6 +126,8 @@ typedef cudaError_t (*prepare_fn)();
 typedef int (*twiddle_count_fn)();
 typedef cudaError_t (*launch_bwd_fn)(const BwdArgs&, cudaStream_t);
 typedef cudaError_t (*launch_step_channel_fn)(const StepArgs&, int phases, int c, cudaStream_t);
+typedef cudaError_t (*kspec_cols_fn)(const float2* rows, float2* kspec, const float2* tw,
+                                      const double* zsum, int K, cudaStream_t);
 typedef cudaError_t (*kgrad_final_fn)(float2* kgrad, float* hbar, int K, const float2* tw,
                                       cudaStream_t);
 
@@ -128,6 +140,8 @@ struct SizeOps {
     kgrad_final_fn kgrad_final;
     prepare_fn prepare_backward;
     launch_step_channel_fn step_channel;   // phases of one channel
+    prepare_fn prepare_builder;
+    kspec_cols_fn kspec_cols;   // kernel builder: row spectra -> packed kernel spectra
 };
 
 // Fill the twiddle buffer of an n-point grid (host side, double precision).
@@ -156,6 +170,14 @@ cudaError_t launch_render(const float* x, int C, size_t px, unsigned* out, cudaS
 cudaError_t launch_rgb24(const unsigned* in, unsigned char* out, size_t px, cudaStream_t s);
 cudaError_t launch_fold_params(const float* mu, const float* sigma, const float* w, int C, int K,
                                const KernelGroups& g, DeviceParams* p, cudaStream_t s);
+// Spatial ring kernels h[K][n][n] (unnormalised), their per-ring sums and
+// zsum[k] = sum of h_k (FP64; partial: K * kRingBlocks * kMaxRings).
+cudaError_t launch_ring_build(int n, int K, const RingSet& rs, const float* ring_w, float* h,
+                              double* partial, double* ring_s, double* zsum, cudaStream_t s);
+// d loss / d ring weight from hbar[K][n][n] = d loss / d h (normalised h).
+cudaError_t launch_ring_grad(int n, int K, const RingSet& rs, const float* ring_w,
+                             const float* hbar, double* partial, const double* ring_s,
+                             const double* zsum, float* grad, cudaStream_t s);
 constexpr int kMassBlocks = 296;   // 2 per SM on a 148/152-SM part
 
 }  // namespace cg

@@ -185,6 +185,9 @@ struct cg_sim {
     cudaGraphExec_t graph8[2] = {nullptr, nullptr};    // kStepsPerGraph steps, per parity
     cudaGraphExec_t graphR[2] = {nullptr, nullptr};    // one step that also renders
     unsigned* render = nullptr;   // [n][n] packed 0x00RRGGBB
+    double* ring_partial = nullptr;   // kernel builder: K * kRingBlocks * kMaxRings
+    double* ring_s = nullptr;         // K * kMaxRings per-ring sums of the last build
+    double* zsum = nullptr;           // K normalisers of the last build
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     KernelGroups groups{};
     GrowthParams gp{};          // host copies of the folded parameters
@@ -244,6 +247,9 @@ void release(cg_sim* s) {
     cudaFree(s->err);
     cudaFree(s->dparams);
     cudaFree(s->render);
+    cudaFree(s->ring_partial);
+    cudaFree(s->ring_s);
+    cudaFree(s->zsum);
     cudaFree(s->abar);
     cudaFree(s->utmp[0]);
     cudaFree(s->utmp[1]);
@@ -424,6 +430,27 @@ BwdArgs bwd_args(cg_sim* s, const float* x, const float* ybar, float* xbar, doub
     return a;
 }
 
+int ring_set(const cg_sim* s, const cg_ring_spec* specs, RingSet* rs, const char* who) {
+    *rs = RingSet{};
+    for (int k = 0; k < s->K; ++k) {
+        const cg_ring_spec& r = specs[k];
+        if (r.family != CG_RING_SHELL && r.family != CG_RING_GAUSS)
+            return fail(CG_ERR_ARG, "%s: kernel %d: unknown ring family %d", who, k, r.family);
+        if (r.family == CG_RING_SHELL && (r.rings < 1 || r.rings > CG_MAX_RINGS))
+            return fail(CG_ERR_ARG, "%s: kernel %d: %d rings outside [1, %d]", who, k, r.rings,
+                        CG_MAX_RINGS);
+        if (!(r.radius > 0.f) || !std::isfinite(r.radius))
+            return fail(CG_ERR_ARG, "%s: kernel %d: radius must be positive", who, k);
+        if (r.family == CG_RING_GAUSS && (!(r.width > 0.f) || !std::isfinite(r.width)))
+            return fail(CG_ERR_ARG, "%s: kernel %d: width must be positive", who, k);
+        rs->family[k] = r.family;
+        rs->rings[k] = r.family == CG_RING_SHELL ? r.rings : 1;
+        rs->radius[k] = r.radius;
+        rs->width[k] = r.width;
+    }
+    return CG_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -493,6 +520,12 @@ int cg_create(int n, int C, int K, const uint32_t* c0, const uint32_t* c1, const
     if (rc == CG_OK) chk(cudaMalloc(&s->dparams, sizeof(DeviceParams)), "cudaMalloc(params)");
     if (rc == CG_OK) chk(cudaMalloc(&s->render, sizeof(unsigned) * px), "cudaMalloc(render)");
     if (rc == CG_OK) chk(cudaMemsetAsync(s->render, 0, sizeof(unsigned) * px, s->stream), "memset");
+    if (rc == CG_OK)
+        chk(cudaMalloc(&s->ring_partial, sizeof(double) * K * kRingBlocks * kMaxRings),
+            "cudaMalloc(builder)");
+    if (rc == CG_OK) chk(cudaMalloc(&s->ring_s, sizeof(double) * K * kMaxRings), "cudaMalloc(builder)");
+    if (rc == CG_OK) chk(cudaMalloc(&s->zsum, sizeof(double) * K), "cudaMalloc(builder)");
+    if (rc == CG_OK) chk(s->ops->prepare_builder(), "configuring builder kernels");
     if (rc == CG_OK) rc = upload_params(s);
     for (int i = 0; i < 4 && rc == CG_OK; ++i) chk(cudaEventCreate(&s->ev[i]), "cudaEventCreate");
     if (rc == CG_OK) chk(cudaMemsetAsync(s->state[0], 0, sizeof(float) * C * px, s->stream), "memset");
@@ -779,6 +812,41 @@ int cg_set_params(cg_sim* s, const float* mu, const float* sigma, const float* w
     CG_CHECK(cudaStreamSynchronize(s->stream), "cudaStreamSynchronize");
     s->temp = temp;
     return recapture(s);
+}
+
+int cg_build_ring_kernels(cg_sim* s, const cg_ring_spec* specs, const float* dev_ring_weights) {
+    if (!s || !specs) return fail(CG_ERR_ARG, "cg_build_ring_kernels: NULL argument");
+    RingSet rs;
+    int rc = ring_set(s, specs, &rs, "cg_build_ring_kernels");
+    if (rc != CG_OK) return rc;
+    // scratch: the two halves of U (free between steps, in stream order)
+    const size_t half = size_t(s->n / 2) * s->n;
+    float2* rows = s->U;
+    float* h = reinterpret_cast<float*>(s->U + size_t(s->K) * half);
+    CG_CHECK(launch_ring_build(s->n, s->K, rs, dev_ring_weights, h, s->ring_partial, s->ring_s,
+                               s->zsum, s->stream),
+             "launching the ring builder");
+    StepArgs a = s->args(s->cur, nullptr);
+    a.C = s->K;   // the kernels pass through the row transform as channels
+    a.x_in = h;
+    a.rowspec = rows;
+    CG_CHECK(s->ops->step(a, kPhaseRowFwd, s->stream), "launching the builder's row transform");
+    CG_CHECK(s->ops->kspec_cols(rows, s->kspec, s->tw, s->zsum, s->K, s->stream),
+             "launching the builder's column transform");
+    return CG_OK;
+}
+
+int cg_ring_weight_grad(cg_sim* s, const cg_ring_spec* specs, const float* dev_ring_weights,
+                        const float* dev_hbar, float* dev_grad) {
+    if (!s || !specs || !dev_hbar || !dev_grad)
+        return fail(CG_ERR_ARG, "cg_ring_weight_grad: NULL argument");
+    RingSet rs;
+    int rc = ring_set(s, specs, &rs, "cg_ring_weight_grad");
+    if (rc != CG_OK) return rc;
+    CG_CHECK(launch_ring_grad(s->n, s->K, rs, dev_ring_weights, dev_hbar, s->ring_partial,
+                              s->ring_s, s->zsum, dev_grad, s->stream),
+             "launching the ring-weight gradient");
+    return CG_OK;
 }
 
 int cg_set_params_device(cg_sim* s, const float* dev_mu, const float* dev_sigma,

@@ -152,6 +152,175 @@ cudaError_t launch_fold_params(const float* mu, const float* sigma, const float*
 }
 
 // ---------------------------------------------------------------------------
+// On-GPU ring-kernel builder, spatial part.  Pixel (y, x) of the origin-
+// centred kernel sits at the wrapped offsets dy, dx in [-n/2, n/2) (the
+// ifftshift of generate_kernel_json.py:137 / example.rs:403).  Family 0 is
+// the Lenia shell kernel of the synthetic creatures: r = |d| / R, ring
+// l = floor(r B), t = frac(r B), value b_l exp(4 - 1/(t(1-t))) for r < 1.
+// Family 1 is the reference generator's Gaussian ring
+// (generate_kernel_json.py:106-146, example.rs:338-407): d = |d| / radius,
+// sigmoid(-(d-1) 10) exp(-(d-1/2)^2 / (2 w^2)), sigmoid(x) = (tanh(x/2)+1)/2.
+// Values are unnormalised; the sums per ring (FP64, fixed order) give the
+// normaliser, which the spectrum packing divides by.
+// ---------------------------------------------------------------------------
+struct RingValue {
+    int ring;      // -1: zero
+    float core;    // shell / Gaussian value before the ring weight
+};
+
+__device__ __forceinline__ RingValue ring_value(const RingSet& rs, int k, int n, size_t p) {
+    const int y = int(p / size_t(n)), x = int(p % size_t(n)), h = n / 2;
+    const float dy = float(((y + h) & (n - 1)) - h), dx = float(((x + h) & (n - 1)) - h);
+    const float dist = sqrtf(dy * dy + dx * dx);
+    RingValue v{-1, 0.f};
+    if (rs.family[k] == 0) {
+        const float r = dist / rs.radius[k];
+        const float rb = r * float(rs.rings[k]);
+        const float fl = floorf(rb);
+        const float t = rb - fl;
+        if (r < 1.f && t > 0.f && t < 1.f) {
+            v.ring = int(fl);
+            v.core = expf(4.f - 1.f / (t * (1.f - t)));
+        }
+    } else {
+        const float d = dist / rs.radius[k];
+        const float sig = 0.5f * tanhf(-(d - 1.f) * 10.f * 0.5f) + 0.5f;
+        const float df = d - 0.5f, w = rs.width[k];
+        v.ring = 0;
+        v.core = sig * expf(-(df * df) / (2.f * w * w));
+    }
+    return v;
+}
+
+// Per block: acc[l] summed over the block's threads, written to
+// partial[(k * gridDim.x + block) * kMaxRings + l].
+__device__ void block_sums(double (&acc)[kMaxRings], double* __restrict__ partial, int k) {
+    __shared__ double red[8][kMaxRings];
+#pragma unroll
+    for (int l = 0; l < kMaxRings; ++l) {
+        double v = warp_sum(acc[l]);
+        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5][l] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < kMaxRings) {
+        double s = 0.0;
+        for (int w = 0; w < int(blockDim.x >> 5); ++w) s += red[w][threadIdx.x];
+        partial[(size_t(k) * gridDim.x + blockIdx.x) * kMaxRings + threadIdx.x] = s;
+    }
+}
+
+// grid (kRingBlocks, K), block 256.
+__global__ void k_ring_build(int n, const __grid_constant__ RingSet rs,
+                             const float* __restrict__ ring_w, float* __restrict__ h,
+                             double* __restrict__ partial) {
+    const int k = blockIdx.y;
+    const size_t px = size_t(n) * n;
+    double acc[kMaxRings];
+#pragma unroll
+    for (int l = 0; l < kMaxRings; ++l) acc[l] = 0.0;
+    float wl[kMaxRings];
+#pragma unroll
+    for (int l = 0; l < kMaxRings; ++l) wl[l] = ring_w ? ring_w[k * kMaxRings + l] : 1.f;
+    float* hk = h + size_t(k) * px;
+    for (size_t p = blockIdx.x * size_t(blockDim.x) + threadIdx.x; p < px;
+         p += size_t(gridDim.x) * blockDim.x) {
+        const RingValue v = ring_value(rs, k, n, p);
+        float out = 0.f;
+#pragma unroll
+        for (int l = 0; l < kMaxRings; ++l)
+            if (v.ring == l) {
+                acc[l] += double(v.core);
+                out = wl[l] * v.core;
+            }
+        hk[p] = out;
+    }
+    block_sums(acc, partial, k);
+}
+
+// grid K, block 32: ring_s[k][l] = sum over blocks (fixed order), zsum[k] =
+// sum_l w_l ring_s[k][l].
+__global__ void k_ring_final(const __grid_constant__ RingSet rs, const float* __restrict__ ring_w,
+                             const double* __restrict__ partial, int nblocks,
+                             double* __restrict__ ring_s, double* __restrict__ zsum) {
+    const int k = blockIdx.x, l = threadIdx.x;
+    __shared__ double s[kMaxRings];
+    if (l < kMaxRings) {
+        double a = 0.0;
+        for (int b = 0; b < nblocks; ++b) a += partial[(size_t(k) * nblocks + b) * kMaxRings + l];
+        s[l] = a;
+        ring_s[k * kMaxRings + l] = a;
+    }
+    __syncthreads();
+    if (l == 0) {
+        double z = 0.0;
+        for (int i = 0; i < rs.rings[k] && i < kMaxRings; ++i)
+            z += double(ring_w ? ring_w[k * kMaxRings + i] : 1.f) * s[i];
+        zsum[k] = z;
+    }
+}
+
+// grid (kRingBlocks, K), block 256: G_l = sum over ring l of hbar * core.
+__global__ void k_ring_grad(int n, const __grid_constant__ RingSet rs,
+                            const float* __restrict__ hbar, double* __restrict__ partial) {
+    const int k = blockIdx.y;
+    const size_t px = size_t(n) * n;
+    double acc[kMaxRings];
+#pragma unroll
+    for (int l = 0; l < kMaxRings; ++l) acc[l] = 0.0;
+    const float* hb = hbar + size_t(k) * px;
+    for (size_t p = blockIdx.x * size_t(blockDim.x) + threadIdx.x; p < px;
+         p += size_t(gridDim.x) * blockDim.x) {
+        const RingValue v = ring_value(rs, k, n, p);
+        const double g = double(__ldg(&hb[p])) * double(v.core);
+#pragma unroll
+        for (int l = 0; l < kMaxRings; ++l)
+            if (v.ring == l) acc[l] += g;
+    }
+    block_sums(acc, partial, k);
+}
+
+// grid K, block 32: h = sum_l b_l S_l / Z, Z = sum_l b_l s_l, so
+// dL/db_l = (G_l - s_l sum_m b_m G_m / Z) / Z.
+__global__ void k_ring_grad_final(const __grid_constant__ RingSet rs,
+                                  const float* __restrict__ ring_w,
+                                  const double* __restrict__ partial, int nblocks,
+                                  const double* __restrict__ ring_s,
+                                  const double* __restrict__ zsum, float* __restrict__ grad) {
+    const int k = blockIdx.x, l = threadIdx.x;
+    __shared__ double G[kMaxRings];
+    if (l < kMaxRings) {
+        double a = 0.0;
+        for (int b = 0; b < nblocks; ++b) a += partial[(size_t(k) * nblocks + b) * kMaxRings + l];
+        G[l] = a;
+    }
+    __syncthreads();
+    if (l < kMaxRings) {
+        const int B = rs.rings[k];
+        double bg = 0.0;
+        for (int m = 0; m < B && m < kMaxRings; ++m)
+            bg += double(ring_w ? ring_w[k * kMaxRings + m] : 1.f) * G[m];
+        const double z = zsum[k];
+        const double g = (l < B && z != 0.0) ? (G[l] - ring_s[k * kMaxRings + l] * bg / z) / z : 0.0;
+        grad[k * kMaxRings + l] = float(g);
+    }
+}
+
+cudaError_t launch_ring_build(int n, int K, const RingSet& rs, const float* ring_w, float* h,
+                              double* partial, double* ring_s, double* zsum, cudaStream_t s) {
+    k_ring_build<<<dim3(kRingBlocks, K), 256, 0, s>>>(n, rs, ring_w, h, partial);
+    k_ring_final<<<K, 32, 0, s>>>(rs, ring_w, partial, kRingBlocks, ring_s, zsum);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_ring_grad(int n, int K, const RingSet& rs, const float* ring_w,
+                             const float* hbar, double* partial, const double* ring_s,
+                             const double* zsum, float* grad, cudaStream_t s) {
+    k_ring_grad<<<dim3(kRingBlocks, K), 256, 0, s>>>(n, rs, hbar, partial);
+    k_ring_grad_final<<<K, 32, 0, s>>>(rs, ring_w, partial, kRingBlocks, ring_s, zsum, grad);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
 // Mass reduction without device allocation (cg_mass_f64_noalloc).
 //
 // The per-block partial sums live in this fixed array instead of a buffer

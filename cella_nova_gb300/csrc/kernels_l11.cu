@@ -1,3 +1,3 @@
 // Step kernels for grid side 2048.
-#include "adjoint.cuh"
+#include "builder.cuh"
 CG_DEFINE_SIZE_OPS(11)

@@ -1,5 +1,5 @@
 // Step kernels for grid sides 16 to 256 (test and small-creature sizes).
-#include "adjoint.cuh"
+#include "builder.cuh"
 CG_DEFINE_SIZE_OPS(4)
 CG_DEFINE_SIZE_OPS(5)
 CG_DEFINE_SIZE_OPS(6)

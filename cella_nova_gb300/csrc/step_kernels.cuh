@@ -708,12 +708,13 @@ cudaError_t launch_pack(const float2* full, float2* out, cudaStream_t st) {
 
 }  // namespace cg
 
-// Per-size operation table (needs adjoint.cuh included before expansion).
+// Per-size operation table (needs builder.cuh included before expansion).
 #define CG_DEFINE_SIZE_OPS(LOGN)                                                          \
     namespace cg {                                                                        \
     extern const SizeOps size_ops_l##LOGN;                                                \
     const SizeOps size_ops_l##LOGN = {launch_step<LOGN>,      launch_pack<LOGN>,          \
                                       prepare_size<LOGN>,     twiddle_count<LOGN>,        \
                                       launch_backward<LOGN>,  launch_kgrad_final<LOGN>,   \
-                                      prepare_backward<LOGN>, launch_step_channel<LOGN>}; \
+                                      prepare_backward<LOGN>, launch_step_channel<LOGN>,  \
+                                      prepare_builder<LOGN>,  launch_kspec_cols<LOGN>};   \
     }

@@ -129,6 +129,23 @@ class GpuMaceLenia:
                                              ctypes.c_void_p(sigma_ptr),
                                              ctypes.c_void_p(weights_ptr)))
 
+    def build_ring_kernels(self, specs, ring_weights_ptr: int | None = None):
+        """On-GPU kernel builder: specs is a list of K (family, rings, radius,
+        width) tuples (family 0: Lenia shells, 1: the reference generator's
+        Gaussian ring); ring_weights_ptr a device address of K * 8 float32
+        ring weights, or None for all ones."""
+        arr = ring_spec_array(specs)
+        check(self._lib.cg_build_ring_kernels(self._h, ctypes.cast(arr, ctypes.c_void_p),
+                                              ctypes.c_void_p(ring_weights_ptr or 0)))
+        self._ring_specs = arr
+
+    def ring_weight_grad(self, hbar_ptr: int, grad_ptr: int, ring_weights_ptr: int | None = None):
+        """dL/d ring weights (K * 8 float32 at grad_ptr) of the last build,
+        from dL/dh (K * n * n float32 at hbar_ptr)."""
+        check(self._lib.cg_ring_weight_grad(self._h, ctypes.cast(self._ring_specs, ctypes.c_void_p),
+                                            ctypes.c_void_p(ring_weights_ptr or 0),
+                                            ctypes.c_void_p(hbar_ptr), ctypes.c_void_p(grad_ptr)))
+
     def iterate_and_render(self):
         """iterate_and_render (mod.rs:390): one step whose diffusion also
         writes the packed 0x00RRGGBB render buffer."""
@@ -248,6 +265,24 @@ class GpuMaceLenia:
 # ---------------------------------------------------------------------------
 # File formats (ml-rs/config.rs) through the C ABI
 # ---------------------------------------------------------------------------
+
+def ring_spec_array(specs):
+    """A ctypes array of cg_ring_spec from (family, rings, radius, width)."""
+    arr = (_abi.cg_ring_spec * len(specs))()
+    for i, (fam, rings, radius, width) in enumerate(specs):
+        arr[i] = _abi.cg_ring_spec(int(fam), int(rings), float(radius), float(width))
+    return arr
+
+
+def creature_ring_specs(cr):
+    """Shell-family specs and padded ring weights (K, 8) of a creature made
+    by :func:`cella_nova_gb300.creature.make_creature`."""
+    specs = [(_abi.RING_SHELL, len(b), R, 0.0) for R, b in zip(cr.ring_radius, cr.ring_weights)]
+    w = np.zeros((cr.K, _abi.MAX_RINGS), dtype=np.float32)
+    for k, b in enumerate(cr.ring_weights):
+        w[k, :len(b)] = b
+    return specs, w
+
 
 SEED_MAGIC = b"CNSEED01"
 

@@ -218,6 +218,40 @@ int cg_set_params(cg_sim* sim, const float* mu, const float* sigma, const float*
 int cg_set_params_device(cg_sim* sim, const float* dev_mu, const float* dev_sigma,
                          const float* dev_weights);
 
+/* ---------------------------------------------------------------------------
+ * On-GPU kernel builder (replaces generate_kernel_json.py:106-146 and
+ * example.rs:338-407 on the host): K ring kernels built in device memory,
+ * normalised to sum 1, transformed with the step's own row and column FFTs
+ * and packed into the handle's kernel spectra (what cg_set_kernel would
+ * store for their fft2).  Enqueued on the handle's stream; capturable.
+ * ------------------------------------------------------------------------- */
+#define CG_MAX_RINGS 8
+enum {
+    CG_RING_SHELL = 0, /* Lenia shells: r = |x| / radius, ring l = floor(r * rings),
+                          t = frac(r * rings), b_l * exp(4 - 1/(t(1-t))) for r < 1 */
+    CG_RING_GAUSS = 1  /* the reference generator's ring: d = |x| / radius,
+                          sigmoid(-(d-1)*10) * exp(-(d-1/2)^2 / (2 width^2)),
+                          radius = global_r * radius of generate_kernel_json.py */
+};
+typedef struct {
+    int family;     /* CG_RING_SHELL or CG_RING_GAUSS */
+    int rings;      /* CG_RING_SHELL: 1..CG_MAX_RINGS; ignored for CG_RING_GAUSS */
+    float radius;   /* px, > 0 */
+    float width;    /* CG_RING_GAUSS: > 0; ignored for CG_RING_SHELL */
+} cg_ring_spec;
+
+/* specs: K host descriptors.  dev_ring_weights: K * CG_MAX_RINGS device
+ * floats (kernel k's ring weights b_l at k * CG_MAX_RINGS + l), or NULL for
+ * all ones.  Uses the handle's spectrum scratch: enqueue it between steps. */
+int cg_build_ring_kernels(cg_sim* sim, const cg_ring_spec* specs, const float* dev_ring_weights);
+
+/* Gradient of a loss with respect to the ring weights of the LAST
+ * cg_build_ring_kernels (same specs and weights), given dev_hbar = dL/dh
+ * (K*n*n device floats, e.g. from cg_kernel_grad_spatial): writes
+ * dev_grad[K * CG_MAX_RINGS] (0 past each kernel's ring count). */
+int cg_ring_weight_grad(cg_sim* sim, const cg_ring_spec* specs, const float* dev_ring_weights,
+                        const float* dev_hbar, float* dev_grad);
+
 /* One step from x_in to x_out (C*n*n f32 each, distinct). */
 int cg_step_from(cg_sim* sim, const float* x_in, float* x_out);
 

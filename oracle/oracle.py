@@ -16,6 +16,8 @@ Contents
 * ``load_config_np`` / ``load_kernels_np``: restatement of
   ml-rs/config.rs:32-125 (JSON seed format with the c0/c1 swap, .bin kernel
   spectra with the spectral zero-padding resample).
+* ``gauss_ring_kernels_np``: restatement of the reference's kernel generator
+  (train/generate_kernel_json.py:106-146, ml-rs/example.rs:338-407).
 * ``render_np`` / ``rgb24_np``: restatement of render_main
   (ml-rs/shaders/compute_1024.wgsl:428-443) and of download_render's byte
   conversion (ml-rs/orchestrator/mod.rs:322-329).
@@ -223,4 +225,27 @@ def rgb24_np(packed):
     bytes R, G, B."""
     p = np.asarray(packed, dtype=np.uint32)
     return np.stack([(p >> 16) & 255, (p >> 8) & 255, p & 255], axis=-1).astype(np.uint8)
+
+
+def gauss_ring_kernels_np(size, global_r, radii, widths):
+    """(K, size, size) complex128 spectra of the reference's Gaussian ring
+    kernels (train/generate_kernel_json.py:106-146): per kernel, distance
+    from the grid centre size//2 scaled by global_r * radius, a sigmoid gate
+    sigmoid(-(d-1)*10) (sigmoid(x) = (tanh(x/2)+1)/2, :102-103) times
+    exp(-(d-1/2)^2 / (2 width^2)), normalised to sum 1, ifftshift-ed to put
+    the centre at [0, 0], then fft2.  Float64 throughout (the generator
+    builds float32 values; the spectra differ from it at the 1e-7 level)."""
+    mid = size // 2
+    i = np.arange(size, dtype=np.float64) - mid
+    dist = np.sqrt(i[:, None] ** 2 + i[None, :] ** 2)
+    out = []
+    for radius, width in zip(radii, widths):
+        d = dist / (global_r * radius)
+        sig = 0.5 * (np.tanh(-(d - 1.0) * 10.0 / 2.0) + 1.0)
+        val = sig * np.exp(-((d - 0.5) ** 2) / (2.0 * width * width))
+        total = val.sum()
+        if total > 0:
+            val = val / total
+        out.append(np.fft.fft2(np.fft.ifftshift(val)))
+    return np.stack(out)
 

@@ -14,7 +14,10 @@ transformed and summed over (lenia_org.py:131-134, diff_lenia_org.py:50).
 Two runs per trajectory fixture: float64 (the pin for the FP64 oracle) and
 float32 (the reference's own precision).  The grad_*.npz fixtures hold
 gradients of MSE(x_T, seed shifted by (+16, +8) px) from the model's own
-autograd in float64.  ``pyperlin`` (used only for random initial
+autograd in float64.  gauss_rings_*.npz hold kernel spectra from the
+reference's kernel generator (train/generate_kernel_json.py:106-146), the
+pin of the on-GPU kernel builder's Gaussian-ring family.
+``pyperlin`` (used only for random initial
 states, lenia_org.py:63-66) is replaced by an empty stub module because the
 state is always given.
 """
@@ -133,7 +136,28 @@ CASES = [
 ]
 
 
-def main(ref_root):
+# The ring radii and widths of ml-rs/example.rs:342-350 (global_r 10).
+GAUSS_RADII = [0.25, 0.3167, 0.3833, 0.45, 0.5167, 0.5833, 0.65, 0.7167, 0.85]
+GAUSS_WIDTHS = [0.03, 0.0411, 0.0522, 0.0633, 0.0744, 0.0856, 0.0967, 0.1078, 0.13]
+GAUSS_CASES = [("gauss_rings_n64", 64, 10.0), ("gauss_rings_n128", 128, 25.0)]
+
+
+def make_gauss_rings(ref_root):
+    sys.path.insert(0, os.path.join(ref_root, "train"))
+    from generate_kernel_json import generate_kernels_fft
+    for name, n, global_r in GAUSS_CASES:
+        ks = generate_kernels_fft(n, len(GAUSS_RADII), global_r, GAUSS_RADII, GAUSS_WIDTHS)
+        path = os.path.join(HERE, f"{name}.npz")
+        np.savez_compressed(path, n=n, global_r=global_r, radii=np.array(GAUSS_RADII),
+                            widths=np.array(GAUSS_WIDTHS), kspec=np.stack(ks))
+        print(f"wrote {path}")
+
+
+def main(ref_root, only=None):
+    if only in (None, "gauss"):
+        make_gauss_rings(ref_root)
+    if only == "gauss":
+        return
     import torch
     DL = load_reference(ref_root)
     for name, n, C, steps, temp, radius, seed in CASES:
@@ -165,4 +189,6 @@ def main(ref_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    args = [a for a in sys.argv[1:] if not a.startswith("--only=")]
+    only = next((a.split("=", 1)[1] for a in sys.argv[1:] if a.startswith("--only=")), None)
+    main(args[0] if args else "/root/reference", only)

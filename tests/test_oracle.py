@@ -15,7 +15,7 @@ import pytest
 from oracle import oracle as O
 
 GOLDEN = sorted(p for p in glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz"))
-                if not os.path.basename(p).startswith("grad_"))
+                if not os.path.basename(p).startswith(("grad_", "gauss_")))
 
 
 def _args(g):
@@ -104,3 +104,14 @@ def test_loaders_swap_and_resample(tmp_path):
         assert abs(k64[k][0, 0] - cr.kspec[k][0, 0]) < 1e-6
         np.testing.assert_allclose(np.fft.fftshift(k64[k])[16:48, 16:48],
                                    np.fft.fftshift(cr.kspec[k]), atol=0)
+
+
+@pytest.mark.parametrize("name", ["gauss_rings_n64", "gauss_rings_n128"])
+def test_gauss_ring_generator_restatement(name):
+    """The kernel generator's Gaussian rings (generate_kernel_json.py:106-146)
+    against the spectra the reference's own generator wrote."""
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", f"{name}.npz"))
+    ks = O.gauss_ring_kernels_np(int(g["n"]), float(g["global_r"]), g["radii"], g["widths"])
+    # the reference builds float32 values and stores complex64
+    assert np.abs(ks - g["kspec"]).max() < 5e-7
+
