@@ -46,6 +46,7 @@ class cg_ring_spec(ctypes.Structure):
 
 
 RING_SHELL, RING_GAUSS, MAX_RINGS = 0, 1, 8
+REDUCE_BLOCKS = 296   # CG_REDUCE_BLOCKS
 
 _P = ctypes.c_void_p
 _I = ctypes.c_int
@@ -66,6 +67,9 @@ SIGNATURES = {
     "cg_set_params": ([_P, _FP, _FP, _FP, _F], _I),
     "cg_set_params_device": ([_P, _P, _P, _P], _I),
     "cg_build_ring_kernels": ([_P, _P, _P], _I),
+    "cg_mse_grad": ([_P, _P, ctypes.c_size_t, _P, _P, _P, _P], _I),
+    "cg_adam_step": ([_P, _P, _P, _P, _P, ctypes.c_size_t, _F, _F, _F, _F, _P, _P], _I),
+    "cg_count_step": ([_P, _P], _I),
     "cg_ring_weight_grad": ([_P, _P, _P, _P, _P], _I),
     "cg_iterate_and_render": ([_P], _I),
     "cg_render": ([_P], _I),
@@ -75,6 +79,7 @@ SIGNATURES = {
     "cg_step_from": ([_P, _P, _P], _I),
     "cg_step_backward": ([_P, _P, _P, _P, _P, _P], _I),
     "cg_kernel_grad_spatial": ([_P, _P, _P], _I),
+    "cg_zero_grads": ([_P, _P, _P], _I),
     "cg_unroll": ([_P, _P, _I, _I, _P, _P], _I),
     "cg_unroll_backward": ([_P, _P, _I, _I, _P, _P, _P, _P, _P, _P], _I),
     "cg_upload_channel_f32": ([_P, _I, _FP], _I),

@@ -883,6 +883,16 @@ int cg_step_backward(cg_sim* s, const float* x, const float* ybar, float* xbar, 
     return CG_OK;
 }
 
+int cg_zero_grads(cg_sim* s, double* pgrad, float* kgrad) {
+    if (!s || !pgrad) return fail(CG_ERR_ARG, "cg_zero_grads: NULL argument");
+    CG_CHECK(cudaMemsetAsync(pgrad, 0, sizeof(double) * 3 * s->K, s->stream), "zeroing pgrad");
+    if (kgrad)
+        CG_CHECK(cudaMemsetAsync(kgrad, 0, sizeof(float2) * s->K * (size_t(s->n / 2) * s->n),
+                                 s->stream),
+                 "zeroing kgrad");
+    return CG_OK;
+}
+
 int cg_kernel_grad_spatial(cg_sim* s, float* kgrad, float* hbar) {
     if (!s || !kgrad || !hbar) return fail(CG_ERR_ARG, "cg_kernel_grad_spatial: NULL argument");
     int rc = ensure_backward(s);

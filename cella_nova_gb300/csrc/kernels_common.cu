@@ -102,6 +102,9 @@ __global__ void k_rgb24(const unsigned* __restrict__ in, unsigned char* __restri
     }
 }
 
+int cuda_fail(cudaError_t e, const char* what);
+static_assert(kMassBlocks == CG_REDUCE_BLOCKS, "reduction scratch size");
+
 static int grid_for(size_t count) {
     return int((count + 255) / 256 < 4096 ? (count + 255) / 256 : 4096);
 }
@@ -319,6 +322,112 @@ cudaError_t launch_ring_grad(int n, int K, const RingSet& rs, const float* ring_
     k_ring_grad_final<<<K, 32, 0, s>>>(rs, ring_w, partial, kRingBlocks, ring_s, zsum, grad);
     return cudaGetLastError();
 }
+
+// ---------------------------------------------------------------------------
+// Gradient-search helpers: the MSE loss with its gradient, and an Adam step
+// (the update rule of torch.optim.Adam, which train/ uses) whose step count
+// lives on the device, so a captured graph can replay it.
+// ---------------------------------------------------------------------------
+__global__ void k_mse_partial(const float* __restrict__ x, const float* __restrict__ t,
+                              size_t count, float* __restrict__ g, double* __restrict__ partial) {
+    double s = 0.0;
+    const float scale = float(2.0 / double(count));
+    const size_t stride = size_t(gridDim.x) * blockDim.x;
+    for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < count; i += stride) {
+        const float d = __ldg(&x[i]) - __ldg(&t[i]);
+        g[i] = scale * d;
+        s += double(d) * double(d);
+    }
+    __shared__ double red[8];
+    s = warp_sum(s);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        double v = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+        v = warp_sum(v);
+        if (threadIdx.x == 0) partial[blockIdx.x] = v;
+    }
+}
+
+__global__ void k_mse_final(const double* __restrict__ partial, int nblocks, size_t count,
+                            double* __restrict__ loss) {
+    double s = 0.0;
+    for (int i = threadIdx.x; i < nblocks; i += blockDim.x) s += partial[i];
+    __shared__ double red[8];
+    s = warp_sum(s);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        double v = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+        v = warp_sum(v);
+        if (threadIdx.x == 0) *loss = v / double(count);
+    }
+}
+
+template <class G>
+__global__ void k_adam(float* __restrict__ p, const G* __restrict__ g, float* __restrict__ m,
+                       float* __restrict__ v, size_t count, float lr, float b1, float b2,
+                       float eps, const int* __restrict__ step) {
+    const float t = float(*step + 1);   // the step being taken, 1-based
+    const float bc1 = 1.f - powf(b1, t);
+    const float bc2s = sqrtf(1.f - powf(b2, t));
+    const float step_size = lr / bc1;
+    const size_t stride = size_t(gridDim.x) * blockDim.x;
+    for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < count; i += stride) {
+        const float gi = float(g[i]);
+        const float mi = fmaf(1.f - b1, gi - m[i], m[i]);          // lerp toward g
+        const float vi = fmaf(1.f - b2, gi * gi, b2 * v[i]);
+        m[i] = mi;
+        v[i] = vi;
+        p[i] -= step_size * (mi / (sqrtf(vi) / bc2s + eps));
+    }
+}
+
+__global__ void k_count_step(int* step) { *step += 1; }
+
+}  // namespace cg
+
+extern "C" int cg_mse_grad(const float* x, const float* target, size_t count, float* grad,
+                           double* loss, double* scratch, cg_stream_t stream) {
+    using namespace cg;
+    if (!x || !target || !grad || !loss || !scratch)
+        return fail(CG_ERR_ARG, "cg_mse_grad: NULL pointer");
+    if (count == 0) return fail(CG_ERR_ARG, "cg_mse_grad: empty input");
+    auto st = static_cast<cudaStream_t>(stream);
+    k_mse_partial<<<kMassBlocks, 256, 0, st>>>(x, target, count, grad, scratch);
+    k_mse_final<<<1, 256, 0, st>>>(scratch, kMassBlocks, count, loss);
+    const cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? CG_OK : cuda_fail(e, "launching the MSE loss");
+}
+
+extern "C" int cg_adam_step(float* param, const float* grad_f32, const double* grad_f64,
+                            float* m, float* v, size_t count, float lr, float beta1, float beta2,
+                            float eps, const int* step, cg_stream_t stream) {
+    using namespace cg;
+    if (!param || !m || !v || !step || (!grad_f32) == (!grad_f64))
+        return fail(CG_ERR_ARG, "cg_adam_step: NULL pointer, or not exactly one gradient");
+    if (count == 0) return CG_OK;
+    auto st = static_cast<cudaStream_t>(stream);
+    const int blocks = grid_for(count);
+    if (grad_f32)
+        k_adam<float><<<blocks, 256, 0, st>>>(param, grad_f32, m, v, count, lr, beta1, beta2, eps,
+                                             step);
+    else
+        k_adam<double><<<blocks, 256, 0, st>>>(param, grad_f64, m, v, count, lr, beta1, beta2,
+                                              eps, step);
+    const cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? CG_OK : cuda_fail(e, "launching the Adam step");
+}
+
+extern "C" int cg_count_step(int* step, cg_stream_t stream) {
+    using namespace cg;
+    if (!step) return fail(CG_ERR_ARG, "cg_count_step: NULL pointer");
+    k_count_step<<<1, 1, 0, static_cast<cudaStream_t>(stream)>>>(step);
+    const cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? CG_OK : cuda_fail(e, "launching the step counter");
+}
+
+namespace cg {
 
 // ---------------------------------------------------------------------------
 // Mass reduction without device allocation (cg_mass_f64_noalloc).

@@ -267,6 +267,10 @@ int cg_step_backward(cg_sim* sim, const float* x, const float* ybar, float* xbar
  * the accumulated kgrad (which this overwrites). */
 int cg_kernel_grad_spatial(cg_sim* sim, float* kgrad, float* hbar);
 
+/* Zero pgrad[3K] and, if not NULL, kgrad (K*(n/2)*n complex f32) on the
+ * handle's stream, before a backward pass accumulates into them. */
+int cg_zero_grads(cg_sim* sim, double* pgrad, float* kgrad);
+
 /* T steps from x0 to xT, storing x_{j*every} in ckpt[j], j = 0..(T-1)/every
  * (ckpt holds (T-1)/every + 1 states). */
 int cg_unroll(cg_sim* sim, const float* x0, int T, int every, float* ckpt, float* xT);
@@ -313,6 +317,31 @@ int cg_batch_stream(cg_batch* b, cg_stream_t* out);
 /* Work items and persistent grid size per phase (either pointer may be
  * NULL). */
 int cg_batch_info(cg_batch* b, int* items4, int* grid4);
+
+/* ---------------------------------------------------------------------------
+ * Gradient-search helpers (the optimisation loop of train/, on the device).
+ * Free functions on device arrays, enqueued on `stream` (NULL: the legacy
+ * default stream); capturable in a CUDA graph.
+ * ------------------------------------------------------------------------- */
+#define CG_REDUCE_BLOCKS 296
+
+/* loss = mean((x - target)^2) (FP64, fixed-order reduction; written to
+ * dev_loss[0]) and grad = 2 (x - target) / count.  dev_scratch holds
+ * CG_REDUCE_BLOCKS doubles. */
+int cg_mse_grad(const float* dev_x, const float* dev_target, size_t count, float* dev_grad,
+                double* dev_loss, double* dev_scratch, cg_stream_t stream);
+
+/* One Adam step (torch.optim.Adam without weight decay or amsgrad) on count
+ * parameters: m = lerp(m, g, 1-beta1), v = beta2 v + (1-beta2) g^2,
+ * p -= lr / (1-beta1^t) * m / (sqrt(v) / sqrt(1-beta2^t) + eps) with
+ * t = *dev_step + 1.  Exactly one of grad_f32 / grad_f64 is given (the
+ * parameter gradients of cg_unroll_backward are FP64). */
+int cg_adam_step(float* dev_param, const float* dev_grad_f32, const double* dev_grad_f64,
+                 float* dev_m, float* dev_v, size_t count, float lr, float beta1, float beta2,
+                 float eps, const int* dev_step, cg_stream_t stream);
+
+/* *dev_step += 1 (after the Adam steps of one iteration). */
+int cg_count_step(int* dev_step, cg_stream_t stream);
 
 /* ---------------------------------------------------------------------------
  * File formats (ml-rs/config.rs)
