@@ -18,6 +18,7 @@ prints one JSON line.
 from __future__ import annotations
 
 import argparse
+import ctypes
 import json
 import os
 import statistics
@@ -500,6 +501,171 @@ def run_grad(args):
     return 0
 
 
+def run_search(args):
+    """Batched gradient search: 32 candidates at 1024^2, C=3, K=9, T=128,
+    checkpoints every 16, MSE to the seed shifted by (+16, +8) px, Adam on
+    the seed, mu, sigma, weights and ring weights; every iteration of all
+    candidates is one CUDA graph (Adam included).  fwd+bwd cell-updates/s =
+    candidates * n^2 * T / iteration time, against the plain per-creature
+    loop (torch autograd over the same kernels + torch.optim.Adam, one
+    candidate at a time)."""
+    import torch
+    world, rank, local, dist = dist_setup(args.gpus)
+    torch.cuda.set_device(local)
+    from cella_nova_gb300 import _abi
+    from cella_nova_gb300.autograd import DiffusionLeniaGPU
+    from cella_nova_gb300.creature import make_creature
+    from cella_nova_gb300.search import AdamConfig, GradientSearch
+    n, C, T, every, ncand = 1024, 3, 128, 16, args.candidates
+    t0 = time.perf_counter()
+    dev = torch.device("cuda", local)
+    crs = [make_creature(n, C, seed=5000 + 100 * rank + i, temp=1.0, device=dev)
+           for i in range(ncand)]
+    tgs = [np.roll(cr.seed, (8, 16), axis=(1, 2)) for cr in crs]
+    gen_s = time.perf_counter() - t0
+    adam = AdamConfig(lr_seed=1e-3, lr_params=1e-3, lr_rings=1e-2)
+    sampler = ClockSampler(local)
+    sampler.start()
+    gs = GradientSearch(crs, tgs, T=T, every=every, adam=adam, n_streams=4)
+    warm = max(args.warmup, 3)
+    gs.run(warm)                      # the first iteration eager, then capture + replays
+    torch.cuda.synchronize()
+    barrier(dist, world)
+    iters = max(1, args.steps)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    t_wall0 = time.perf_counter()
+    e0.record()
+    gs.run(iters)
+    e1.record()
+    e1.synchronize()
+    t_wall1 = time.perf_counter()
+    barrier(dist, world)
+    ms = max_over_ranks(e0.elapsed_time(e1), dist, world) / iters
+    clocks = sampler.summary(t_wall0, t_wall1)
+    losses = gs.losses()
+    # mass of x_T against the seed it started from, FP64 on the GPU
+    lib = _abi.load()
+    # (x_T of the last iteration against the x_0 it was unrolled from, the
+    # first checkpoint)
+    drift = 0.0
+    m0 = torch.zeros(C, dtype=torch.float64, device=dev)
+    m1 = torch.zeros_like(m0)
+    torch.cuda.synchronize()
+    for c in gs.cands:
+        _abi.check(lib.cg_mass_f64_noalloc(ctypes.c_void_p(c.ckpt.data_ptr()), n, C,
+                                           ctypes.c_void_p(m0.data_ptr()), None))
+        _abi.check(lib.cg_mass_f64_noalloc(ctypes.c_void_p(c.xT.data_ptr()), n, C,
+                                           ctypes.c_void_p(m1.data_ptr()), None))
+        torch.cuda.synchronize()
+        drift = max(drift, float((m1 / m0 - 1).abs().max()))
+    gs.close()
+
+    # plain per-creature loop: torch autograd over the same adjoint kernels
+    # and torch.optim.Adam, one candidate at a time (no graphs)
+    plain_cands = min(ncand, 4)
+    plain_ms = 0.0
+    tgt = [torch.tensor(tg, dtype=torch.float32, device=dev) for tg in tgs[:plain_cands]]
+    models = [DiffusionLeniaGPU(cr) for cr in crs[:plain_cands]]
+    opts = [torch.optim.Adam([{"params": [m.seed], "lr": adam.lr_seed},
+                              {"params": [m.mu, m.sigma, m.weights], "lr": adam.lr_params},
+                              {"params": list(m.ring_weights), "lr": adam.lr_rings}])
+            for m in models]
+
+    def plain_iteration(i):
+        m, opt = models[i], opts[i]
+        opt.zero_grad(set_to_none=True)
+        loss = torch.mean((m(T, every) - tgt[i]) ** 2)
+        loss.backward()
+        opt.step()
+
+    for i in range(plain_cands):
+        plain_iteration(i)
+    torch.cuda.synchronize()
+    p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    p0.record()
+    for i in range(plain_cands):
+        plain_iteration(i)
+    p1.record()
+    p1.synchronize()
+    plain_ms = p0.elapsed_time(p1) / plain_cands * ncand    # per iteration of all candidates
+    del models, opts
+    sampler.stop()
+
+    cells = ncand * n * n * T
+    value = world * cells / (ms / 1e3)
+    line = {
+        "metric": "cell-updates/s (batched gradient search fwd+bwd: 32 x 1024^2, C=3, K=9, "
+                  "T=128, checkpoints every 16, in-graph Adam)",
+        "value": value, "unit": UNIT, "n_gpus": world, "steps": iters, "warmup": warm,
+        "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"{ncand} candidates 1024^2, 3 channels, 9 kernels (all pairs), "
+                               "ring kernels built on the GPU each iteration, T=128, checkpoint "
+                               "every 16, loss MSE vs seed shifted (+16,+8) px, Adam on seed, "
+                               "mu, sigma, weights, ring weights; one CUDA graph per iteration "
+                               "over 4 streams",
+                   "step_unit": "one iteration (forward, backward, Adam) of every candidate",
+                   "candidates": ncand},
+        "plain_loop": {"value": world * cells / (plain_ms / 1e3), "unit": UNIT,
+                       "ms_per_step": plain_ms,
+                       "how": f"torch autograd + torch.optim.Adam per candidate, "
+                              f"{plain_cands} candidates timed and scaled to {ncand}"},
+        "batched_over_plain": plain_ms / ms,
+        "loss_mean": float(np.mean(losses)),
+        "mass_drift_max": drift,
+        # per candidate and iteration: builder 4, parameter fold 1, forward 4
+        # per step, MSE 2, backward 8 per step, segment recompute 4 per step
+        # but each segment's first, kernel gradient 2, ring gradient 2, Adam 3;
+        # plus the step counter once per iteration
+        "gpu_launches": iters * (ncand * (14 + 16 * T - 4 * ((T + every - 1) // every)) + 1),
+        "clocks": clocks,
+        "setup_s": {"generate": gen_s},
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"], line["grad_check"] = search_cpu_check(args)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def search_cpu_check(args):
+    """CPU leg: the FP64 autograd oracle (torch, float64, all host threads)
+    on a bounded sample -- one 128^2 candidate, C=3, K=9, T=16, checkpoints
+    every 4 -- timed as fwd+bwd cell-updates/s, and used as the checker of
+    the GPU search's gradients on the same instance."""
+    import torch
+    from cella_nova_gb300.creature import make_creature
+    from cella_nova_gb300.search import GradientSearch
+    from oracle import autograd_ref as AR
+    n, C, T, every = 128, 3, 16, 4
+    cr = make_creature(n, C, seed=777, temp=1.0, radius=(6, 20), seed_box=64)
+    tg = AR.shifted_target(cr.seed)
+    t0 = time.perf_counter()
+    ref = AR.gradients(cr, T, tg, ring=True)
+    el = time.perf_counter() - t0
+    with GradientSearch([cr], [tg], T=T, every=every, n_streams=1) as gs:
+        gs.run_eager(1)
+        got = gs.gradients(0)
+
+    def rel(a, b):
+        a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
+        return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-30))
+
+    err = {k: rel(got[k], ref[k]) for k in ("seed", "mu", "sigma", "weights")}
+    err["ring_weights"] = rel(np.concatenate([got["ring_weights"][k, :len(b)]
+                                              for k, b in enumerate(ref["ring_weights"])]),
+                              np.concatenate(ref["ring_weights"]))
+    cpu = {"value": n * n * T / el, "unit": UNIT, "cores": torch.get_num_threads(),
+           "kind": "port",
+           "sample": f"FP64 torch autograd of the step (oracle/autograd_ref.py), one {n}^2 "
+                     f"C={C} K=9 candidate, T={T}, fwd+bwd, {el:.1f} s"}
+    check = {"instance": f"{n}^2, C={C}, K=9, T={T}", "max_rel_error": err,
+             "loss_rel_error": abs(got["loss"] / ref["loss"] - 1)}
+    return cpu, check
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -512,10 +678,11 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
-    ap.add_argument("--config", default="plain", choices=["plain", "batched", "grad"])
+    ap.add_argument("--config", default="plain", choices=["plain", "batched", "grad", "search"])
+    ap.add_argument("--candidates", type=int, default=32)
     args = ap.parse_args()
     if args.steps is None:
-        args.steps = {"plain": 4000, "batched": 500, "grad": 20}[args.config]
+        args.steps = {"plain": 4000, "batched": 500, "grad": 20, "search": 3}[args.config]
         if args.impl == "reference":
             args.steps = 1000
     if args.impl == "reference":
@@ -524,6 +691,8 @@ def main():
         return run_batched(args)
     if args.config == "grad":
         return run_grad(args)
+    if args.config == "search":
+        return run_search(args)
     return run_ours(args)
 
 

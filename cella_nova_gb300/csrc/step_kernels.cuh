@@ -568,14 +568,143 @@ __device__ __forceinline__ void diffusion_body(const float* __restrict__ A,
     });
 }
 
+// The same arithmetic, in the same order (hence the same bits), with the
+// vertical sums carried in registers down a column instead of staged in
+// shared memory.  NSEG segments of rows per tile; in the Z phase one thread
+// owns one of the TX+2 halo columns of a segment, in the output phase one of
+// the TX columns.  The A tile is read with 16-byte loads (a 4-pixel side
+// halo keeps them aligned; the toroidal wrap stays aligned because n is a
+// multiple of 4).
 template <int LOGN, int V = 0>
-__global__ void __launch_bounds__(256) k_diffusion(const float* __restrict__ A,
-                                                    const float* __restrict__ x,
-                                                    float* __restrict__ out, int cbase,
-                                                    unsigned char* __restrict__ render, int nch) {
+struct DiffGeo2 {
+    using G = Geo<LOGN, V>;
+    static constexpr int N = G::N, TX = G::TX, TY = G::TY;
+    static constexpr int NSEG = 4;
+    static constexpr int AS = TX + 8, AH = TY + 4, HW = TX + 2, QH = TY + 2;
+    static constexpr int ZR = (QH + NSEG - 1) / NSEG;   // Z rows per segment, at most
+    static constexpr int OR = TY / NSEG;                // output rows per segment
+    static constexpr int THREADS = ((HW * NSEG + 31) / 32) * 32;
+    static constexpr int V4 = AS / 4;                   // 16-byte loads per A row
+    static constexpr size_t SMEM = size_t(2 * AH * AS + QH * HW) * sizeof(float);
+    static_assert(TY % NSEG == 0 && TX % 4 == 0, "tile shape");
+};
+
+template <int LOGN, int V = 0>
+__device__ __forceinline__ void diffusion2_body(const float* __restrict__ A,
+                                                const float* __restrict__ x,
+                                                float* __restrict__ out, int c, int x0, int y0,
+                                                float* smf, unsigned char* render, int nch) {
+    using D = DiffGeo2<LOGN, V>;
+    constexpr int N = D::N, TX = D::TX, AS = D::AS, AH = D::AH, HW = D::HW, QH = D::QH;
+    float* sAh = smf;                  // [AH][AS]: row a <-> y0 + a - 2, column j <-> x0 - 4 + j
+    float* sAl = smf + AH * AS;
+    float* sQ = smf + 2 * AH * AS;     // [QH][HW]: row b <-> y0 + b - 1, column q <-> x0 - 1 + q
+    const float* Ac = A + size_t(c) * N * N;
+    const float* xc = x + size_t(c) * N * N;
+    const int t = threadIdx.x;
+
+    // this thread's Z column and rows, and the state there (loaded first)
+    const bool zthr = t < HW * D::NSEG;
+    const int zq = t % HW, zseg = t / HW;
+    const int zr0 = zseg * QH / D::NSEG, zr1 = (zseg + 1) * QH / D::NSEG;
+    float xv[D::ZR];
+    if (zthr) {
+        const int gx = (x0 + zq - 1) & (N - 1);
+#pragma unroll
+        for (int i = 0; i < D::ZR; ++i)
+            if (zr0 + i < zr1) xv[i] = __ldg(&xc[size_t((y0 + zr0 + i - 1) & (N - 1)) * N + gx]);
+    }
+    // the A tile, split into 12-bit heads and exact tails
+    constexpr int NV = AH * D::V4;
+    constexpr int PER = (NV + D::THREADS - 1) / D::THREADS;
+    float4 av[PER];
+#pragma unroll
+    for (int i = 0; i < PER; ++i) {
+        const int e = t + i * D::THREADS;
+        if (e < NV) {
+            const int r = e / D::V4, v = e % D::V4;
+            const int gy = (y0 + r - 2) & (N - 1), gx = (x0 - 4 + 4 * v) & (N - 1);
+            av[i] = __ldg(reinterpret_cast<const float4*>(&Ac[size_t(gy) * N + gx]));
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < PER; ++i) {
+        const int e = t + i * D::THREADS;
+        if (e < NV) {
+            const int r = e / D::V4, v = e % D::V4;
+            const float4 a = av[i];
+            const float4 h = make_float4(head12(a.x), head12(a.y), head12(a.z), head12(a.w));
+            *reinterpret_cast<float4*>(&sAh[r * AS + 4 * v]) = h;
+            *reinterpret_cast<float4*>(&sAl[r * AS + 4 * v]) =
+                make_float4(a.x - h.x, a.y - h.y, a.z - h.z, a.w - h.w);
+        }
+    }
+    __syncthreads();
+
+    // Z = zh + zl down this thread's column, then q = x / Z
+    if (zthr) {
+        const float* ph = sAh + zq + 2;   // A columns x0 - 2 + zq .. x0 + zq
+        const float* pl = sAl + zq + 2;
+        auto hsum = [&](int a, float& hh, float& hl) {
+            hh = ph[a * AS] + ph[a * AS + 1] + ph[a * AS + 2];
+            hl = pl[a * AS] + pl[a * AS + 1] + pl[a * AS + 2];
+        };
+        float h0, l0, h1, l1;
+        hsum(zr0, h0, l0);
+        hsum(zr0 + 1, h1, l1);
+#pragma unroll
+        for (int i = 0; i < D::ZR; ++i) {
+            const int r = zr0 + i;
+            if (r < zr1) {
+                float h2, l2;
+                hsum(r + 2, h2, l2);
+                const float zh = h0 + h1 + h2;
+                const float zt = l0 + l1 + l2;
+                const float z = zh + zt;
+                const float zl = zt - (z - zh);
+                const float rz = rcp_approx(z);
+                const float q0 = xv[i] * rz;
+                const float rem = fmaf(-q0, z, xv[i]);
+                sQ[r * HW + zq] = fmaf(rem - q0 * zl, rz, q0);
+                h0 = h1;
+                l0 = l1;
+                h1 = h2;
+                l1 = l2;
+            }
+        }
+    }
+    __syncthreads();
+
+    // new = A * (3x3 sum of q), down this thread's output column
+    if (t < TX * D::NSEG) {
+        const int fq = t % TX, r0 = (t / TX) * D::OR;
+        const float* pq = sQ + fq;
+        auto qsum = [&](int b) { return pq[b * HW] + pq[b * HW + 1] + pq[b * HW + 2]; };
+        float s0 = qsum(r0), s1 = qsum(r0 + 1);
+        float* oc = out + size_t(c) * N * N;
+        const bool draw = render != nullptr && c < 3;
+#pragma unroll
+        for (int i = 0; i < D::OR; ++i) {
+            const int r = r0 + i;
+            const float s2 = qsum(r + 2);
+            const float a = sAh[(r + 2) * AS + fq + 4] + sAl[(r + 2) * AS + fq + 4];
+            const size_t p = size_t(y0 + r) * N + x0 + fq;
+            const float v = a * ((s0 + s1) + s2);
+            oc[p] = v;
+            if (draw) render_store(render, nch, c, p, v);
+            s0 = s1;
+            s1 = s2;
+        }
+    }
+}
+
+template <int LOGN, int V = 0>
+__global__ void __launch_bounds__(DiffGeo2<LOGN, V>::THREADS)
+    k_diffusion(const float* __restrict__ A, const float* __restrict__ x, float* __restrict__ out,
+                int cbase, unsigned char* __restrict__ render, int nch) {
     extern __shared__ __align__(128) float sm_diff[];
-    diffusion_body<LOGN, V>(A, x, out, blockIdx.z + cbase, blockIdx.x * Geo<LOGN, V>::TX,
-                            blockIdx.y * Geo<LOGN, V>::TY, sm_diff, render, nch);
+    diffusion2_body<LOGN, V>(A, x, out, blockIdx.z + cbase, blockIdx.x * Geo<LOGN, V>::TX,
+                             blockIdx.y * Geo<LOGN, V>::TY, sm_diff, render, nch);
 }
 
 // ---------------------------------------------------------------------------
@@ -621,7 +750,7 @@ cudaError_t prepare_variant() {
         return e;
     if ((e = cudaFuncSetAttribute(k_diffusion<LOGN, V>,
                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  int(DiffGeo<LOGN, V>::SMEM))) != cudaSuccess)
+                                  int(DiffGeo2<LOGN, V>::SMEM))) != cudaSuccess)
         return e;
     return cudaFuncSetAttribute(k_col_conv<LOGN, V>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 int(G::COL_SMEM));
@@ -658,8 +787,9 @@ void launch_c2r(const StepArgs& a, int c_lo, int nc, cudaStream_t st) {
 template <int LOGN, int V>
 void launch_diff(const StepArgs& a, int c_lo, int nc, cudaStream_t st) {
     using G = Geo<LOGN, V>;
-    k_diffusion<LOGN, V><<<dim3(G::N / G::TX, G::N / G::TY, nc), 256, DiffGeo<LOGN, V>::SMEM,
-                           st>>>(a.A, a.x_in, a.x_out, c_lo, a.render, a.C);
+    using D = DiffGeo2<LOGN, V>;
+    k_diffusion<LOGN, V><<<dim3(G::N / G::TX, G::N / G::TY, nc), D::THREADS, D::SMEM, st>>>(
+        a.A, a.x_in, a.x_out, c_lo, a.render, a.C);
 }
 
 #define CG_VARIANT_SWITCH(v, FN, ...)            \

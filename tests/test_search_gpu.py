@@ -88,7 +88,7 @@ def test_mse_grad_and_loss():
     torch.cuda.synchronize()
     _abi.check(lib.cg_mse_grad(P(xd), P(td), x.size, P(g), P(loss), P(scratch), None))
     torch.cuda.synchronize()
-    d = x.astype(np.float64) - t
+    d = (x - t).astype(np.float64)          # the difference is taken in f32
     assert abs(loss.item() - (d * d).mean()) <= 1e-12 * (d * d).mean()
     np.testing.assert_allclose(g.cpu().numpy(), 2 * (x - t) / x.size, rtol=1e-6)
 
