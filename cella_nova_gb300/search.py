@@ -211,11 +211,14 @@ class GradientSearch:
                 "weights": p[2 * K:], "ring_weights": c.rings.cpu().numpy()}
 
     def gradients(self, i: int) -> dict:
-        """Gradients of candidate i's last iteration."""
+        """Gradients of candidate i's last iteration, with the state it
+        started from (the seed before that iteration's Adam step) and its
+        final state."""
         c = self.cands[i]
         K = c.cr.K
         torch.cuda.synchronize()
         g = c.pgrad.cpu().numpy()
         return {"loss": float(c.loss.item()), "seed": c.g0.cpu().numpy(), "mu": g[:K],
                 "sigma": g[K:2 * K], "weights": g[2 * K:],
-                "ring_weights": c.ring_grad.cpu().numpy(), "final": c.xT.cpu().numpy()}
+                "ring_weights": c.ring_grad.cpu().numpy(), "final": c.xT.cpu().numpy(),
+                "initial": c.ckpt[0].cpu().numpy()}

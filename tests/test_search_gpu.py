@@ -108,7 +108,7 @@ def test_graph_replays_equal_eager_iterations_and_conserve_mass():
                 np.testing.assert_allclose(pa[k], pb[k], rtol=1e-5, atol=1e-6, err_msg=k)
             ga = a.gradients(i)
             # the unroll conserves each channel's mass
-            m0 = pa["seed"].astype(np.float64).sum(axis=(1, 2))
+            m0 = ga["initial"].astype(np.float64).sum(axis=(1, 2))
             mT = ga["final"].astype(np.float64).sum(axis=(1, 2))
             assert np.abs(mT / m0 - 1).max() < 1e-6
 
