@@ -227,7 +227,10 @@ def run_ours(args):
     sim = GpuMaceLenia.from_creature(cr)
     px = N_GRID * N_GRID
     tuned = None
-    if not args.no_autotune:
+    if args.variants:
+        sim.set_variants([int(v) for v in args.variants.split(",")])
+        tuned = {"variants": sim.variants(), "ms": None, "how": "--variants"}
+    elif not args.no_autotune:
         chosen, tms = sim.autotune(reps=10)
         tuned = {"variants": chosen, "ms": np.round(tms, 4).tolist()}
     stream = torch.cuda.ExternalStream(sim.stream())
@@ -678,6 +681,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--variants", default=None,
+                    help="fixed CTA-shape variants r2c,col,c2r,diffusion (skips the autotuner)")
     ap.add_argument("--config", default="plain", choices=["plain", "batched", "grad", "search"])
     ap.add_argument("--candidates", type=int, default=32)
     args = ap.parse_args()
