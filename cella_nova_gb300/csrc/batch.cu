@@ -95,17 +95,22 @@ __global__ void __launch_bounds__(512) kb_row_c2r_growth(const WorldDesc* __rest
     }
 }
 
+// Every batched size (64 and up) uses 64-wide diffusion tiles, hence one
+// block size for the phase.
+constexpr int kDiffThreads = DiffGeo2<6>::THREADS;
+static_assert(DiffGeo2<11>::THREADS == kDiffThreads, "one diffusion block size for all sizes");
+
 template <int LOGN>
-__global__ void __launch_bounds__(256) kb_diffusion(const WorldDesc* __restrict__ worlds,
-                                                     const WorkItem* __restrict__ items,
-                                                     int count, int parity) {
+__global__ void __launch_bounds__(kDiffThreads) kb_diffusion(const WorldDesc* __restrict__ worlds,
+                                                              const WorkItem* __restrict__ items,
+                                                              int count, int parity) {
     extern __shared__ __align__(128) float smb_diff[];
     for (int i = blockIdx.x; i < count; i += gridDim.x) {
         __syncthreads();
         const WorkItem it = items[i];
         const WorldDesc& w = worlds[it.world];
-        diffusion_body<LOGN>(w.A, w.state[parity], w.state[parity ^ 1], it.c, it.a, it.b,
-                             smb_diff);
+        diffusion2_body<LOGN>(w.A, w.state[parity], w.state[parity ^ 1], it.c, it.a, it.b,
+                              smb_diff, nullptr, 0);
     }
 }
 
@@ -139,7 +144,7 @@ struct PhaseSmem {
 template <int LOGN>
 PhaseSmem phase_smem() {
     using G = Geo<LOGN>;
-    return {G::R2C_SMEM, G::COL_SMEM, G::C2R_SMEM, DiffGeo<LOGN>::SMEM};
+    return {G::R2C_SMEM, G::COL_SMEM, G::C2R_SMEM, DiffGeo2<LOGN>::SMEM};
 }
 static PhaseSmem phase_smem_for(int logn) {
     switch (logn) {
@@ -244,7 +249,7 @@ void batch_release(cg_batch* b) {
 
 // One phase: a persistent launch per size class (largest first).
 cudaError_t launch_phase(cg_batch* b, int phase, int parity, cudaStream_t st) {
-    static const unsigned threads[4] = {512, 256, 512, 256};
+    static const unsigned threads[4] = {512, 256, 512, unsigned(kDiffThreads)};
     for (size_t i = 0; i < b->classes.size(); ++i) {
         auto& sc = b->classes[i];
         if (sc.count[phase] == 0) continue;
@@ -422,7 +427,7 @@ int cg_batch_create(int n_worlds, const int* n, const int* C, const int* K, cons
         sc.fns = phase_fns_for(logn);
         const PhaseSmem ps = phase_smem_for(logn);
         const size_t smem[4] = {ps.r2c, ps.col, ps.c2r, ps.diff};
-        const int threads[4] = {512, 256, 512, 256};
+        const int threads[4] = {512, 256, 512, kDiffThreads};
         for (int p = 0; p < 4 && rc == CG_OK; ++p) {
             sc.count[p] = int(lists[p].size());
             sc.smem[p] = smem[p];

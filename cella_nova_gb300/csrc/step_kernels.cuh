@@ -430,149 +430,17 @@ __global__ void __launch_bounds__(Geo<LOGN, V>::RT, 512 / Geo<LOGN, V>::RT) k_ro
 // within a factor 2^8 of each other, and the tails are summed in f32
 // (relative weight 2^-12), so zh + zl is Z to ~1e-11.  q = x / Z comes from a
 // reciprocal refined with the exact remainder, i.e. ~correctly rounded.
-// grid (N/TX, N/TY, C), block 256 (64 x 4).
+// grid (N/TX, N/TY, C), DiffGeo2::THREADS threads.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ float head12(float a) {
     return __int_as_float(__float_as_int(a) & 0xFFFFF000);
 }
 
-// Visit every (r, q) of an H x W region of a tile with 256 threads: rows in
-// steps of 4 with q = lane index (no divergence for q < 64), then the few
-// columns past 64 as one flat loop.
-template <int H, int W, class F>
-__device__ __forceinline__ void for_tile(F fn) {
-    const int tx = threadIdx.x & 63, ty = threadIdx.x >> 6;
-    constexpr int W0 = W < 64 ? W : 64;
-#pragma unroll 4
-    for (int r = ty; r < H; r += 4)
-        if (tx < W0) fn(r, tx);
-    if constexpr (W > 64) {
-        constexpr int E = W - 64;
-        for (int i = threadIdx.x; i < H * E; i += 256) fn(i / E, 64 + i % E);
-    }
-}
-
-template <int LOGN, int V = 0>
-struct DiffGeo {
-    static constexpr int TX = Geo<LOGN, V>::TX, TY = Geo<LOGN, V>::TY;
-    static constexpr int AW = TX + 4, AH = TY + 4, HW = TX + 2, QH = TY + 2;
-    static constexpr size_t SMEM = size_t(2 * AH * AW + 2 * AH * HW + QH * HW) * sizeof(float);
-};
-
-template <int LOGN, int V = 0>
-__device__ __forceinline__ void diffusion_body(const float* __restrict__ A,
-                                               const float* __restrict__ x,
-                                               float* __restrict__ out, int c, int x0, int y0,
-                                               float* smf, unsigned char* render = nullptr,
-                                               int nch = 0) {
-    using G = Geo<LOGN, V>;
-    using D = DiffGeo<LOGN, V>;
-    constexpr int N = G::N, TX = G::TX, TY = G::TY;
-    constexpr int AW = D::AW, AH = D::AH, HW = D::HW, QH = D::QH;
-    auto sAh = reinterpret_cast<float (*)[AW]>(smf);
-    auto sAl = reinterpret_cast<float (*)[AW]>(smf + AH * AW);
-    auto sHh = reinterpret_cast<float (*)[HW]>(smf + 2 * AH * AW);
-    auto sHl = reinterpret_cast<float (*)[HW]>(smf + 2 * AH * AW + AH * HW);
-    auto sQ = reinterpret_cast<float (*)[HW]>(smf + 2 * AH * AW + 2 * AH * HW);
-    auto sQs = reinterpret_cast<float (*)[TX]>(smf + 2 * AH * AW);   // reuses sHh
-    const int tx = threadIdx.x & 63, ty = threadIdx.x >> 6;
-    const float* Ac = A + size_t(c) * N * N;
-    const float* xc = x + size_t(c) * N * N;
-
-    // All halo loads are issued before any is stored, so each thread keeps
-    // ~20 independent DRAM reads in flight instead of one at a time.  Lanes
-    // cover columns 0..63; the 2-4 columns past 64 go through flat tails.
-    constexpr int RA = (AH + 3) / 4, RQ = (QH + 3) / 4;
-    constexpr int A0 = AW < 64 ? AW : 64, Q0 = HW < 64 ? HW : 64;
-    float av[RA], xin[RQ];
-#pragma unroll
-    for (int i = 0; i < RA; ++i) {
-        const int r = ty + 4 * i;
-        if (r < AH && tx < A0)
-            av[i] = __ldg(&Ac[size_t((y0 + r - 2) & (N - 1)) * N + ((x0 + tx - 2) & (N - 1))]);
-    }
-#pragma unroll
-    for (int i = 0; i < RQ; ++i) {
-        const int r = ty + 4 * i;
-        if (r < QH && tx < Q0)
-            xin[i] = __ldg(&xc[size_t((y0 + r - 1) & (N - 1)) * N + ((x0 + tx - 1) & (N - 1))]);
-    }
-    if constexpr (AW > 64) {
-        constexpr int E = AW - 64;
-        for (int t = threadIdx.x; t < AH * E; t += 256) {
-            const int r = t / E, q = 64 + t % E;
-            const float a = __ldg(&Ac[size_t((y0 + r - 2) & (N - 1)) * N + ((x0 + q - 2) & (N - 1))]);
-            const float h = head12(a);
-            sAh[r][q] = h;
-            sAl[r][q] = a - h;
-        }
-    }
-    if constexpr (HW > 64) {
-        constexpr int E = HW - 64;
-        for (int t = threadIdx.x; t < QH * E; t += 256) {
-            const int r = t / E, q = 64 + t % E;
-            sQ[r][q] = __ldg(&xc[size_t((y0 + r - 1) & (N - 1)) * N + ((x0 + q - 1) & (N - 1))]);
-        }
-    }
-#pragma unroll
-    for (int i = 0; i < RA; ++i) {
-        const int r = ty + 4 * i;
-        if (r < AH && tx < A0) {
-            const float h = head12(av[i]);
-            sAh[r][tx] = h;
-            sAl[r][tx] = av[i] - h;
-        }
-    }
-    __syncthreads();
-    // horizontal 3-sums of the heads (exact) and of the tails
-    for_tile<AH, HW>([&](int r, int q) {
-        sHh[r][q] = sAh[r][q] + sAh[r][q + 1] + sAh[r][q + 2];
-        sHl[r][q] = sAl[r][q] + sAl[r][q + 1] + sAl[r][q + 2];
-    });
-    __syncthreads();
-    // Z = zh + zl on the 1-pixel halo, then q = x / Z
-    auto qval = [&](int r, int q, float xv) {
-        const float zh = sHh[r][q] + sHh[r + 1][q] + sHh[r + 2][q];
-        const float zt = sHl[r][q] + sHl[r + 1][q] + sHl[r + 2][q];
-        const float z = zh + zt;
-        const float zl = zt - (z - zh);
-        const float rz = rcp_approx(z);
-        const float q0 = xv * rz;
-        const float rem = fmaf(-q0, z, xv);
-        return fmaf(rem - q0 * zl, rz, q0);
-    };
-#pragma unroll
-    for (int i = 0; i < RQ; ++i) {
-        const int r = ty + 4 * i;
-        if (r < QH && tx < Q0) sQ[r][tx] = qval(r, tx, xin[i]);
-    }
-    if constexpr (HW > 64) {
-        constexpr int E = HW - 64;
-        for (int t = threadIdx.x; t < QH * E; t += 256) {
-            const int r = t / E, q = 64 + t % E;
-            sQ[r][q] = qval(r, q, sQ[r][q]);
-        }
-    }
-    __syncthreads();   // sHh is reused as sQs below
-    // horizontal 3-sums of q, then the vertical sum times A
-    for_tile<QH, TX>([&](int r, int q) { sQs[r][q] = sQ[r][q] + sQ[r][q + 1] + sQ[r][q + 2]; });
-    __syncthreads();
-    float* oc = out + size_t(c) * N * N;
-    const bool draw = render != nullptr && c < 3;
-    for_tile<TY, TX>([&](int r, int q) {
-        const float a = sAh[r + 2][q + 2] + sAl[r + 2][q + 2];
-        const size_t p = size_t(y0 + r) * N + x0 + q;
-        const float v = a * ((sQs[r][q] + sQs[r + 1][q]) + sQs[r + 2][q]);
-        oc[p] = v;
-        if (draw) render_store(render, nch, c, p, v);
-    });
-}
-
-// The same arithmetic, in the same order (hence the same bits), with the
-// vertical sums carried in registers down a column instead of staged in
-// shared memory.  NSEG segments of rows per tile; in the Z phase one thread
-// owns one of the TX+2 halo columns of a segment, in the output phase one of
-// the TX columns.  The A tile is read with 16-byte loads (a 4-pixel side
+// Horizontal 3-sums come from shared memory, vertical ones are carried in
+// registers down a column: NSEG segments of rows per tile; in the Z phase one
+// thread owns one of the TX+2 halo columns of a segment, in the output phase
+// one of the TX columns.  Every sum keeps a fixed order ((a + b) + c, heads
+// and tails apart), so all tile shapes give the same bits.  The A tile is read with 16-byte loads (a 4-pixel side
 // halo keeps them aligned; the toroidal wrap stays aligned because n is a
 // multiple of 4).
 template <int LOGN, int V = 0>
