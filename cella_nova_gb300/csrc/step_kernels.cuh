@@ -447,14 +447,16 @@ template <int LOGN, int V = 0>
 struct DiffGeo2 {
     using G = Geo<LOGN, V>;
     static constexpr int N = G::N, TX = G::TX, TY = G::TY;
-    static constexpr int NSEG = 4;
+    static constexpr int NSEG = 2;
     static constexpr int AS = TX + 8, AH = TY + 4, HW = TX + 2, QH = TY + 2;
-    static constexpr int ZR = (QH + NSEG - 1) / NSEG;   // Z rows per segment, at most
-    static constexpr int OR = TY / NSEG;                // output rows per segment
+    static constexpr int ZR = QH / NSEG;       // Z rows per segment
+    static constexpr int OR = TY / NSEG;       // output rows per segment
     static constexpr int THREADS = ((HW * NSEG + 31) / 32) * 32;
-    static constexpr int V4 = AS / 4;                   // 16-byte loads per A row
+    static constexpr int V4 = AS / 4;          // 16-byte loads per A row
+    static constexpr int LR = THREADS / V4;    // A rows per sweep of the block
+    static constexpr int SWEEPS = (AH + LR - 1) / LR;
     static constexpr size_t SMEM = size_t(2 * AH * AS + QH * HW) * sizeof(float);
-    static_assert(TY % NSEG == 0 && TX % 4 == 0, "tile shape");
+    static_assert(QH % NSEG == 0 && TY % NSEG == 0 && TX % 4 == 0, "tile shape");
 };
 
 template <int LOGN, int V = 0>
@@ -464,6 +466,7 @@ __device__ __forceinline__ void diffusion2_body(const float* __restrict__ A,
                                                 float* smf, unsigned char* render, int nch) {
     using D = DiffGeo2<LOGN, V>;
     constexpr int N = D::N, TX = D::TX, AS = D::AS, AH = D::AH, HW = D::HW, QH = D::QH;
+    constexpr int MASK = N * N - 1;            // row offsets wrap as (row * N) & MASK
     float* sAh = smf;                  // [AH][AS]: row a <-> y0 + a - 2, column j <-> x0 - 4 + j
     float* sAl = smf + AH * AS;
     float* sQ = smf + 2 * AH * AS;     // [QH][HW]: row b <-> y0 + b - 1, column q <-> x0 - 1 + q
@@ -473,72 +476,62 @@ __device__ __forceinline__ void diffusion2_body(const float* __restrict__ A,
 
     // this thread's Z column and rows, and the state there (loaded first)
     const bool zthr = t < HW * D::NSEG;
-    const int zq = t % HW, zseg = t / HW;
-    const int zr0 = zseg * QH / D::NSEG, zr1 = (zseg + 1) * QH / D::NSEG;
+    const int zq = t % HW, zr0 = (t / HW) * D::ZR;
     float xv[D::ZR];
     if (zthr) {
-        const int gx = (x0 + zq - 1) & (N - 1);
+        const float* xcol = xc + ((x0 + zq - 1) & (N - 1));
+        const int base = (y0 + zr0 - 1) * N;
 #pragma unroll
-        for (int i = 0; i < D::ZR; ++i)
-            if (zr0 + i < zr1) xv[i] = __ldg(&xc[size_t((y0 + zr0 + i - 1) & (N - 1)) * N + gx]);
+        for (int i = 0; i < D::ZR; ++i) xv[i] = __ldg(xcol + ((base + i * N) & MASK));
     }
     // the A tile, split into 12-bit heads and exact tails
-    constexpr int NV = AH * D::V4;
-    constexpr int PER = (NV + D::THREADS - 1) / D::THREADS;
-    float4 av[PER];
+    if (t < D::LR * D::V4) {
+        const int v = t % D::V4, r0 = t / D::V4;
+        const float* acol = Ac + ((x0 - 4 + 4 * v) & (N - 1));
+        const int base = (y0 + r0 - 2) * N;
+        float4 av[D::SWEEPS];
 #pragma unroll
-    for (int i = 0; i < PER; ++i) {
-        const int e = t + i * D::THREADS;
-        if (e < NV) {
-            const int r = e / D::V4, v = e % D::V4;
-            const int gy = (y0 + r - 2) & (N - 1), gx = (x0 - 4 + 4 * v) & (N - 1);
-            av[i] = __ldg(reinterpret_cast<const float4*>(&Ac[size_t(gy) * N + gx]));
-        }
-    }
+        for (int i = 0; i < D::SWEEPS; ++i)
+            if (r0 + i * D::LR < AH)
+                av[i] = __ldg(reinterpret_cast<const float4*>(acol + ((base + i * D::LR * N) & MASK)));
 #pragma unroll
-    for (int i = 0; i < PER; ++i) {
-        const int e = t + i * D::THREADS;
-        if (e < NV) {
-            const int r = e / D::V4, v = e % D::V4;
-            const float4 a = av[i];
-            const float4 h = make_float4(head12(a.x), head12(a.y), head12(a.z), head12(a.w));
-            *reinterpret_cast<float4*>(&sAh[r * AS + 4 * v]) = h;
-            *reinterpret_cast<float4*>(&sAl[r * AS + 4 * v]) =
-                make_float4(a.x - h.x, a.y - h.y, a.z - h.z, a.w - h.w);
+        for (int i = 0; i < D::SWEEPS; ++i) {
+            if (r0 + i * D::LR < AH) {
+                const float4 a = av[i];
+                const float4 h = make_float4(head12(a.x), head12(a.y), head12(a.z), head12(a.w));
+                const int o = (r0 + i * D::LR) * AS + 4 * v;
+                *reinterpret_cast<float4*>(sAh + o) = h;
+                *reinterpret_cast<float4*>(sAl + o) =
+                    make_float4(a.x - h.x, a.y - h.y, a.z - h.z, a.w - h.w);
+            }
         }
     }
     __syncthreads();
 
     // Z = zh + zl down this thread's column, then q = x / Z
     if (zthr) {
-        const float* ph = sAh + zq + 2;   // A columns x0 - 2 + zq .. x0 + zq
-        const float* pl = sAl + zq + 2;
-        auto hsum = [&](int a, float& hh, float& hl) {
-            hh = ph[a * AS] + ph[a * AS + 1] + ph[a * AS + 2];
-            hl = pl[a * AS] + pl[a * AS + 1] + pl[a * AS + 2];
-        };
-        float h0, l0, h1, l1;
-        hsum(zr0, h0, l0);
-        hsum(zr0 + 1, h1, l1);
+        const float* ph = sAh + zr0 * AS + zq + 2;   // A columns x0 - 2 + zq .. x0 + zq
+        const float* pl = sAl + zr0 * AS + zq + 2;
+        float* pq = sQ + zr0 * HW + zq;
+        float h0 = ph[0] + ph[1] + ph[2], l0 = pl[0] + pl[1] + pl[2];
+        float h1 = ph[AS] + ph[AS + 1] + ph[AS + 2], l1 = pl[AS] + pl[AS + 1] + pl[AS + 2];
 #pragma unroll
         for (int i = 0; i < D::ZR; ++i) {
-            const int r = zr0 + i;
-            if (r < zr1) {
-                float h2, l2;
-                hsum(r + 2, h2, l2);
-                const float zh = h0 + h1 + h2;
-                const float zt = l0 + l1 + l2;
-                const float z = zh + zt;
-                const float zl = zt - (z - zh);
-                const float rz = rcp_approx(z);
-                const float q0 = xv[i] * rz;
-                const float rem = fmaf(-q0, z, xv[i]);
-                sQ[r * HW + zq] = fmaf(rem - q0 * zl, rz, q0);
-                h0 = h1;
-                l0 = l1;
-                h1 = h2;
-                l1 = l2;
-            }
+            const int o = (i + 2) * AS;
+            const float h2 = ph[o] + ph[o + 1] + ph[o + 2];
+            const float l2 = pl[o] + pl[o + 1] + pl[o + 2];
+            const float zh = h0 + h1 + h2;
+            const float zt = l0 + l1 + l2;
+            const float z = zh + zt;
+            const float zl = zt - (z - zh);
+            const float rz = rcp_approx(z);
+            const float q0 = xv[i] * rz;
+            const float rem = fmaf(-q0, z, xv[i]);
+            pq[i * HW] = fmaf(rem - q0 * zl, rz, q0);
+            h0 = h1;
+            l0 = l1;
+            h1 = h2;
+            l1 = l2;
         }
     }
     __syncthreads();
@@ -546,20 +539,22 @@ __device__ __forceinline__ void diffusion2_body(const float* __restrict__ A,
     // new = A * (3x3 sum of q), down this thread's output column
     if (t < TX * D::NSEG) {
         const int fq = t % TX, r0 = (t / TX) * D::OR;
-        const float* pq = sQ + fq;
-        auto qsum = [&](int b) { return pq[b * HW] + pq[b * HW + 1] + pq[b * HW + 2]; };
-        float s0 = qsum(r0), s1 = qsum(r0 + 1);
-        float* oc = out + size_t(c) * N * N;
+        const float* pq = sQ + r0 * HW + fq;
+        const float* pa = sAh + (r0 + 2) * AS + fq + 4;
+        const float* pb = sAl + (r0 + 2) * AS + fq + 4;
+        const int p0 = (y0 + r0) * N + x0 + fq;
+        float* oc = out + size_t(c) * N * N + p0;
         const bool draw = render != nullptr && c < 3;
+        float s0 = pq[0] + pq[1] + pq[2];
+        float s1 = pq[HW] + pq[HW + 1] + pq[HW + 2];
 #pragma unroll
         for (int i = 0; i < D::OR; ++i) {
-            const int r = r0 + i;
-            const float s2 = qsum(r + 2);
-            const float a = sAh[(r + 2) * AS + fq + 4] + sAl[(r + 2) * AS + fq + 4];
-            const size_t p = size_t(y0 + r) * N + x0 + fq;
+            const int o = (i + 2) * HW;
+            const float s2 = pq[o] + pq[o + 1] + pq[o + 2];
+            const float a = pa[i * AS] + pb[i * AS];
             const float v = a * ((s0 + s1) + s2);
-            oc[p] = v;
-            if (draw) render_store(render, nch, c, p, v);
+            oc[i * N] = v;
+            if (draw) render_store(render, nch, c, size_t(p0 + i * N), v);
             s0 = s1;
             s1 = s2;
         }
