@@ -117,16 +117,24 @@ class ClockSampler:
                 "samples": len(rows)}
 
 
-def dist_setup(n_gpus):
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
+def rank_info():
+    """(world, rank, local rank) from the torchrun environment."""
+    return (int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")),
+            int(os.environ.get("LOCAL_RANK", "0")))
+
+
+def dist_setup(n_gpus, backend=None):
+    """One process per GPU (replicas): NCCL on GPUs, gloo otherwise.  Only the
+    timing max-reduce and barriers cross ranks."""
+    world, rank, local = rank_info()
     dist = None
     if world > 1:
         import torch
         import torch.distributed as dist
-        torch.cuda.set_device(local)
-        dist.init_process_group("nccl")
+        backend = backend or ("nccl" if torch.cuda.is_available() else "gloo")
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
     return world, rank, local, dist
 
 
@@ -134,7 +142,8 @@ def max_over_ranks(x, dist, world):
     if dist is None or world == 1:
         return x
     import torch
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 
@@ -168,7 +177,9 @@ def cpu_baseline(cr, budget_s=20.0, nthreads=None):
 
 
 def run_reference(args):
-    world, rank, local, dist = dist_setup(args.gpus)
+    # rank 0 alone times the CPU reference; the other ranks exit without work
+    # (and without joining a process group)
+    world, rank, _ = rank_info()
     if rank != 0:
         return 0
     from cella_nova_gb300.creature import make_creature
