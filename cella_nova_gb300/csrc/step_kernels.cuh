@@ -447,16 +447,16 @@ template <int LOGN, int V = 0>
 struct DiffGeo2 {
     using G = Geo<LOGN, V>;
     static constexpr int N = G::N, TX = G::TX, TY = G::TY;
-    static constexpr int NSEG = 2;
+    static constexpr int NSEG = 4;
     static constexpr int AS = TX + 8, AH = TY + 4, HW = TX + 2, QH = TY + 2;
-    static constexpr int ZR = QH / NSEG;       // Z rows per segment
-    static constexpr int OR = TY / NSEG;       // output rows per segment
+    static constexpr int ZR = (QH + NSEG - 1) / NSEG;   // Z rows per segment, at most
+    static constexpr int OR = TY / NSEG;                // output rows per segment
     static constexpr int THREADS = ((HW * NSEG + 31) / 32) * 32;
     static constexpr int V4 = AS / 4;          // 16-byte loads per A row
     static constexpr int LR = THREADS / V4;    // A rows per sweep of the block
     static constexpr int SWEEPS = (AH + LR - 1) / LR;
     static constexpr size_t SMEM = size_t(2 * AH * AS + QH * HW) * sizeof(float);
-    static_assert(QH % NSEG == 0 && TY % NSEG == 0 && TX % 4 == 0, "tile shape");
+    static_assert(TY % NSEG == 0 && TX % 4 == 0, "tile shape");
 };
 
 template <int LOGN, int V = 0>
@@ -476,13 +476,15 @@ __device__ __forceinline__ void diffusion2_body(const float* __restrict__ A,
 
     // this thread's Z column and rows, and the state there (loaded first)
     const bool zthr = t < HW * D::NSEG;
-    const int zq = t % HW, zr0 = (t / HW) * D::ZR;
+    const int zq = t % HW, zseg = t / HW;
+    const int zr0 = zseg * QH / D::NSEG, zn = (zseg + 1) * QH / D::NSEG - zr0;
     float xv[D::ZR];
     if (zthr) {
         const float* xcol = xc + ((x0 + zq - 1) & (N - 1));
         const int base = (y0 + zr0 - 1) * N;
 #pragma unroll
-        for (int i = 0; i < D::ZR; ++i) xv[i] = __ldg(xcol + ((base + i * N) & MASK));
+        for (int i = 0; i < D::ZR; ++i)
+            if (i < zn) xv[i] = __ldg(xcol + ((base + i * N) & MASK));
     }
     // the A tile, split into 12-bit heads and exact tails
     if (t < D::LR * D::V4) {
@@ -517,6 +519,7 @@ __device__ __forceinline__ void diffusion2_body(const float* __restrict__ A,
         float h1 = ph[AS] + ph[AS + 1] + ph[AS + 2], l1 = pl[AS] + pl[AS + 1] + pl[AS + 2];
 #pragma unroll
         for (int i = 0; i < D::ZR; ++i) {
+            if (i >= zn) break;
             const int o = (i + 2) * AS;
             const float h2 = ph[o] + ph[o + 1] + ph[o + 2];
             const float l2 = pl[o] + pl[o + 1] + pl[o + 2];
