@@ -126,8 +126,7 @@ __device__ __forceinline__ void gather_rows(const float2* __restrict__ src, floa
 template <int LOGN, class OUT>
 __device__ __forceinline__ void c2r_rows(float2* buf, const float2* __restrict__ tw, OUT& out) {
     using G = Geo<LOGN>;
-    auto smld = [&](int s, int i, int, int) { return buf[s * G::RP + pidx(i)]; };
-    auto smst = [&](int s, int i, float2 v, int, int) { buf[s * G::RP + pidx(i)] = v; };
+    SmemRows rows{buf, G::RP};
     auto ld0 = [&](int s, int m, int, int) -> float2 {
         const float2* row = buf + s * G::RP;
         if (m == 0) {
@@ -141,7 +140,7 @@ __device__ __forceinline__ void c2r_rows(float2* buf, const float2* __restrict__
         return make_float2(E.x - O.y, E.y + O.x);
     };
     auto st = [&](int s, int i, float2 v, int, int) { out(s, i, v); };
-    FftPasses<G::M, 1, true, G::RT, G::RB>::run(ld0, smld, smst, st, tw + G::TW_ROW);
+    FftPasses<G::M, 1, true, G::RT, G::RB>::run(ld0, rows, rows, st, tw + G::TW_ROW);
 }
 
 __device__ __forceinline__ double block_sum(double v, double* red) {
@@ -191,9 +190,8 @@ __device__ __forceinline__ void growth_bwd_body(float2* __restrict__ U,
         sm[s * G::RP + pidx(i)] = make_float2(ub[0], ub[1]);
     };
     c2r_rows<LOGN>(sm, tw, out);
-    auto smld = [&](int s, int i, int, int) { return sm[s * G::RP + pidx(i)]; };
-    auto smst = [&](int s, int i, float2 v, int, int) { sm[s * G::RP + pidx(i)] = v; };
-    FftPasses<G::M, 1, false, G::RT, G::RB>::run(smld, smld, smst, smst, tw + G::TW_ROW);
+    SmemRows rows{sm, G::RP};
+    FftPasses<G::M, 1, false, G::RT, G::RB>::run(rows, rows, rows, rows, tw + G::TW_ROW);
     r2c_finish<LOGN>(sm, tw, Uk);
     const double sw = block_sum(double(pw), red);
     const double smu = block_sum(double(pmu), red);
@@ -267,15 +265,14 @@ __device__ __forceinline__ bool col_conv_adj_body(float2* __restrict__ rowspec,
         return true;
     };
     auto ld_in = [&](int s, int i, int, int) { return KS[s * N + i]; };
-    auto wld = [&](int s, int i, int, int) { return W[s * G::CP + pidx(i)]; };
-    auto wst = [&](int s, int i, float2 v, int, int) { W[s * G::CP + pidx(i)] = v; };
+    SmemRows wrows{W, G::CP};
 
     for (int gi = 0; gi < cnt; ++gi) {
         const int k = groups.in_idx[base + gi];
         issue(U + (size_t(k) * M + kx0) * N);
         if (!wait_tile()) return false;
         const float2* ktile = kspec + (size_t(k) * (M + 1) + kx0) * N;
-        fft_with_hook<N, false, T, TW, false>(ld_in, wld, wst, wst, tw + G::TW_COL_FWD,
+        fft_with_hook<N, false, T, TW, false>(ld_in, wrows, wrows, wrows, tw + G::TW_COL_FWD,
                                              [&]() { issue(ktile); });
         if (!wait_tile()) return false;
         const float2* kb = kspec + (size_t(k) * (M + 1) + M) * N;
@@ -301,7 +298,7 @@ __device__ __forceinline__ bool col_conv_adj_body(float2* __restrict__ rowspec,
     }
     auto ld_acc = [&](int, int, int it, int r) { return acc[it][r]; };
     auto gst = [&](int s, int i, float2 v, int, int) { dst[size_t(s) * N + i] = v; };
-    FftPasses<N, 1, true, T, TW, true>::run(ld_acc, wld, wst, gst, tw + G::TW_COL_INV);
+    FftPasses<N, 1, true, T, TW, true>::run(ld_acc, wrows, wrows, gst, tw + G::TW_COL_INV);
     return true;
 }
 
@@ -374,9 +371,8 @@ __global__ void __launch_bounds__(256) k_kgrad(const float2* __restrict__ rowspe
     if (cnt == 0) return;
     auto fwd = [&](const float2* src, float2* buf) {
         auto ld = [&](int s, int i, int, int) { return __ldg(&src[size_t(s) * N + i]); };
-        auto bl = [&](int s, int i, int, int) { return buf[s * G::CP + pidx(i)]; };
-        auto bs = [&](int s, int i, float2 v, int, int) { buf[s * G::CP + pidx(i)] = v; };
-        FftPasses<N, 1, false, T, TW, false>::run(ld, bl, bs, bs, tw + G::TW_COL_FWD);
+        SmemRows rows{buf, G::CP};
+        FftPasses<N, 1, false, T, TW, false>::run(ld, rows, rows, rows, tw + G::TW_COL_FWD);
     };
     fwd(rowspec + (size_t(c) * M + kx0) * N, Wx);
     for (int gi = 0; gi < cnt; ++gi) {
@@ -419,10 +415,9 @@ __global__ void __launch_bounds__(256) k_col_inv(float2* __restrict__ spec,
     extern __shared__ __align__(128) float2 sm_ci[];
     float2* col = spec + (size_t(blockIdx.y) * M + blockIdx.x * TW) * N;
     auto ld = [&](int s, int i, int, int) { return col[size_t(s) * N + i]; };
-    auto bl = [&](int s, int i, int, int) { return sm_ci[s * G::CP + pidx(i)]; };
-    auto bs = [&](int s, int i, float2 v, int, int) { sm_ci[s * G::CP + pidx(i)] = v; };
+    SmemRows rows{sm_ci, G::CP};
     auto st = [&](int s, int i, float2 v, int, int) { col[size_t(s) * N + i] = v; };
-    FftPasses<N, 1, true, T, TW, false>::run(ld, bl, bs, st, tw + G::TW_COL_FWD);
+    FftPasses<N, 1, true, T, TW, false>::run(ld, rows, rows, st, tw + G::TW_COL_FWD);
 }
 
 // ---------------------------------------------------------------------------

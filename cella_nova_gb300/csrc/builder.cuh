@@ -24,9 +24,8 @@ __global__ void __launch_bounds__(256) k_kspec_cols(const float2* __restrict__ r
     const int k = blockIdx.y, kx0 = blockIdx.x * TW;
     const float2* src = rows + (size_t(k) * M + kx0) * N;
     auto ld = [&](int s, int i, int, int) { return __ldg(&src[size_t(s) * N + i]); };
-    auto bl = [&](int s, int i, int, int) { return sm_kb[s * G::CP + pidx(i)]; };
-    auto bs = [&](int s, int i, float2 v, int, int) { sm_kb[s * G::CP + pidx(i)] = v; };
-    FftPasses<N, 1, false, T, TW, false>::run(ld, bl, bs, bs, tw + G::TW_COL_FWD);
+    SmemRows cols{sm_kb, G::CP};
+    FftPasses<N, 1, false, T, TW, false>::run(ld, cols, cols, cols, tw + G::TW_COL_FWD);
     __syncthreads();
     // P = 2 K^ (column kx >= 1); kspec holds K^ / (2 N^2 sum h)
     const double z = zsum[k];

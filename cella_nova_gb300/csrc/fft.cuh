@@ -16,12 +16,27 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 namespace cg {
 
 // Shared-memory index padding: one spare float2 per 16, which keeps the
 // strided stores of every pass free of bank conflicts within a half-warp.
-__device__ __forceinline__ int pidx(int i) { return i + (i >> 4); }
+__host__ __device__ constexpr int pidx(int i) { return i + (i >> 4); }
 __host__ __device__ constexpr int padded_len(int n) { return n + n / 16; }
+
+// S padded sequences in shared memory, sequence s at buf + s * pitch.  A pass
+// that reads or writes one of these addresses element j + c (c = r * J or
+// r * NS, a compile-time constant after unrolling) as pidx(j) + pidx(c): the
+// low four bits of j and c never carry into each other in any Stockham pass
+// of a power-of-two plan, so this equals pidx(j + c), and the per-element
+// offsets become immediates.
+struct SmemRows {
+    float2* buf;
+    int pitch;
+};
+template <class F>
+struct is_smem_rows : std::is_same<std::remove_cv_t<std::remove_reference_t<F>>, SmemRows> {};
 
 __device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
 __device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
@@ -151,8 +166,14 @@ __device__ __forceinline__ void stockham_pass(LD& ld, ST& st, const float2* __re
         const int item = threadIdx.x + it * T;
         if (ITEMS % T == 0 || item < ITEMS) {
             const int s = item / J, j = item % J;
+            if constexpr (is_smem_rows<LD>::value) {
+                const float2* b = ld.buf + s * ld.pitch + pidx(j);
 #pragma unroll
-            for (int r = 0; r < R; ++r) v[it][r] = ld(s, j + r * J, it, r);
+                for (int r = 0; r < R; ++r) v[it][r] = b[pidx(r * J)];
+            } else {
+#pragma unroll
+                for (int r = 0; r < R; ++r) v[it][r] = ld(s, j + r * J, it, r);
+            }
         }
     }
     __syncthreads();
@@ -172,8 +193,14 @@ __device__ __forceinline__ void stockham_pass(LD& ld, ST& st, const float2* __re
             }
             Dft<R, INV>::run(v[it]);
             const int d = (j / NS) * NS * R + k;
+            if constexpr (is_smem_rows<ST>::value) {
+                float2* b = st.buf + s * st.pitch + pidx(d);
 #pragma unroll
-            for (int r = 0; r < R; ++r) st(s, d + r * NS, v[it][r], it, r);
+                for (int r = 0; r < R; ++r) b[pidx(r * NS)] = v[it][r];
+            } else {
+#pragma unroll
+                for (int r = 0; r < R; ++r) st(s, d + r * NS, v[it][r], it, r);
+            }
         }
     }
     __syncthreads();

@@ -93,9 +93,8 @@ __device__ __forceinline__ void row_r2c_body(const float* __restrict__ state,
     const float2* src =
         reinterpret_cast<const float2*>(state + (size_t(c) * G::N + y0) * G::N);
     auto ld0 = [&](int s, int i, int, int) { return __ldg(&src[size_t(s) * G::M + i]); };
-    auto smld = [&](int s, int i, int, int) { return sm[s * G::RP + pidx(i)]; };
-    auto smst = [&](int s, int i, float2 v, int, int) { sm[s * G::RP + pidx(i)] = v; };
-    FftPasses<G::M, 1, false, G::RT, G::RB>::run(ld0, smld, smst, smst, tw + G::TW_ROW);
+    SmemRows rows{sm, G::RP};
+    FftPasses<G::M, 1, false, G::RT, G::RB>::run(ld0, rows, rows, rows, tw + G::TW_ROW);
     r2c_finish<LOGN, V>(sm, tw, rowspec + size_t(c) * G::M * G::N + y0);
 }
 
@@ -232,10 +231,9 @@ __device__ __forceinline__ bool col_conv_body(const float2* __restrict__ rowspec
     constexpr int IPTL = (TW * JL + T - 1) / T;
     float2 F[IPTL][RL];
     auto ld_in = [&](int s, int i, int, int) { return KS[s * N + i]; };
-    auto wld = [&](int s, int i, int, int) { return W[s * G::CP + pidx(i)]; };
-    auto wst = [&](int s, int i, float2 v, int, int) { W[s * G::CP + pidx(i)] = v; };
+    SmemRows wrows{W, G::CP};
     auto keep = [&](int, int, float2 v, int it, int r) { F[it][r] = v; };
-    fft_with_hook<N, false, T, TW, false>(ld_in, wld, wst, keep, tw + G::TW_COL_FWD,
+    fft_with_hook<N, false, T, TW, false>(ld_in, wrows, wrows, keep, tw + G::TW_COL_FWD,
                                          [&]() { issue(kernel_tile(0)); });
 
     for (int gi = 0; gi < cnt; ++gi) {
@@ -266,7 +264,7 @@ __device__ __forceinline__ bool col_conv_body(const float2* __restrict__ rowspec
         };
         float2* dst = U + (size_t(k) * M + kx0) * N;
         auto gst = [&](int s, int i, float2 v, int, int) { dst[size_t(s) * N + i] = v; };
-        fft_with_hook<N, true, T, TW, true>(ld_mul, wld, wst, gst, tw + G::TW_COL_INV, [&]() {
+        fft_with_hook<N, true, T, TW, true>(ld_mul, wrows, wrows, gst, tw + G::TW_COL_INV, [&]() {
             if (gi + 1 < cnt) issue(kernel_tile(gi + 1));
         });
     }
@@ -353,8 +351,7 @@ __device__ __forceinline__ void row_c2r_growth_body(const float2* __restrict__ U
             cp_async_wait<0>();
         }
         __syncthreads();
-        auto smld = [&](int s, int i, int, int) { return buf[s * G::RP + pidx(i)]; };
-        auto smst = [&](int s, int i, float2 v, int, int) { buf[s * G::RP + pidx(i)] = v; };
+        SmemRows rows{buf, G::RP};
         auto ld0 = [&](int s, int m, int, int) -> float2 {
             const float2* row = buf + s * G::RP;
             if (m == 0) {
@@ -381,7 +378,7 @@ __device__ __forceinline__ void row_c2r_growth_body(const float2* __restrict__ U
                     make_float2(v.x * udbg_scale, v.y * udbg_scale);
             }
         };
-        FftPasses<G::M, 1, true, G::RT, G::RB>::run(ld0, smld, smst, gst, tw + G::TW_ROW);
+        FftPasses<G::M, 1, true, G::RT, G::RB>::run(ld0, rows, rows, gst, tw + G::TW_ROW);
     }
 
     float* Ac = A + (size_t(c) * G::N + y0) * G::N;
