@@ -433,30 +433,27 @@ __device__ __forceinline__ float head12(float a) {
     return __int_as_float(__float_as_int(a) & 0xFFFFF000);
 }
 
-// Each thread owns four adjacent columns.  Horizontal 3-sums of four columns
-// take six consecutive values, read as one 8-byte and one 16-byte shared load;
-// vertical sums are carried in registers down the thread's rows (Z phase:
-// ZR rows of the TY+2 halo rows, output phase: OR rows), the state arrives by
-// 16-byte loads and the result leaves by 16-byte stores.  Every sum keeps a
-// fixed order ((a + b) + c, heads and tails apart), so all tile shapes give
-// the same bits.
+// Horizontal 3-sums come from shared memory, vertical ones are carried in
+// registers down a column: NSEG segments of rows per tile; in the Z phase one
+// thread owns one of the TX+2 halo columns of a segment, in the output phase
+// one of the TX columns.  Every sum keeps a fixed order ((a + b) + c, heads
+// and tails apart), so all tile shapes give the same bits.  The A tile is read with 16-byte loads (a 4-pixel side
+// halo keeps them aligned; the toroidal wrap stays aligned because n is a
+// multiple of 4).
 template <int LOGN, int V = 0>
 struct DiffGeo2 {
     using G = Geo<LOGN, V>;
     static constexpr int N = G::N, TX = G::TX, TY = G::TY;
-    static constexpr int AS = TX + 8, AH = TY + 4, QH = TY + 2, QS = TX + 4;
-    static constexpr int OG = TX / 4;                    // output column groups
-    static constexpr int ZG = (TX + 2 + 3) / 4;          // Z column groups (the last partly spare)
-    static constexpr int OR = 4;                         // output rows per thread
-    static constexpr int THREADS = ((OG * (TY / OR) + 31) / 32) * 32;
-    static constexpr int NSZ = THREADS / ZG;             // Z row segments
-    static constexpr int ZR = (QH + NSZ - 1) / NSZ;      // Z rows per segment, at most
-    static constexpr int V4 = AS / 4;                    // 16-byte loads per A row
-    static constexpr int LR = THREADS / V4;              // A rows per sweep of the block
+    static constexpr int NSEG = 4;
+    static constexpr int AS = TX + 8, AH = TY + 4, HW = TX + 2, QH = TY + 2;
+    static constexpr int ZR = (QH + NSEG - 1) / NSEG;   // Z rows per segment, at most
+    static constexpr int OR = TY / NSEG;                // output rows per segment
+    static constexpr int THREADS = ((HW * NSEG + 31) / 32) * 32;
+    static constexpr int V4 = AS / 4;          // 16-byte loads per A row
+    static constexpr int LR = THREADS / V4;    // A rows per sweep of the block
     static constexpr int SWEEPS = (AH + LR - 1) / LR;
-    static constexpr size_t SMEM = size_t(2 * AH * AS + QH * QS) * sizeof(float);
-    static_assert(TY % OR == 0 && TX % 4 == 0 && NSZ >= 1 && LR >= 1, "tile shape");
-    static_assert(4 * ZG + 4 <= AS && 4 * ZG <= QS, "Z groups stay inside the tiles");
+    static constexpr size_t SMEM = size_t(2 * AH * AS + QH * HW) * sizeof(float);
+    static_assert(TY % NSEG == 0 && TX % 4 == 0, "tile shape");
 };
 
 template <int LOGN, int V = 0>
@@ -465,37 +462,26 @@ __device__ __forceinline__ void diffusion2_body(const float* __restrict__ A,
                                                 float* __restrict__ out, int c, int x0, int y0,
                                                 float* smf, unsigned char* render, int nch) {
     using D = DiffGeo2<LOGN, V>;
-    constexpr int N = D::N, AS = D::AS, AH = D::AH, QH = D::QH, QS = D::QS;
+    constexpr int N = D::N, TX = D::TX, AS = D::AS, AH = D::AH, HW = D::HW, QH = D::QH;
     constexpr int MASK = N * N - 1;            // row offsets wrap as (row * N) & MASK
     float* sAh = smf;                  // [AH][AS]: row a <-> y0 + a - 2, column j <-> x0 - 4 + j
     float* sAl = smf + AH * AS;
-    float* sQ = smf + 2 * AH * AS;     // [QH][QS]: row b <-> y0 + b - 1, column q <-> x0 - 1 + q
+    float* sQ = smf + 2 * AH * AS;     // [QH][HW]: row b <-> y0 + b - 1, column q <-> x0 - 1 + q
     const float* Ac = A + size_t(c) * N * N;
     const float* xc = x + size_t(c) * N * N;
     const int t = threadIdx.x;
 
-    // Z phase work: columns 4 zu .. 4 zu + 3, rows zr0 .. zr0 + zn - 1
-    const int zu = t % D::ZG, zs = t / D::ZG;
-    const int zr0 = zs * D::ZR;
-    const int zn = zs < D::NSZ ? min(D::ZR, QH - zr0) : 0;
-    // the state there (columns x0 - 1 + 4 zu + m), from two aligned 16-byte loads a row
-    float xv[D::ZR][4];
-    if (zn > 0) {
-        const float* xa = xc + ((x0 + 4 * zu - 4) & (N - 1));
-        const float* xb = xc + ((x0 + 4 * zu) & (N - 1));
+    // this thread's Z column and rows, and the state there (loaded first)
+    const bool zthr = t < HW * D::NSEG;
+    const int zq = t % HW, zseg = t / HW;
+    const int zr0 = zseg * QH / D::NSEG, zn = (zseg + 1) * QH / D::NSEG - zr0;
+    float xv[D::ZR];
+    if (zthr) {
+        const float* xcol = xc + ((x0 + zq - 1) & (N - 1));
         const int base = (y0 + zr0 - 1) * N;
 #pragma unroll
-        for (int i = 0; i < D::ZR; ++i) {
-            if (i < zn) {
-                const int o = (base + i * N) & MASK;
-                const float4 u = __ldg(reinterpret_cast<const float4*>(xa + o));
-                const float4 w = __ldg(reinterpret_cast<const float4*>(xb + o));
-                xv[i][0] = u.w;
-                xv[i][1] = w.x;
-                xv[i][2] = w.y;
-                xv[i][3] = w.z;
-            }
-        }
+        for (int i = 0; i < D::ZR; ++i)
+            if (i < zn) xv[i] = __ldg(xcol + ((base + i * N) & MASK));
     }
     // the A tile, split into 12-bit heads and exact tails
     if (t < D::LR * D::V4) {
@@ -521,98 +507,56 @@ __device__ __forceinline__ void diffusion2_body(const float* __restrict__ A,
     }
     __syncthreads();
 
-    // out[m] = (p[m] + p[m+1]) + p[m+2], m < 4, from p[0..1] (8-byte aligned)
-    // and p[2..5] (16-byte aligned)
-    auto sum3x4_a = [](const float* p, float* o) {
-        const float2 a = *reinterpret_cast<const float2*>(p);
-        const float4 b = *reinterpret_cast<const float4*>(p + 2);
-        o[0] = a.x + a.y + b.x;
-        o[1] = a.y + b.x + b.y;
-        o[2] = b.x + b.y + b.z;
-        o[3] = b.y + b.z + b.w;
-    };
-    // the same from p[0..3] (16-byte aligned) and p[4..5]
-    auto sum3x4_b = [](const float* p, float* o) {
-        const float4 a = *reinterpret_cast<const float4*>(p);
-        const float2 b = *reinterpret_cast<const float2*>(p + 4);
-        o[0] = a.x + a.y + a.z;
-        o[1] = a.y + a.z + a.w;
-        o[2] = a.z + a.w + b.x;
-        o[3] = a.w + b.x + b.y;
-    };
-
-    // Z = zh + zl down this thread's four columns, then q = x / Z
-    if (zn > 0) {
-        const float* ph = sAh + zr0 * AS + 4 * zu + 2;   // A columns x0 - 2 + 4 zu ..
-        const float* pl = sAl + zr0 * AS + 4 * zu + 2;
-        float* pq = sQ + zr0 * QS + 4 * zu;
-        float h0[4], l0[4], h1[4], l1[4];
-        sum3x4_a(ph, h0);
-        sum3x4_a(pl, l0);
-        sum3x4_a(ph + AS, h1);
-        sum3x4_a(pl + AS, l1);
+    // Z = zh + zl down this thread's column, then q = x / Z
+    if (zthr) {
+        const float* ph = sAh + zr0 * AS + zq + 2;   // A columns x0 - 2 + zq .. x0 + zq
+        const float* pl = sAl + zr0 * AS + zq + 2;
+        float* pq = sQ + zr0 * HW + zq;
+        float h0 = ph[0] + ph[1] + ph[2], l0 = pl[0] + pl[1] + pl[2];
+        float h1 = ph[AS] + ph[AS + 1] + ph[AS + 2], l1 = pl[AS] + pl[AS + 1] + pl[AS + 2];
 #pragma unroll
         for (int i = 0; i < D::ZR; ++i) {
             if (i >= zn) break;
-            float h2[4], l2[4], q[4];
-            sum3x4_a(ph + (i + 2) * AS, h2);
-            sum3x4_a(pl + (i + 2) * AS, l2);
-#pragma unroll
-            for (int m = 0; m < 4; ++m) {
-                const float zh = h0[m] + h1[m] + h2[m];
-                const float zt = l0[m] + l1[m] + l2[m];
-                const float z = zh + zt;
-                const float zl = zt - (z - zh);
-                const float rz = rcp_approx(z);
-                const float q0 = xv[i][m] * rz;
-                const float rem = fmaf(-q0, z, xv[i][m]);
-                q[m] = fmaf(rem - q0 * zl, rz, q0);
-                h0[m] = h1[m];
-                l0[m] = l1[m];
-                h1[m] = h2[m];
-                l1[m] = l2[m];
-            }
-            *reinterpret_cast<float4*>(pq + i * QS) = make_float4(q[0], q[1], q[2], q[3]);
+            const int o = (i + 2) * AS;
+            const float h2 = ph[o] + ph[o + 1] + ph[o + 2];
+            const float l2 = pl[o] + pl[o + 1] + pl[o + 2];
+            const float zh = h0 + h1 + h2;
+            const float zt = l0 + l1 + l2;
+            const float z = zh + zt;
+            const float zl = zt - (z - zh);
+            const float rz = rcp_approx(z);
+            const float q0 = xv[i] * rz;
+            const float rem = fmaf(-q0, z, xv[i]);
+            pq[i * HW] = fmaf(rem - q0 * zl, rz, q0);
+            h0 = h1;
+            l0 = l1;
+            h1 = h2;
+            l1 = l2;
         }
     }
     __syncthreads();
 
-    // new = A * (3x3 sum of q), down this thread's four output columns
-    const int ou = t % D::OG, os = t / D::OG;
-    if (os < D::TY / D::OR) {
-        const int r0 = os * D::OR;
-        const float* pq = sQ + r0 * QS + 4 * ou;
-        const float* pa = sAh + (r0 + 2) * AS + 4 * ou + 4;
-        const float* pb = sAl + (r0 + 2) * AS + 4 * ou + 4;
-        const int p0 = (y0 + r0) * N + x0 + 4 * ou;
+    // new = A * (3x3 sum of q), down this thread's output column
+    if (t < TX * D::NSEG) {
+        const int fq = t % TX, r0 = (t / TX) * D::OR;
+        const float* pq = sQ + r0 * HW + fq;
+        const float* pa = sAh + (r0 + 2) * AS + fq + 4;
+        const float* pb = sAl + (r0 + 2) * AS + fq + 4;
+        const int p0 = (y0 + r0) * N + x0 + fq;
         float* oc = out + size_t(c) * N * N + p0;
         const bool draw = render != nullptr && c < 3;
-        float s0[4], s1[4];
-        sum3x4_b(pq, s0);
-        sum3x4_b(pq + QS, s1);
+        float s0 = pq[0] + pq[1] + pq[2];
+        float s1 = pq[HW] + pq[HW + 1] + pq[HW + 2];
 #pragma unroll
         for (int i = 0; i < D::OR; ++i) {
-            float s2[4];
-            sum3x4_b(pq + (i + 2) * QS, s2);
-            const float4 ah = *reinterpret_cast<const float4*>(pa + i * AS);
-            const float4 al = *reinterpret_cast<const float4*>(pb + i * AS);
-            const float4 v = make_float4((ah.x + al.x) * ((s0[0] + s1[0]) + s2[0]),
-                                         (ah.y + al.y) * ((s0[1] + s1[1]) + s2[1]),
-                                         (ah.z + al.z) * ((s0[2] + s1[2]) + s2[2]),
-                                         (ah.w + al.w) * ((s0[3] + s1[3]) + s2[3]));
-            *reinterpret_cast<float4*>(oc + i * N) = v;
-            if (draw) {
-                const size_t p = size_t(p0 + i * N);
-                render_store(render, nch, c, p, v.x);
-                render_store(render, nch, c, p + 1, v.y);
-                render_store(render, nch, c, p + 2, v.z);
-                render_store(render, nch, c, p + 3, v.w);
-            }
-#pragma unroll
-            for (int m = 0; m < 4; ++m) {
-                s0[m] = s1[m];
-                s1[m] = s2[m];
-            }
+            const int o = (i + 2) * HW;
+            const float s2 = pq[o] + pq[o + 1] + pq[o + 2];
+            const float a = pa[i * AS] + pb[i * AS];
+            const float v = a * ((s0 + s1) + s2);
+            oc[i * N] = v;
+            if (draw) render_store(render, nch, c, size_t(p0 + i * N), v);
+            s0 = s1;
+            s1 = s2;
         }
     }
 }
