@@ -380,6 +380,10 @@ def run_batched(args):
     gen_s = time.perf_counter() - t0
     cells = sum(cr.n * cr.n for cr in crs)
     b = GpuMaceLeniaBatch(crs)
+    tuned = None
+    if not args.no_autotune:
+        tuned = {str(k): {"variants": v[0], "ms": np.round(v[1], 4).tolist()}
+                 for k, v in b.autotune(reps=5).items()}
     stream = torch.cuda.ExternalStream(b.stream())
     sampler = ClockSampler(local)
     sampler.start()
@@ -400,10 +404,13 @@ def run_batched(args):
     items, grid = b.info()
     b.close()
     # the plain single-world path on the same worlds, one world at a time
+    # (each world autotuned like the batch)
     plain_steps = max(3, min(args.steps, 20))
     plain_s = 0.0
     for cr in crs:
         s = GpuMaceLenia.from_creature(cr)
+        if not args.no_autotune:
+            s.autotune(reps=3)
         s.run_steps(2)
         s.synchronize()
         st = torch.cuda.ExternalStream(s.stream())
@@ -434,7 +441,7 @@ def run_batched(args):
         "batched_over_plain": (cells / (ms / 1e3 / args.steps)) / (cells / plain_s),
         "phase_ms": {"row_r2c": phase_ms[0], "col_conv": phase_ms[1],
                      "row_c2r_growth": phase_ms[2], "diffusion": phase_ms[3]},
-        "work_items": items, "persistent_grid": grid,
+        "work_items": items, "persistent_grid": grid, "autotune": tuned,
         # one persistent launch per phase per grid size
         "gpu_launches": 4 * len({cr.n for cr in crs}) * args.steps, "clocks": clocks,
         "setup_s": {"generate": gen_s},

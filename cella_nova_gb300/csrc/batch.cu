@@ -45,28 +45,30 @@ struct WorkItem {
 };
 
 
-// One persistent kernel per phase and grid size: a kernel that served
-// several sizes made the compiler spill the column pass's register-resident
-// spectrum, so each size gets its own instantiation.  Within one size the
-// items cost about the same (sorted by cost, largest first), so each
-// resident CTA takes items blockIdx.x, blockIdx.x + gridDim.x, ...
-template <int LOGN>
-__global__ void __launch_bounds__(512, 2) kb_row_r2c(const WorldDesc* __restrict__ worlds,
-                                                   const WorkItem* __restrict__ items, int count,
-                                                   int parity) {
+// One persistent kernel per phase, grid size and CTA-shape variant: a kernel
+// that served several sizes made the compiler spill the column pass's
+// register-resident spectrum, so each size gets its own instantiation.
+// Within one size the items cost about the same (sorted by cost, largest
+// first), so each resident CTA takes items blockIdx.x, blockIdx.x + gridDim.x,
+// ...  The variants are the single-world kernels' (Geo<LOGN, V>), with the same
+// bits.
+template <int LOGN, int V>
+__global__ void __launch_bounds__(Geo<LOGN, V>::RT, 512 / Geo<LOGN, V>::RT)
+    kb_row_r2c(const WorldDesc* __restrict__ worlds, const WorkItem* __restrict__ items, int count,
+               int parity) {
     extern __shared__ __align__(128) float2 smb_r2c[];
     for (int i = blockIdx.x; i < count; i += gridDim.x) {
         __syncthreads();
         const WorkItem it = items[i];
         const WorldDesc& w = worlds[it.world];
-        row_r2c_body<LOGN>(w.state[parity], w.rowspec, w.tw, it.c, it.a, smb_r2c);
+        row_r2c_body<LOGN, V>(w.state[parity], w.rowspec, w.tw, it.c, it.a, smb_r2c);
     }
 }
 
-template <int LOGN>
-__global__ void __launch_bounds__(256, 2) kb_col_conv(const WorldDesc* __restrict__ worlds,
-                                                       const WorkItem* __restrict__ items,
-                                                       int count, int* err) {
+template <int LOGN, int V>
+__global__ void __launch_bounds__(Geo<LOGN, V>::CT, 512 / Geo<LOGN, V>::CT)
+    kb_col_conv(const WorldDesc* __restrict__ worlds, const WorkItem* __restrict__ items, int count,
+                int* err) {
     extern __shared__ __align__(128) float2 smb_col[];
     __shared__ __align__(8) uint64_t bar;
     init_tile_barrier(&bar);
@@ -75,103 +77,76 @@ __global__ void __launch_bounds__(256, 2) kb_col_conv(const WorldDesc* __restric
         __syncthreads();
         const WorkItem it = items[i];
         const WorldDesc& w = worlds[it.world];
-        if (!col_conv_body<LOGN>(w.rowspec, w.kspec, w.U, w.tw, w.groups, it.c, it.a, smb_col,
-                                 &bar, phase, err))
+        if (!col_conv_body<LOGN, V>(w.rowspec, w.kspec, w.U, w.tw, w.groups, it.c, it.a, smb_col,
+                                    &bar, phase, err))
             return;   // a bounded wait timed out (uniform across the block)
     }
 }
 
-template <int LOGN>
-__global__ void __launch_bounds__(512) kb_row_c2r_growth(const WorldDesc* __restrict__ worlds,
-                                                          const WorkItem* __restrict__ items,
-                                                          int count) {
+template <int LOGN, int V>
+__global__ void __launch_bounds__(Geo<LOGN, V>::RT, 512 / Geo<LOGN, V>::RT)
+    kb_row_c2r_growth(const WorldDesc* __restrict__ worlds, const WorkItem* __restrict__ items,
+                      int count) {
     extern __shared__ __align__(128) float2 smb_c2r[];
     for (int i = blockIdx.x; i < count; i += gridDim.x) {
         __syncthreads();
         const WorkItem it = items[i];
         const WorldDesc& w = worlds[it.world];
-        row_c2r_growth_body<LOGN>(w.U, w.A, w.tw, w.groups, w.gp, w.temp, nullptr, 0.f, it.c,
-                                  it.a, smb_c2r);
+        row_c2r_growth_body<LOGN, V>(w.U, w.A, w.tw, w.groups, w.gp, w.temp, nullptr, 0.f, it.c,
+                                     it.a, smb_c2r);
     }
 }
 
-// Every batched size (64 and up) uses 64-wide diffusion tiles, hence one
-// block size for the phase.
-constexpr int kDiffThreads = DiffGeo2<6>::THREADS;
-static_assert(DiffGeo2<11>::THREADS == kDiffThreads, "one diffusion block size for all sizes");
-
-template <int LOGN>
-__global__ void __launch_bounds__(kDiffThreads) kb_diffusion(const WorldDesc* __restrict__ worlds,
-                                                              const WorkItem* __restrict__ items,
-                                                              int count, int parity) {
+template <int LOGN, int V>
+__global__ void __launch_bounds__(DiffGeo2<LOGN, V>::THREADS)
+    kb_diffusion(const WorldDesc* __restrict__ worlds, const WorkItem* __restrict__ items,
+                 int count, int parity) {
     extern __shared__ __align__(128) float smb_diff[];
     for (int i = blockIdx.x; i < count; i += gridDim.x) {
         __syncthreads();
         const WorkItem it = items[i];
         const WorldDesc& w = worlds[it.world];
-        diffusion2_body<LOGN>(w.A, w.state[parity], w.state[parity ^ 1], it.c, it.a, it.b,
-                              smb_diff, nullptr, 0);
+        diffusion2_body<LOGN, V>(w.A, w.state[parity], w.state[parity ^ 1], it.c, it.a, it.b,
+                                 smb_diff, nullptr, 0);
     }
 }
 
-// The four persistent kernels of one size, as untyped pointers for the
-// occupancy query and the launches.
-struct PhaseFns {
-    const void* fn[4];
-};
-template <int LOGN>
-PhaseFns phase_fns() {
-    return {{reinterpret_cast<const void*>(kb_row_r2c<LOGN>),
-             reinterpret_cast<const void*>(kb_col_conv<LOGN>),
-             reinterpret_cast<const void*>(kb_row_c2r_growth<LOGN>),
-             reinterpret_cast<const void*>(kb_diffusion<LOGN>)}};
-}
-static PhaseFns phase_fns_for(int logn) {
-    switch (logn) {
-        case 6: return phase_fns<6>();
-        case 7: return phase_fns<7>();
-        case 8: return phase_fns<8>();
-        case 9: return phase_fns<9>();
-        case 10: return phase_fns<10>();
-        default: return phase_fns<11>();
-    }
-}
+constexpr int kVariants = 3;
 
-// Per-size shared-memory needs (bytes) of the four phases.
-struct PhaseSmem {
-    size_t r2c, col, c2r, diff;
+// Per size and variant: the four kernels, their block sizes, shared memory
+// and the unit each work item covers.
+struct PhaseVariant {
+    const void* fn;
+    int threads;
+    size_t smem;
+    int unit_a, unit_b;   // rows per item (row phases), columns per item (column
+                          // phase), tile width and height (diffusion)
 };
+template <int LOGN, int V>
+void fill_variant(PhaseVariant (&pv)[4][kVariants]) {
+    using G = Geo<LOGN, V>;
+    using D = DiffGeo2<LOGN, V>;
+    pv[0][V] = {reinterpret_cast<const void*>(kb_row_r2c<LOGN, V>), G::RT, G::R2C_SMEM, G::RB, 0};
+    pv[1][V] = {reinterpret_cast<const void*>(kb_col_conv<LOGN, V>), G::CT, G::COL_SMEM, G::TW, 0};
+    pv[2][V] = {reinterpret_cast<const void*>(kb_row_c2r_growth<LOGN, V>), G::RT, G::C2R_SMEM,
+                G::RB, 0};
+    pv[3][V] = {reinterpret_cast<const void*>(kb_diffusion<LOGN, V>), D::THREADS, D::SMEM, G::TX,
+                G::TY};
+}
 template <int LOGN>
-PhaseSmem phase_smem() {
-    using G = Geo<LOGN>;
-    return {G::R2C_SMEM, G::COL_SMEM, G::C2R_SMEM, DiffGeo2<LOGN>::SMEM};
+void fill_size(PhaseVariant (&pv)[4][kVariants]) {
+    fill_variant<LOGN, 0>(pv);
+    fill_variant<LOGN, 1>(pv);
+    fill_variant<LOGN, 2>(pv);
 }
-static PhaseSmem phase_smem_for(int logn) {
+static void phase_variants_for(int logn, PhaseVariant (&pv)[4][kVariants]) {
     switch (logn) {
-        case 6: return phase_smem<6>();
-        case 7: return phase_smem<7>();
-        case 8: return phase_smem<8>();
-        case 9: return phase_smem<9>();
-        case 10: return phase_smem<10>();
-        default: return phase_smem<11>();
-    }
-}
-struct UnitGeo {
-    int RB, TW, TX, TY;
-};
-template <int LOGN>
-UnitGeo unit_geo() {
-    using G = Geo<LOGN>;
-    return {G::RB, G::TW, G::TX, G::TY};
-}
-static UnitGeo unit_geo_for(int logn) {
-    switch (logn) {
-        case 6: return unit_geo<6>();
-        case 7: return unit_geo<7>();
-        case 8: return unit_geo<8>();
-        case 9: return unit_geo<9>();
-        case 10: return unit_geo<10>();
-        default: return unit_geo<11>();
+        case 6: fill_size<6>(pv); break;
+        case 7: fill_size<7>(pv); break;
+        case 8: fill_size<8>(pv); break;
+        case 9: fill_size<9>(pv); break;
+        case 10: fill_size<10>(pv); break;
+        default: fill_size<11>(pv); break;
     }
 }
 
@@ -191,15 +166,15 @@ struct cg_batch {
         KernelGroups groups{};
         GrowthParams gp{};
     };
-    // All worlds of one grid side: per phase a work list and a persistent
-    // grid.
+    // All worlds of one grid side: per phase and CTA-shape variant a work
+    // list and a persistent grid; var[] names the variant in use.
     struct SizeClass {
         int logn = 0;
-        PhaseFns fns{};
-        WorkItem* d_items[4] = {nullptr, nullptr, nullptr, nullptr};
-        int count[4] = {0, 0, 0, 0};
-        int grid[4] = {0, 0, 0, 0};
-        size_t smem[4] = {0, 0, 0, 0};
+        PhaseVariant pv[4][kVariants]{};
+        WorkItem* d_items[4][kVariants] = {};
+        int count[4][kVariants] = {};
+        int grid[4][kVariants] = {};
+        int var[4] = {0, 0, 0, 0};
     };
     std::vector<World> worlds;
     std::vector<SizeClass> classes;   // largest grid side first
@@ -237,7 +212,8 @@ void batch_release(cg_batch* b) {
     }
     for (auto p : b->tw_by_logn) cudaFree(p);
     for (auto& sc : b->classes)
-        for (auto p : sc.d_items) cudaFree(p);
+        for (auto& per_phase : sc.d_items)
+            for (auto p : per_phase) cudaFree(p);
     cudaFree(b->d_worlds);
     cudaFree(b->err);
     cudaFree(b->staging);
@@ -247,23 +223,27 @@ void batch_release(cg_batch* b) {
     delete b;
 }
 
+// One phase of one size class in variant v: a persistent launch.
+cudaError_t launch_class_phase(cg_batch* b, const cg_batch::SizeClass& sc, int phase, int v,
+                               int parity, cudaStream_t st) {
+    if (sc.count[phase][v] == 0) return cudaSuccess;
+    const PhaseVariant& pv = sc.pv[phase][v];
+    const WorldDesc* worlds = b->d_worlds;
+    const WorkItem* items = sc.d_items[phase][v];
+    int count = sc.count[phase][v];
+    void* args[4];
+    args[0] = &worlds;
+    args[1] = &items;
+    args[2] = &count;
+    if (phase == 1) args[3] = &b->err;
+    else args[3] = &parity;   // (the c2r kernel takes only three)
+    return cudaLaunchKernel(pv.fn, dim3(sc.grid[phase][v]), dim3(pv.threads), args, pv.smem, st);
+}
+
 // One phase: a persistent launch per size class (largest first).
 cudaError_t launch_phase(cg_batch* b, int phase, int parity, cudaStream_t st) {
-    static const unsigned threads[4] = {512, 256, 512, unsigned(kDiffThreads)};
-    for (size_t i = 0; i < b->classes.size(); ++i) {
-        auto& sc = b->classes[i];
-        if (sc.count[phase] == 0) continue;
-        const WorldDesc* worlds = b->d_worlds;
-        const WorkItem* items = sc.d_items[phase];
-        int count = sc.count[phase];
-        void* args5[4];
-        args5[0] = &worlds;
-        args5[1] = &items;
-        args5[2] = &count;
-        if (phase == 1) args5[3] = &b->err;
-        else args5[3] = &parity;   // (the c2r kernel takes only three)
-        cudaError_t e = cudaLaunchKernel(sc.fns.fn[phase], dim3(sc.grid[phase]), dim3(threads[phase]),
-                                         args5, sc.smem[phase], st);
+    for (const auto& sc : b->classes) {
+        cudaError_t e = launch_class_phase(b, sc, phase, sc.var[phase], parity, st);
         if (e != cudaSuccess) return e;
     }
     return cudaGetLastError();
@@ -272,6 +252,30 @@ cudaError_t launch_phase(cg_batch* b, int phase, int parity, cudaStream_t st) {
 cudaError_t enqueue_step(cg_batch* b, int parity, cudaStream_t st) {
     cudaError_t e = cudaSuccess;
     for (int p = 0; p < 4 && e == cudaSuccess; ++p) e = launch_phase(b, p, parity, st);
+    return e;
+}
+
+// One graph per ping-pong parity, (re)captured from the current variants.
+cudaError_t capture_batch_graphs(cg_batch* b) {
+    for (auto& g : b->graph)
+        if (g) {
+            cudaGraphExecDestroy(g);
+            g = nullptr;
+        }
+    cudaStream_t cap = nullptr;
+    cudaError_t e = cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking);
+    for (int p = 0; p < 2 && e == cudaSuccess; ++p) {
+        cudaGraph_t g = nullptr;
+        e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) {
+            cudaError_t le = enqueue_step(b, p, cap);
+            e = cudaStreamEndCapture(cap, &g);
+            if (le != cudaSuccess) e = le;
+        }
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&b->graph[p], g, 0);
+        if (g) cudaGraphDestroy(g);
+    }
+    if (cap) cudaStreamDestroy(cap);
     return e;
 }
 
@@ -405,46 +409,49 @@ int cg_batch_create(int n_worlds, const int* n, const int* C, const int* K, cons
     if (rc == CG_OK)
         chk(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device), "attr");
     for (int logn = kBatchMaxLogN; logn >= kBatchMinLogN && rc == CG_OK; --logn) {
-        std::vector<WorkItem> lists[4];
-        for (int w = 0; w < n_worlds; ++w) {
-            const auto& W = b->worlds[w];
-            if (W.logn != logn) continue;
-            const UnitGeo g = unit_geo_for(logn);
-            for (int c = 0; c < W.C; ++c)
-                for (int y0 = 0; y0 < W.n; y0 += g.RB) lists[0].push_back({w, c, y0, 0});
-            for (int c = 0; c < W.C; ++c)
-                if (W.groups.in_count[c] > 0)
-                    for (int x0 = 0; x0 < W.n / 2; x0 += g.TW) lists[1].push_back({w, c, x0, 0});
-            for (int c = 0; c < W.C; ++c)
-                for (int y0 = 0; y0 < W.n; y0 += g.RB) lists[2].push_back({w, c, y0, 0});
-            for (int c = 0; c < W.C; ++c)
-                for (int y0 = 0; y0 < W.n; y0 += g.TY)
-                    for (int x0 = 0; x0 < W.n; x0 += g.TX) lists[3].push_back({w, c, x0, y0});
-        }
-        if (lists[0].empty()) continue;
+        bool present = false;
+        for (const auto& W : b->worlds) present = present || W.logn == logn;
+        if (!present) continue;
         cg_batch::SizeClass sc;
         sc.logn = logn;
-        sc.fns = phase_fns_for(logn);
-        const PhaseSmem ps = phase_smem_for(logn);
-        const size_t smem[4] = {ps.r2c, ps.col, ps.c2r, ps.diff};
-        const int threads[4] = {512, 256, 512, kDiffThreads};
-        for (int p = 0; p < 4 && rc == CG_OK; ++p) {
-            sc.count[p] = int(lists[p].size());
-            sc.smem[p] = smem[p];
-            if (chk(cudaMalloc(&sc.d_items[p], sizeof(WorkItem) * std::max<size_t>(1, lists[p].size())),
-                    "cudaMalloc(items)"))
-                chk(cudaMemcpy(sc.d_items[p], lists[p].data(), sizeof(WorkItem) * lists[p].size(),
-                               cudaMemcpyHostToDevice),
-                    "uploading work lists");
-            chk(cudaFuncSetAttribute(sc.fns.fn[p], cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     int(smem[p])),
-                "cudaFuncSetAttribute");
-            int per_sm = 0;
-            chk(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sc.fns.fn[p], threads[p],
-                                                              smem[p]),
-                "occupancy");
-            sc.grid[p] = std::max(1, std::min(per_sm * sms, std::max(1, sc.count[p])));
-        }
+        phase_variants_for(logn, sc.pv);
+        for (int p = 0; p < 4 && rc == CG_OK; ++p)
+            for (int v = 0; v < kVariants && rc == CG_OK; ++v) {
+                const PhaseVariant& pv = sc.pv[p][v];
+                std::vector<WorkItem> list;
+                for (int w = 0; w < n_worlds; ++w) {
+                    const auto& W = b->worlds[w];
+                    if (W.logn != logn) continue;
+                    for (int c = 0; c < W.C; ++c) {
+                        if (p == 0 || p == 2) {
+                            for (int y0 = 0; y0 < W.n; y0 += pv.unit_a) list.push_back({w, c, y0, 0});
+                        } else if (p == 1) {
+                            if (W.groups.in_count[c] > 0)
+                                for (int x0 = 0; x0 < W.n / 2; x0 += pv.unit_a)
+                                    list.push_back({w, c, x0, 0});
+                        } else {
+                            for (int y0 = 0; y0 < W.n; y0 += pv.unit_b)
+                                for (int x0 = 0; x0 < W.n; x0 += pv.unit_a)
+                                    list.push_back({w, c, x0, y0});
+                        }
+                    }
+                }
+                sc.count[p][v] = int(list.size());
+                if (chk(cudaMalloc(&sc.d_items[p][v],
+                                   sizeof(WorkItem) * std::max<size_t>(1, list.size())),
+                        "cudaMalloc(items)"))
+                    chk(cudaMemcpy(sc.d_items[p][v], list.data(), sizeof(WorkItem) * list.size(),
+                                   cudaMemcpyHostToDevice),
+                        "uploading work lists");
+                chk(cudaFuncSetAttribute(pv.fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         int(pv.smem)),
+                    "cudaFuncSetAttribute");
+                int per_sm = 0;
+                chk(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pv.fn, pv.threads,
+                                                                  pv.smem),
+                    "occupancy");
+                sc.grid[p][v] = std::max(1, std::min(per_sm * sms, std::max(1, sc.count[p][v])));
+            }
         b->classes.push_back(sc);
     }
     if (rc == CG_OK) chk(cudaMalloc(&b->err, sizeof(int)), "cudaMalloc(err)");
@@ -454,25 +461,7 @@ int cg_batch_create(int n_worlds, const int* n, const int* C, const int* K, cons
         chk(cudaMalloc(&b->mass_partial, sizeof(double) * kMaxC * kMassBlocks), "cudaMalloc(mass)");
     if (rc == CG_OK) chk(cudaMalloc(&b->mass_out, sizeof(double) * kMaxC), "cudaMalloc(mass)");
     for (int i = 0; i < 5 && rc == CG_OK; ++i) chk(cudaEventCreate(&b->ev[i]), "cudaEventCreate");
-    // graphs
-    if (rc == CG_OK) {
-        cudaStream_t cap;
-        if (chk(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking), "cudaStreamCreate")) {
-            for (int p = 0; p < 2 && rc == CG_OK; ++p) {
-                cudaGraph_t g = nullptr;
-                cudaError_t e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
-                if (e == cudaSuccess) {
-                    cudaError_t le = enqueue_step(b, p, cap);
-                    e = cudaStreamEndCapture(cap, &g);
-                    if (le != cudaSuccess) e = le;
-                }
-                if (e == cudaSuccess) e = cudaGraphInstantiate(&b->graph[p], g, 0);
-                if (g) cudaGraphDestroy(g);
-                chk(e, "capturing the batched step graph");
-            }
-            cudaStreamDestroy(cap);
-        }
-    }
+    if (rc == CG_OK) chk(capture_batch_graphs(b), "capturing the batched step graph");
     if (rc == CG_OK) chk(cudaStreamSynchronize(b->stream), "cudaStreamSynchronize");
     if (rc != CG_OK) {
         batch_release(b);
@@ -605,12 +594,56 @@ int cg_batch_info(cg_batch* b, int* items4, int* grid4) {
     for (int p = 0; p < 4; ++p) {
         int items = 0, grid = 0;
         for (auto& sc : b->classes) {
-            items += sc.count[p];
-            grid = std::max(grid, sc.grid[p]);
+            items += sc.count[p][sc.var[p]];
+            grid = std::max(grid, sc.grid[p][sc.var[p]]);
         }
         if (items4) items4[p] = items;
         if (grid4) grid4[p] = grid;
     }
+    return CG_OK;
+}
+
+int cg_batch_autotune(cg_batch* b, int reps, int* chosen, double* ms_out) {
+    if (!b) return fail(CG_ERR_ARG, "cg_batch_autotune: NULL handle");
+    if (reps < 1 || reps > 1000)
+        return fail(CG_ERR_ARG, "cg_batch_autotune: reps %d outside [1, 1000]", reps);
+    BCHECK(cudaStreamSynchronize(b->stream), "cudaStreamSynchronize");
+    constexpr int kSizes = kBatchMaxLogN - kBatchMinLogN + 1;
+    if (chosen)
+        for (int i = 0; i < kSizes * 4; ++i) chosen[i] = -1;
+    if (ms_out)
+        for (int i = 0; i < kSizes * 4 * kVariants; ++i) ms_out[i] = 0.0;
+    // Each phase of a size class reads the state or the scratch the previous
+    // phases wrote; run in order on the live batch, the state is untouched
+    // (diffusion writes the spare ping-pong buffer only).
+    for (auto& sc : b->classes) {
+        const int slot = sc.logn - kBatchMinLogN;
+        for (int p = 0; p < 4; ++p) {
+            double t[kVariants];
+            int best = 0;
+            for (int v = 0; v < kVariants; ++v) {
+                for (int q = 0; q < p; ++q)
+                    BCHECK(launch_class_phase(b, sc, q, sc.var[q], b->cur, b->stream),
+                           "autotune prologue");
+                BCHECK(launch_class_phase(b, sc, p, v, b->cur, b->stream), "autotune warm-up");
+                BCHECK(cudaEventRecord(b->ev[0], b->stream), "cudaEventRecord");
+                for (int r = 0; r < reps; ++r)
+                    BCHECK(launch_class_phase(b, sc, p, v, b->cur, b->stream), "autotune launch");
+                BCHECK(cudaEventRecord(b->ev[1], b->stream), "cudaEventRecord");
+                BCHECK(cudaEventSynchronize(b->ev[1]), "cudaEventSynchronize");
+                float f = 0.f;
+                BCHECK(cudaEventElapsedTime(&f, b->ev[0], b->ev[1]), "cudaEventElapsedTime");
+                t[v] = double(f) / reps;
+                if (t[v] < t[best]) best = v;
+                if (ms_out) ms_out[(slot * 4 + p) * kVariants + v] = t[v];
+            }
+            sc.var[p] = best;
+            if (chosen) chosen[slot * 4 + p] = best;
+        }
+    }
+    int rc = batch_sync_check(b);
+    if (rc != CG_OK) return rc;
+    BCHECK(capture_batch_graphs(b), "re-capturing the batched step graph");
     return CG_OK;
 }
 

@@ -449,3 +449,15 @@ class GpuMaceLeniaBatch:
         grid = (ctypes.c_int * 4)()
         check(self._lib.cg_batch_info(self._h, items, grid))
         return list(items), list(grid)
+
+    def autotune(self, reps=5):
+        """Per grid side present: time every CTA-shape variant of every phase
+        and keep the fastest.  Returns {side: (chosen[4], ms[4][3])}."""
+        chosen = (ctypes.c_int * 24)()
+        ms = np.zeros(72, dtype=np.float64)
+        check(self._lib.cg_batch_autotune(self._h, int(reps), chosen, dptr(ms)))
+        out = {}
+        for i in range(6):
+            if chosen[4 * i] >= 0:
+                out[64 << i] = (list(chosen[4 * i:4 * i + 4]), ms[12 * i:12 * i + 12].reshape(4, 3))
+        return out

@@ -318,6 +318,14 @@ int cg_batch_stream(cg_batch* b, cg_stream_t* out);
  * NULL). */
 int cg_batch_info(cg_batch* b, int* items4, int* grid4);
 
+/* Autotuner of the batch: per grid side present and per phase, times the
+ * three CTA-shape variants (those of cg_autotune; all give the same bits) on
+ * the live batch without stepping it, keeps the fastest and re-captures the
+ * step graphs.  chosen[6*4] and ms[6*4*3] (either may be NULL) are indexed
+ * by grid side 64, 128, ..., 2048, then phase, then variant; sides the batch
+ * lacks give -1 and 0. */
+int cg_batch_autotune(cg_batch* b, int reps, int* chosen, double* ms);
+
 /* ---------------------------------------------------------------------------
  * Gradient-search helpers (the optimisation loop of train/, on the device).
  * Free functions on device arrays, enqueued on `stream` (NULL: the legacy

@@ -63,3 +63,21 @@ def test_batch_rejects_bad_world():
     cr = make_creature(32, 1, seed=1, radius=(2, 4), seed_box=16)
     with pytest.raises(CellaError, match="world 0"):
         GpuMaceLeniaBatch([cr])
+
+
+def test_batch_autotune_keeps_the_bits():
+    """The batch's autotuner picks per grid side among variants that compute
+    the same bits, and does not step the worlds."""
+    crs = mixed_creatures()
+    with GpuMaceLeniaBatch(crs) as a, GpuMaceLeniaBatch(crs) as b:
+        x0 = [b.state(i) for i in range(len(crs))]
+        tuned = b.autotune(reps=2)
+        assert sorted(tuned) == sorted({cr.n for cr in crs})
+        for side, (chosen, ms) in tuned.items():
+            assert all(0 <= v <= 2 for v in chosen) and ms.shape == (4, 3) and (ms > 0).all()
+        for i in range(len(crs)):
+            np.testing.assert_array_equal(b.state(i), x0[i])
+        a.run_steps(4)
+        b.run_steps(4)
+        for i in range(len(crs)):
+            np.testing.assert_array_equal(b.state(i), a.state(i), err_msg=f"world {i}")
