@@ -55,6 +55,12 @@ struct Geo {
     static constexpr int TW = (V == 1) ? (TW1 > 1 ? TW1 / 2 : 1)
                                        : (V == 2 ? (2 * TW1 > M ? M : 2 * TW1) : TW1);
     static constexpr int CT = (V == 1) ? 128 : (V == 2 ? 512 : 256);
+    // Resident CTAs per SM the compiler must allow for (the register cap) in
+    // the single-world kernels: the small-CTA variant asks for more where
+    // ptxas meets it without spills (inverse row pass at n >= 1024: 80
+    // registers; column pass: 96 at n = 2048).
+    static constexpr int C2R_MINB = (V == 1 && LOGN >= 10) ? 3 : 512 / RT;
+    static constexpr int COL_MINB = (V == 1) ? 5 : 512 / CT;
     static constexpr int CP = padded_len(N) + 1;
     // the staging tile is a bulk-copy (TMA) destination: 16-byte aligned
     static constexpr int KSOFF = (TW * CP + 1) & ~1;
@@ -280,7 +286,7 @@ __device__ __forceinline__ void init_tile_barrier(uint64_t* bar) {
 }
 
 template <int LOGN, int V = 0>
-__global__ void __launch_bounds__(Geo<LOGN, V>::CT, 512 / Geo<LOGN, V>::CT)
+__global__ void __launch_bounds__(Geo<LOGN, V>::CT, Geo<LOGN, V>::COL_MINB)
     k_col_conv(const float2* __restrict__ rowspec, const float2* __restrict__ kspec,
                float2* __restrict__ U, const float2* __restrict__ tw,
                const __grid_constant__ KernelGroups groups, int* err, int cbase) {
@@ -400,7 +406,7 @@ __device__ __forceinline__ void row_c2r_growth_body(const float2* __restrict__ U
 }
 
 template <int LOGN, int V = 0>
-__global__ void __launch_bounds__(Geo<LOGN, V>::RT, 512 / Geo<LOGN, V>::RT) k_row_c2r_growth(const float2* __restrict__ U,
+__global__ void __launch_bounds__(Geo<LOGN, V>::RT, Geo<LOGN, V>::C2R_MINB) k_row_c2r_growth(const float2* __restrict__ U,
                                                          float* __restrict__ A,
                                                          const float2* __restrict__ tw,
                                                          const __grid_constant__ KernelGroups groups,
