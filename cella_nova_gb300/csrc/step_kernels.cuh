@@ -56,10 +56,10 @@ struct Geo {
                                        : (V == 2 ? (2 * TW1 > M ? M : 2 * TW1) : TW1);
     static constexpr int CT = (V == 1) ? 128 : (V == 2 ? 512 : 256);
     // Resident CTAs per SM the compiler must allow for (the register cap) in
-    // the single-world kernels: the small-CTA variant asks for more where
-    // ptxas meets it without spills (inverse row pass at n >= 1024: 80
-    // registers; column pass: 96 at n = 2048).
-    static constexpr int C2R_MINB = (V == 1 && LOGN >= 10) ? 3 : 512 / RT;
+    // the single-world column pass: the small-CTA variant asks for five, which
+    // ptxas meets without spills (96 registers at n = 2048; 66.0 against
+    // 67.6 us).  The same for the inverse row pass (three CTAs, 80 registers)
+    // ran slower, 121 against 92 us, so that pass keeps its 128.
     static constexpr int COL_MINB = (V == 1) ? 5 : 512 / CT;
     static constexpr int CP = padded_len(N) + 1;
     // the staging tile is a bulk-copy (TMA) destination: 16-byte aligned
@@ -406,7 +406,7 @@ __device__ __forceinline__ void row_c2r_growth_body(const float2* __restrict__ U
 }
 
 template <int LOGN, int V = 0>
-__global__ void __launch_bounds__(Geo<LOGN, V>::RT, Geo<LOGN, V>::C2R_MINB) k_row_c2r_growth(const float2* __restrict__ U,
+__global__ void __launch_bounds__(Geo<LOGN, V>::RT, 512 / Geo<LOGN, V>::RT) k_row_c2r_growth(const float2* __restrict__ U,
                                                          float* __restrict__ A,
                                                          const float2* __restrict__ tw,
                                                          const __grid_constant__ KernelGroups groups,
