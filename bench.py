@@ -176,6 +176,20 @@ def cpu_baseline(cr, budget_s=20.0, nthreads=None):
                       f"f32 C port of example.rs (FFT per kernel), OpenMP, best {t:.2f} s/step"}
 
 
+def step_error_vs_fp64(sim, cr):
+    """Checker beside the CPU baseline: one GPU step from the GPU's current
+    state against the FP64 oracle's step from the same state (numpy FP64
+    twin of example.rs), max-abs over the whole 2048^2 grid."""
+    from oracle import oracle as O
+    x = sim.state()
+    sim.iterate()
+    y = sim.state()
+    ref, _, _ = O.step_np(x.astype(np.float64), cr.kspec.astype(np.complex128), cr.c0, cr.c1,
+                          cr.mu.astype(np.float64), cr.sigma.astype(np.float64),
+                          cr.weights.astype(np.float64), cr.temp)
+    return float(np.abs(y - ref).max())
+
+
 def run_reference(args):
     # rank 0 alone times the CPU reference; the other ranks exit without work
     # (and without joining a process group)
@@ -248,6 +262,7 @@ def run_ours(args):
     sampler = ClockSampler(local)
     sampler.start()
 
+    mass0 = sim.mass_f64()
     # warm-up, then K timed graph launches between barriers + syncs
     sim.run_steps(max(args.warmup, 3))
     sim.synchronize()
@@ -267,6 +282,10 @@ def run_ours(args):
     ms = max_over_ranks(ms_local, dist, world)
     clocks = sampler.summary(t_wall0, t_wall1)
 
+    mass1 = sim.mass_f64()
+    drift = {"steps": max(args.warmup, 3) + args.steps,
+             "max_rel": float(np.abs(mass1 / mass0 - 1).max()), "reduction": "FP64 on the GPU"}
+
     # per-kernel device time with events between kernels (same stream)
     prof_steps = min(max(args.steps, 8), 256)
     kms = sim.profile_kernels(prof_steps)
@@ -280,9 +299,10 @@ def run_ours(args):
         e2e = e2e_run(sim, cr, args, dist, world)
     sampler.stop()
 
-    cpu = None
+    cpu = step_err = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(cr)
+        step_err = step_error_vs_fp64(sim, cr)
 
     peak, peak_kind = peaks()
     bpp = bytes_per_px(C_CH, K_KER)
@@ -313,9 +333,13 @@ def run_ours(args):
         "gpu_launches": 4 * C_CH * args.steps,
         "clocks": clocks,
         "autotune": tuned,
+        "mass_drift": drift,
     }
     if cpu is not None:
         line["cpu_baseline"] = cpu
+        line["step_error_vs_fp64"] = {"max_abs": step_err, "bar": 1e-5,
+                                      "how": "one step from the GPU state after the timed run, "
+                                             "against the FP64 oracle from the same state"}
     if rank == 0:
         print(json.dumps(line), flush=True)
     sim.close()

@@ -204,3 +204,13 @@ def test_variants_bit_identical_and_autotune(n):
         assert sim.variants() == chosen
         sim.run_steps(3)
         np.testing.assert_array_equal(sim.state(), ref)
+
+
+def test_maximum_channels_and_kernels():
+    """The largest world the ABI accepts in channels and kernels: C = 16,
+    K = 64 (each channel feeds four kernels, outputs spread over all 16)."""
+    C, K = 16, 64
+    c0 = np.arange(K) % C
+    c1 = (np.arange(K) * 5 + 3) % C
+    cr = make_creature(32, C, seed=33, c0=c0, c1=c1, radius=(2, 6), seed_box=16)
+    check_steps(cr, steps=2)
