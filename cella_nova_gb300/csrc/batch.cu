@@ -98,7 +98,7 @@ __global__ void __launch_bounds__(Geo<LOGN, V>::RT, 512 / Geo<LOGN, V>::RT)
 }
 
 template <int LOGN, int V>
-__global__ void __launch_bounds__(DiffGeo2<LOGN, V>::THREADS)
+__global__ void __launch_bounds__(DiffTile<LOGN, V>::THREADS)
     kb_diffusion(const WorldDesc* __restrict__ worlds, const WorkItem* __restrict__ items,
                  int count, int parity) {
     extern __shared__ __align__(128) float smb_diff[];
@@ -106,8 +106,8 @@ __global__ void __launch_bounds__(DiffGeo2<LOGN, V>::THREADS)
         __syncthreads();
         const WorkItem it = items[i];
         const WorldDesc& w = worlds[it.world];
-        diffusion2_body<LOGN, V>(w.A, w.state[parity], w.state[parity ^ 1], it.c, it.a, it.b,
-                                 smb_diff, nullptr, 0);
+        diffusion_tile<LOGN, V>(w.A, w.state[parity], w.state[parity ^ 1], it.c, it.a, it.b,
+                                smb_diff, nullptr, 0);
     }
 }
 
@@ -125,7 +125,7 @@ struct PhaseVariant {
 template <int LOGN, int V>
 void fill_variant(PhaseVariant (&pv)[4][kVariants]) {
     using G = Geo<LOGN, V>;
-    using D = DiffGeo2<LOGN, V>;
+    using D = DiffTile<LOGN, V>;
     pv[0][V] = {reinterpret_cast<const void*>(kb_row_r2c<LOGN, V>), G::RT, G::R2C_SMEM, G::RB, 0};
     pv[1][V] = {reinterpret_cast<const void*>(kb_col_conv<LOGN, V>), G::CT, G::COL_SMEM, G::TW, 0};
     pv[2][V] = {reinterpret_cast<const void*>(kb_row_c2r_growth<LOGN, V>), G::RT, G::C2R_SMEM,

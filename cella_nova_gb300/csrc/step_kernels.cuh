@@ -567,13 +567,187 @@ __device__ __forceinline__ void diffusion2_body(const float* __restrict__ A,
     }
 }
 
+// The same arithmetic with two adjacent columns per thread: four consecutive
+// values (two 8-byte shared loads) give the horizontal 3-sums of both, so
+// the shared-memory pipe sees a third of the loads.  Output threads own 4
+// rows of a column pair; Z threads ZR rows of a halo-column pair.
 template <int LOGN, int V = 0>
-__global__ void __launch_bounds__(DiffGeo2<LOGN, V>::THREADS)
+struct DiffGeoPair {
+    using G = Geo<LOGN, V>;
+    static constexpr int N = G::N, TX = G::TX, TY = G::TY;
+    static constexpr int AS = TX + 8, AH = TY + 4, QH = TY + 2, QS = TX + 4;
+    static constexpr int OG = TX / 2;                   // output column pairs
+    static constexpr int ZG = (TX + 2 + 1) / 2;         // halo column pairs
+    static constexpr int OR = 4;                        // output rows per thread
+    static constexpr int THREADS = ((OG * (TY / OR) + 31) / 32) * 32;
+    static constexpr int NSZ = THREADS / ZG;            // Z row segments
+    static constexpr int ZR = (QH + NSZ - 1) / NSZ;     // Z rows per segment, at most
+    static constexpr int V4 = AS / 4;
+    static constexpr int LR = THREADS / V4;
+    static constexpr int SWEEPS = (AH + LR - 1) / LR;
+    static constexpr size_t SMEM = size_t(2 * AH * AS + QH * QS) * sizeof(float);
+    static_assert(TY % OR == 0 && TX % 4 == 0 && NSZ >= 1 && LR >= 1, "tile shape");
+    static_assert(2 * ZG + 4 <= AS && 2 * ZG <= QS, "pairs stay inside the tiles");
+};
+
+template <int LOGN, int V = 0>
+__device__ __forceinline__ void diffusion_pair_body(const float* __restrict__ A,
+                                                    const float* __restrict__ x,
+                                                    float* __restrict__ out, int c, int x0,
+                                                    int y0, float* smf, unsigned char* render,
+                                                    int nch) {
+    using D = DiffGeoPair<LOGN, V>;
+    constexpr int N = D::N, AS = D::AS, AH = D::AH, QH = D::QH, QS = D::QS;
+    constexpr int MASK = N * N - 1;
+    float* sAh = smf;                  // [AH][AS]: row a <-> y0 + a - 2, column j <-> x0 - 4 + j
+    float* sAl = smf + AH * AS;
+    float* sQ = smf + 2 * AH * AS;     // [QH][QS]: row b <-> y0 + b - 1, column q <-> x0 - 1 + q
+    const float* Ac = A + size_t(c) * N * N;
+    const float* xc = x + size_t(c) * N * N;
+    const int t = threadIdx.x;
+
+    const int zu = t % D::ZG, zs = t / D::ZG;
+    const int zr0 = zs * D::ZR;
+    const int zn = zs < D::NSZ ? min(D::ZR, QH - zr0) : 0;
+    float xv[D::ZR][2];
+    if (zn > 0) {
+        const float* xa = xc + ((x0 + 2 * zu - 1) & (N - 1));
+        const float* xb = xc + ((x0 + 2 * zu) & (N - 1));
+        const int base = (y0 + zr0 - 1) * N;
+#pragma unroll
+        for (int i = 0; i < D::ZR; ++i) {
+            if (i < zn) {
+                const int o = (base + i * N) & MASK;
+                xv[i][0] = __ldg(xa + o);
+                xv[i][1] = __ldg(xb + o);
+            }
+        }
+    }
+    if (t < D::LR * D::V4) {
+        const int v = t % D::V4, r0 = t / D::V4;
+        const float* acol = Ac + ((x0 - 4 + 4 * v) & (N - 1));
+        const int base = (y0 + r0 - 2) * N;
+        float4 av[D::SWEEPS];
+#pragma unroll
+        for (int i = 0; i < D::SWEEPS; ++i)
+            if (r0 + i * D::LR < AH)
+                av[i] = __ldg(reinterpret_cast<const float4*>(acol + ((base + i * D::LR * N) & MASK)));
+#pragma unroll
+        for (int i = 0; i < D::SWEEPS; ++i) {
+            if (r0 + i * D::LR < AH) {
+                const float4 a = av[i];
+                const float4 h = make_float4(head12(a.x), head12(a.y), head12(a.z), head12(a.w));
+                const int o = (r0 + i * D::LR) * AS + 4 * v;
+                *reinterpret_cast<float4*>(sAh + o) = h;
+                *reinterpret_cast<float4*>(sAl + o) =
+                    make_float4(a.x - h.x, a.y - h.y, a.z - h.z, a.w - h.w);
+            }
+        }
+    }
+    __syncthreads();
+
+    // o[m] = (p[m] + p[m+1]) + p[m+2], m < 2, from two 8-byte loads
+    auto sum3x2 = [](const float* p, float& o0, float& o1) {
+        const float2 a = *reinterpret_cast<const float2*>(p);
+        const float2 b = *reinterpret_cast<const float2*>(p + 2);
+        o0 = a.x + a.y + b.x;
+        o1 = a.y + b.x + b.y;
+    };
+    if (zn > 0) {
+        const float* ph = sAh + zr0 * AS + 2 * zu + 2;   // A columns x0 - 2 + 2 zu ..
+        const float* pl = sAl + zr0 * AS + 2 * zu + 2;
+        float* pq = sQ + zr0 * QS + 2 * zu;
+        float h0[2], l0[2], h1[2], l1[2];
+        sum3x2(ph, h0[0], h0[1]);
+        sum3x2(pl, l0[0], l0[1]);
+        sum3x2(ph + AS, h1[0], h1[1]);
+        sum3x2(pl + AS, l1[0], l1[1]);
+#pragma unroll
+        for (int i = 0; i < D::ZR; ++i) {
+            if (i >= zn) break;
+            float h2[2], l2[2], q[2];
+            sum3x2(ph + (i + 2) * AS, h2[0], h2[1]);
+            sum3x2(pl + (i + 2) * AS, l2[0], l2[1]);
+#pragma unroll
+            for (int m = 0; m < 2; ++m) {
+                const float zh = h0[m] + h1[m] + h2[m];
+                const float zt = l0[m] + l1[m] + l2[m];
+                const float z = zh + zt;
+                const float zl = zt - (z - zh);
+                const float rz = rcp_approx(z);
+                const float q0 = xv[i][m] * rz;
+                const float rem = fmaf(-q0, z, xv[i][m]);
+                q[m] = fmaf(rem - q0 * zl, rz, q0);
+                h0[m] = h1[m];
+                l0[m] = l1[m];
+                h1[m] = h2[m];
+                l1[m] = l2[m];
+            }
+            *reinterpret_cast<float2*>(pq + i * QS) = make_float2(q[0], q[1]);
+        }
+    }
+    __syncthreads();
+
+    const int ou = t % D::OG, os = t / D::OG;
+    if (os < D::TY / D::OR) {
+        const int r0 = os * D::OR;
+        const float* pq = sQ + r0 * QS + 2 * ou;
+        const float* pa = sAh + (r0 + 2) * AS + 2 * ou + 4;
+        const float* pb = sAl + (r0 + 2) * AS + 2 * ou + 4;
+        const int p0 = (y0 + r0) * N + x0 + 2 * ou;
+        float* oc = out + size_t(c) * N * N + p0;
+        const bool draw = render != nullptr && c < 3;
+        float s0[2], s1[2];
+        sum3x2(pq, s0[0], s0[1]);
+        sum3x2(pq + QS, s1[0], s1[1]);
+#pragma unroll
+        for (int i = 0; i < D::OR; ++i) {
+            float s2[2];
+            sum3x2(pq + (i + 2) * QS, s2[0], s2[1]);
+            const float2 ah = *reinterpret_cast<const float2*>(pa + i * AS);
+            const float2 al = *reinterpret_cast<const float2*>(pb + i * AS);
+            const float2 v = make_float2((ah.x + al.x) * ((s0[0] + s1[0]) + s2[0]),
+                                         (ah.y + al.y) * ((s0[1] + s1[1]) + s2[1]));
+            *reinterpret_cast<float2*>(oc + i * N) = v;
+            if (draw) {
+                const size_t p = size_t(p0 + i * N);
+                render_store(render, nch, c, p, v.x);
+                render_store(render, nch, c, p + 1, v.y);
+            }
+            s0[0] = s1[0];
+            s0[1] = s1[1];
+            s1[0] = s2[0];
+            s1[1] = s2[1];
+        }
+    }
+}
+
+// Variant 2 of the diffusion phase is the column-pair body.
+template <int LOGN, int V>
+struct DiffTile {
+    static constexpr bool PAIR = (V == 2);
+    static constexpr int THREADS = PAIR ? DiffGeoPair<LOGN, V>::THREADS : DiffGeo2<LOGN, V>::THREADS;
+    static constexpr size_t SMEM = PAIR ? DiffGeoPair<LOGN, V>::SMEM : DiffGeo2<LOGN, V>::SMEM;
+};
+
+template <int LOGN, int V>
+__device__ __forceinline__ void diffusion_tile(const float* __restrict__ A,
+                                               const float* __restrict__ x,
+                                               float* __restrict__ out, int c, int x0, int y0,
+                                               float* smf, unsigned char* render, int nch) {
+    if constexpr (DiffTile<LOGN, V>::PAIR)
+        diffusion_pair_body<LOGN, V>(A, x, out, c, x0, y0, smf, render, nch);
+    else
+        diffusion2_body<LOGN, V>(A, x, out, c, x0, y0, smf, render, nch);
+}
+
+template <int LOGN, int V = 0>
+__global__ void __launch_bounds__(DiffTile<LOGN, V>::THREADS)
     k_diffusion(const float* __restrict__ A, const float* __restrict__ x, float* __restrict__ out,
                 int cbase, unsigned char* __restrict__ render, int nch) {
     extern __shared__ __align__(128) float sm_diff[];
-    diffusion2_body<LOGN, V>(A, x, out, blockIdx.z + cbase, blockIdx.x * Geo<LOGN, V>::TX,
-                             blockIdx.y * Geo<LOGN, V>::TY, sm_diff, render, nch);
+    diffusion_tile<LOGN, V>(A, x, out, blockIdx.z + cbase, blockIdx.x * Geo<LOGN, V>::TX,
+                            blockIdx.y * Geo<LOGN, V>::TY, sm_diff, render, nch);
 }
 
 // ---------------------------------------------------------------------------
@@ -619,7 +793,7 @@ cudaError_t prepare_variant() {
         return e;
     if ((e = cudaFuncSetAttribute(k_diffusion<LOGN, V>,
                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  int(DiffGeo2<LOGN, V>::SMEM))) != cudaSuccess)
+                                  int(DiffTile<LOGN, V>::SMEM))) != cudaSuccess)
         return e;
     return cudaFuncSetAttribute(k_col_conv<LOGN, V>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 int(G::COL_SMEM));
@@ -656,7 +830,7 @@ void launch_c2r(const StepArgs& a, int c_lo, int nc, cudaStream_t st) {
 template <int LOGN, int V>
 void launch_diff(const StepArgs& a, int c_lo, int nc, cudaStream_t st) {
     using G = Geo<LOGN, V>;
-    using D = DiffGeo2<LOGN, V>;
+    using D = DiffTile<LOGN, V>;
     k_diffusion<LOGN, V><<<dim3(G::N / G::TX, G::N / G::TY, nc), D::THREADS, D::SMEM, st>>>(
         a.A, a.x_in, a.x_out, c_lo, a.render, a.C);
 }
