@@ -42,7 +42,7 @@ typedef enum {
     CG_ERR_TIMEOUT = -4,     /* a bounded device wait gave up */
     CG_ERR_IO = -5,          /* file could not be read or written */
     CG_ERR_FORMAT = -6,      /* file contents do not match the format */
-    CG_ERR_UNSUPPORTED = -7  /* valid request this build does not serve */
+    CG_ERR_UNSUPPORTED = -7  /* valid request this library does not serve */
 } cg_status;
 
 typedef struct cg_sim cg_sim;

@@ -18,7 +18,7 @@
  * (ml-rs/orchestrator/convolution.rs:689, shaders/compute_1024.wgsl:313-319).
  *
  * Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg may use
- * this code, and only as the checker.
+ * this code, and only to check results or to time the CPU baseline.
  */
 
 #define CAT2(a, b) a##b
