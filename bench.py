@@ -586,7 +586,9 @@ def run_search(args):
     sampler.start()
     gs = GradientSearch(crs, tgs, T=T, every=every, adam=adam, n_streams=4)
     warm = max(args.warmup, 3)
-    gs.run(warm)                      # the first iteration eager, then capture + replays
+    gs.run(1)                         # the first iteration eagerly (allocates scratch)
+    loss_first = float(np.mean(gs.losses()))
+    gs.run(warm - 1)                  # capture, then replays
     torch.cuda.synchronize()
     barrier(dist, world)
     iters = max(1, args.steps)
@@ -670,6 +672,8 @@ def run_search(args):
                               f"{plain_cands} candidates timed and scaled to {ncand}"},
         "batched_over_plain": plain_ms / ms,
         "loss_mean": float(np.mean(losses)),
+        "loss_mean_first_iteration": loss_first,
+        "iterations_total": warm + iters,
         "mass_drift_max": drift,
         # per candidate and iteration: builder 4, parameter fold 1, forward 4
         # per step, MSE 2, backward 8 per step, segment recompute 4 per step
