@@ -19,6 +19,9 @@
 #include <string>
 #include <vector>
 
+#include <errno.h>
+#include <unistd.h>
+
 #include "cella_gpu.h"
 #include "cella_internal.h"
 #include "fft.cuh"
@@ -185,6 +188,8 @@ struct cg_sim {
     cudaGraphExec_t graph8[2] = {nullptr, nullptr};    // kStepsPerGraph steps, per parity
     cudaGraphExec_t graphR[2] = {nullptr, nullptr};    // one step that also renders
     unsigned* render = nullptr;   // [n][n] packed 0x00RRGGBB
+    unsigned char* frames[2] = {nullptr, nullptr};   // pinned RGB24 frames (frame streaming)
+    cudaEvent_t frame_ev[2] = {nullptr, nullptr};
     double* ring_partial = nullptr;   // kernel builder: K * kRingBlocks * kMaxRings
     double* ring_s = nullptr;         // K * kMaxRings per-ring sums of the last build
     double* zsum = nullptr;           // K normalisers of the last build
@@ -247,6 +252,10 @@ void release(cg_sim* s) {
     cudaFree(s->err);
     cudaFree(s->dparams);
     cudaFree(s->render);
+    for (auto& f : s->frames)
+        if (f) cudaFreeHost(f);
+    for (auto& e : s->frame_ev)
+        if (e) cudaEventDestroy(e);
     cudaFree(s->ring_partial);
     cudaFree(s->ring_s);
     cudaFree(s->zsum);
@@ -623,6 +632,63 @@ int cg_render(cg_sim* s) {
     if (!s) return fail(CG_ERR_ARG, "cg_render: NULL handle");
     CG_CHECK(launch_render(s->state[s->cur], s->C, s->px(), s->render, s->stream),
              "launching render");
+    return CG_OK;
+}
+
+// Write all of buf to fd (a file or a pipe), retrying short writes.
+static bool write_all(int fd, const unsigned char* buf, size_t bytes) {
+    while (bytes > 0) {
+        const ssize_t w = ::write(fd, buf, bytes);
+        if (w < 0) {
+            if (errno == EINTR) continue;
+            return false;
+        }
+        buf += w;
+        bytes -= size_t(w);
+    }
+    return true;
+}
+
+int cg_stream_frames(cg_sim* s, int fd, int nframes, int steps_per_frame) {
+    if (!s) return fail(CG_ERR_ARG, "cg_stream_frames: NULL handle");
+    if (fd < 0 || nframes < 0 || steps_per_frame < 1)
+        return fail(CG_ERR_ARG, "cg_stream_frames: fd %d, %d frames, %d steps per frame", fd,
+                    nframes, steps_per_frame);
+    const size_t bytes = 3 * s->px();
+    for (int i = 0; i < 2; ++i) {
+        if (!s->frames[i])
+            CG_CHECK(cudaMallocHost(reinterpret_cast<void**>(&s->frames[i]), bytes),
+                     "cudaMallocHost(frames)");
+        if (!s->frame_ev[i])
+            CG_CHECK(cudaEventCreateWithFlags(&s->frame_ev[i], cudaEventDisableTiming),
+                     "cudaEventCreate");
+    }
+    auto* dev_rgb = static_cast<unsigned char*>(s->staging);   // 8 B per pixel, 3 used
+    // Frame f is enqueued (its steps, the render epilogue, the RGB24
+    // conversion and the copy into host buffer f % 2) before frame f - 1 is
+    // written out, so the GPU computes while the host writes.
+    for (int f = 0; f <= nframes; ++f) {
+        if (f < nframes) {
+            int rc = cg_step(s, steps_per_frame - 1);
+            if (rc == CG_OK) rc = cg_iterate_and_render(s);
+            if (rc != CG_OK) return rc;
+            CG_CHECK(launch_rgb24(s->render, dev_rgb, s->px(), s->stream), "launching RGB24");
+            CG_CHECK(cudaMemcpyAsync(s->frames[f & 1], dev_rgb, bytes, cudaMemcpyDeviceToHost,
+                                     s->stream),
+                     "downloading a frame");
+            CG_CHECK(cudaEventRecord(s->frame_ev[f & 1], s->stream), "cudaEventRecord");
+        }
+        if (f > 0) {
+            const int b = (f - 1) & 1;
+            CG_CHECK(cudaEventSynchronize(s->frame_ev[b]), "cudaEventSynchronize");
+            if (!write_all(fd, s->frames[b], bytes)) {
+                cudaStreamSynchronize(s->stream);
+                return fail(CG_ERR_IO, "writing frame %d to fd %d failed (errno %d)", f - 1, fd,
+                            errno);
+            }
+        }
+    }
+    CG_SYNC_CHECK(s);
     return CG_OK;
 }
 

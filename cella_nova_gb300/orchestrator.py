@@ -168,6 +168,12 @@ class GpuMaceLenia:
         check(self._lib.cg_download_render_packed(self._h, uptr(out)))
         return out.reshape(self.n, self.n)
 
+    def stream_frames(self, fd: int, nframes: int, steps_per_frame: int = 1):
+        """Write nframes RGB24 frames (each after steps_per_frame steps) to the
+        file descriptor fd, computing each frame while the previous one is
+        written (main.rs:239-303's loop, to a file or a pipe)."""
+        check(self._lib.cg_stream_frames(self._h, int(fd), int(nframes), int(steps_per_frame)))
+
     def render_ptr(self) -> int:
         """Device address of the render buffer (n*n uint32)."""
         p = ctypes.c_void_p()

@@ -115,6 +115,14 @@ int cg_render(cg_sim* sim);
  * until the first render. */
 int cg_download_render(cg_sim* sim, uint8_t* rgb24);
 
+/* Frame streaming (the video loop of main.rs:239-303 without ffmpeg): nframes
+ * frames, each steps_per_frame steps of which the last renders, written as
+ * RGB24 (3*n*n bytes per frame, the bytes main.rs pipes to ffmpeg) to the
+ * file descriptor fd (a file, or the write end of a pipe to an encoder).
+ * Each frame is computed and copied while the previous one is written.
+ * Blocking; CG_ERR_IO if a write fails. */
+int cg_stream_frames(cg_sim* sim, int fd, int nframes, int steps_per_frame);
+
 /* The packed render words themselves (n*n uint32_t), blocking. */
 int cg_download_render_packed(cg_sim* sim, uint32_t* out);
 

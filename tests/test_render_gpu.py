@@ -80,3 +80,37 @@ def test_set_params_device_equals_host_folding():
         a.run_steps(5)
         b.run_steps(5)
         np.testing.assert_array_equal(a.state(), b.state())
+
+
+def test_stream_frames_to_a_file_and_a_pipe(tmp_path):
+    """Frame streaming writes exactly the frames the iterate_and_render +
+    download_render loop of main.rs produces, to a file or through a pipe."""
+    import os
+    import threading
+    n, frames, spf = 64, 5, 2
+    cr = make_creature(n, 3, seed=21, radius=(4, 12), seed_box=32)
+    with GpuMaceLenia.from_creature(cr) as a, GpuMaceLenia.from_creature(cr) as b, \
+            GpuMaceLenia.from_creature(cr) as c:
+        path = tmp_path / "frames.rgb"
+        with open(path, "wb") as f:
+            a.stream_frames(f.fileno(), frames, steps_per_frame=spf)
+        raw = np.fromfile(path, np.uint8).reshape(frames, n, n, 3)
+        for i in range(frames):
+            b.run_steps(spf - 1)
+            b.iterate_and_render()
+            np.testing.assert_array_equal(raw[i], b.download_render(), err_msg=f"frame {i}")
+        np.testing.assert_array_equal(a.state(), b.state())
+        # the same through a pipe, read by another thread (as an encoder would)
+        rfd, wfd = os.pipe()
+        got = []
+
+        def reader():
+            with os.fdopen(rfd, "rb") as r:
+                got.append(r.read())
+
+        th = threading.Thread(target=reader)
+        th.start()
+        c.stream_frames(wfd, frames, steps_per_frame=spf)
+        os.close(wfd)
+        th.join(timeout=60)
+        np.testing.assert_array_equal(np.frombuffer(got[0], np.uint8).reshape(frames, n, n, 3), raw)
