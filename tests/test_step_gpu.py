@@ -214,3 +214,19 @@ def test_maximum_channels_and_kernels():
     c1 = (np.arange(K) * 5 + 3) % C
     cr = make_creature(32, C, seed=33, c0=c0, c1=c1, radius=(2, 6), seed_box=16)
     check_steps(cr, steps=2)
+
+
+@pytest.mark.parametrize("trial", range(6))
+def test_random_worlds(trial):
+    """Seeded random worlds: grid side, channel and kernel counts and the
+    c0/c1 maps drawn at random (repeated and unused channels included)."""
+    rng = np.random.default_rng(1000 + trial)
+    n = int(rng.choice([16, 32, 64, 128]))
+    C = int(rng.integers(1, 7))
+    K = int(rng.integers(1, 13))
+    c0 = rng.integers(0, C, K)
+    c1 = rng.integers(0, C, K)
+    cr = make_creature(n, C, seed=2000 + trial, c0=c0, c1=c1,
+                       radius=(max(2.0, n / 16), max(3.0, n / 5)), seed_box=n // 2,
+                       temp=float(rng.uniform(0.5, 2.0)))
+    check_steps(cr, steps=2)
