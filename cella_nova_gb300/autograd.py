@@ -4,9 +4,14 @@
 steps on the GPU (cg_unroll, checkpoints every ``every`` steps) and its
 backward runs the adjoint kernels (cg_unroll_backward, each segment recomputed
 from its checkpoint), returning gradients for the seed, mu, sigma, the growth
-weights and the spatial kernels h (K, n, n).  Gradients for ring weights (or
-any other kernel parametrisation) follow from h by ordinary torch autograd,
-e.g. through :class:`RingKernelBuilder`.
+weights and the spatial kernels h (K, n, n).  Gradients for any kernel
+parametrisation follow from h by ordinary torch autograd, e.g. through
+:class:`RingKernelBuilder`.
+
+``unroll_rings(world, specs, seed, mu, sigma, weights, rings, T, every)`` does
+the same for Lenia ring kernels given by their ring weights: the kernels are
+built on the GPU (cg_build_ring_kernels) and the ring-weight gradients come
+from cg_ring_weight_grad, so no step of the loop runs torch compute.
 
 This is the differentiable form of train/diff_lenia_org.py's
 ``DiffusionLenia.step`` (the reference differentiates it with torch
@@ -62,6 +67,17 @@ class LeniaWorld:
             self.close()
         except Exception:
             pass
+
+    def load_rings(self, specs, rings: torch.Tensor, params: torch.Tensor):
+        """Device-side parameters: params = [mu | sigma | weights] (3K f32) and
+        ring weights rings (K, 8) f32, both on the world's stream; the kernel
+        spectra are built on the GPU."""
+        p = params.data_ptr()
+        K = self.K
+        check(self.lib.cg_set_params_device(self.h, ctypes.c_void_p(p), ctypes.c_void_p(p + 4 * K),
+                                            ctypes.c_void_p(p + 8 * K)))
+        check(self.lib.cg_build_ring_kernels(self.h, ctypes.cast(specs, ctypes.c_void_p),
+                                             _p(rings)))
 
     def load(self, mu, sigma, weights, spec):
         """Growth parameters (host arrays) and kernel spectra (K, n, n, 2) f32
@@ -127,6 +143,56 @@ def unroll(world: LeniaWorld, seed, mu, sigma, weights, h, T: int, every: int = 
     return _Unroll.apply(world, T, every, seed, mu, sigma, weights, h)
 
 
+class _UnrollRings(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, world, T, every, specs, seed, mu, sigma, weights, rings):
+        lib = world.lib
+        params = torch.cat([mu.detach(), sigma.detach(), weights.detach()]).float().contiguous()
+        rw = rings.detach().float().contiguous()
+        world.load_rings(specs, rw, params)
+        x0 = seed.detach().float().contiguous()
+        nck = (T - 1) // every + 1
+        ckpt = torch.empty((nck,) + tuple(x0.shape), dtype=torch.float32, device=x0.device)
+        xT = torch.empty_like(x0)
+        check(lib.cg_unroll(world.h, _p(x0), int(T), int(every), _p(ckpt), _p(xT)))
+        ctx.world, ctx.T, ctx.every, ctx.specs = world, int(T), int(every), specs
+        ctx.dtypes = (seed.dtype, mu.dtype, sigma.dtype, weights.dtype, rings.dtype)
+        ctx.save_for_backward(ckpt, params, rw)
+        return xT
+
+    @staticmethod
+    def backward(ctx, gT):
+        world = ctx.world
+        lib = world.lib
+        ckpt, params, rw = ctx.saved_tensors
+        world.load_rings(ctx.specs, rw, params)   # another unroll may have run since
+        gT = gT.contiguous().float()
+        g0 = torch.empty_like(gT)
+        gtmp = torch.empty_like(gT)
+        seg = torch.empty((ctx.every,) + tuple(gT.shape), dtype=torch.float32, device=gT.device)
+        K, n = world.K, world.n
+        pgrad = torch.zeros(3 * K, dtype=torch.float64, device=gT.device)
+        kgrad = torch.zeros((K, n // 2, n, 2), dtype=torch.float32, device=gT.device)
+        check(lib.cg_unroll_backward(world.h, _p(ckpt), ctx.T, ctx.every, _p(gT), _p(g0),
+                                     _p(pgrad), _p(kgrad), _p(seg), _p(gtmp)))
+        hbar = torch.empty((K, n, n), dtype=torch.float32, device=gT.device)
+        check(lib.cg_kernel_grad_spatial(world.h, _p(kgrad), _p(hbar)))
+        grings = torch.zeros_like(rw)
+        check(lib.cg_ring_weight_grad(world.h, ctypes.cast(ctx.specs, ctypes.c_void_p), _p(rw),
+                                      _p(hbar), _p(grings)))
+        ds, dm, dsg, dw, dr = ctx.dtypes
+        return (None, None, None, None, g0.to(ds), pgrad[:K].to(dm), pgrad[K:2 * K].to(dsg),
+                pgrad[2 * K:].to(dw), grings.to(dr))
+
+
+def unroll_rings(world: LeniaWorld, specs, seed, mu, sigma, weights, rings, T: int,
+                 every: int = 8):
+    """x_T after T steps with Lenia ring kernels built on the GPU from their
+    ring weights rings (K, 8); differentiable in seed, mu, sigma, weights and
+    rings.  specs: the kernels' cg_ring_spec array (ring_spec_array)."""
+    return _UnrollRings.apply(world, T, every, specs, seed, mu, sigma, weights, rings)
+
+
 class RingKernelBuilder(torch.nn.Module):
     """Lenia ring kernels h_k = sum_l b_kl S_kl / sum(...) (the construction of
     cella_nova_gb300/creature.py) as differentiable torch ops; the shells
@@ -169,10 +235,19 @@ class DiffusionLeniaGPU(torch.nn.Module):
              for b in cr.ring_weights])
         self.builder = RingKernelBuilder(cr.n, cr.ring_radius, [len(b) for b in cr.ring_weights],
                                          device=device)
+        from .orchestrator import creature_ring_specs, ring_spec_array
+        self.specs = ring_spec_array(creature_ring_specs(cr)[0])
 
     def kernels(self):
+        """The spatial kernels (K, n, n) as differentiable torch ops (float64)."""
         return self.builder(list(self.ring_weights))
 
+    def rings(self):
+        """Ring weights padded to (K, 8), differentiable."""
+        return torch.stack([torch.nn.functional.pad(b, (0, _abi.MAX_RINGS - b.numel()))
+                            for b in self.ring_weights])
+
     def forward(self, T: int, every: int = 8):
-        h = self.kernels()
-        return unroll(self.world, self.seed, self.mu, self.sigma, self.weights, h, T, every)
+        """x_T; the kernels are built on the GPU from the ring weights."""
+        return unroll_rings(self.world, self.specs, self.seed, self.mu, self.sigma, self.weights,
+                            self.rings(), T, every)

@@ -81,14 +81,46 @@ def test_unroll_gradients_match_fp64(n, C, T, every):
 
 
 def test_unroll_forward_equals_graph_steps():
+    """The differentiable unroll (kernels built on the GPU from the ring
+    weights, parameters folded on the device) steps exactly like the graph
+    path with the same kernels."""
+    from cella_nova_gb300.orchestrator import creature_ring_specs
     cr = make_creature(128, 3, seed=60, radius=(8, 20), seed_box=64)
-    h = torch.tensor(spatial_kernels(cr), device="cuda")
-    spec = kernel_spectra(h).cpu().numpy()
-    cr.kspec = spec[..., 0] + 1j * spec[..., 1]
-    with GpuMaceLenia.from_creature(cr) as sim:
-        sim.run_steps(7)
-        ref = sim.state()
     m = DiffusionLeniaGPU(cr)
     with torch.no_grad():
         xT = m(7, 3)
+    specs, w = creature_ring_specs(cr)
+    wd = torch.tensor(w, device="cuda")
+    torch.cuda.synchronize()
+    with GpuMaceLenia.from_creature(cr) as sim:
+        sim.build_ring_kernels(specs, wd.data_ptr())
+        sim.run_steps(7)
+        ref = sim.state()
     np.testing.assert_array_equal(xT.cpu().numpy(), ref)
+
+
+def test_unroll_with_spatial_kernels_matches_fp64():
+    """The kernel-agnostic path: spatial kernels h as a tensor (here the
+    ring kernels, spectra taken by torch), gradients against FP64 autograd."""
+    from cella_nova_gb300.autograd import unroll
+    n, C, T, every = 64, 2, 6, 4
+    cr = make_creature(n, C, seed=77, radius=(4, 12), seed_box=32)
+    target = AR.shifted_target(cr.seed)
+    h64 = spatial_kernels(cr)
+    ref = AR.gradients(cr, T, target, kspec=np.fft.fft2(h64))
+    dev = torch.device("cuda")
+    f32 = dict(dtype=torch.float32, device=dev)
+    seed = torch.tensor(cr.seed, **f32, requires_grad=True)
+    mu = torch.tensor(cr.mu, **f32, requires_grad=True)
+    sg = torch.tensor(cr.sigma, **f32, requires_grad=True)
+    ww = torch.tensor(cr.weights, **f32, requires_grad=True)
+    h = torch.tensor(h64, device=dev, requires_grad=True)
+    w = LeniaWorld(cr.n, cr.C, cr.c0, cr.c1, cr.temp)
+    xT = unroll(w, seed, mu, sg, ww, h, T, every)
+    loss = torch.mean((xT - torch.tensor(target, **f32)) ** 2)
+    loss.backward()
+    errs = {"seed": rel(seed.grad.cpu(), ref["seed"]), "mu": rel(mu.grad.cpu(), ref["mu"]),
+            "sigma": rel(sg.grad.cpu(), ref["sigma"]), "weights": rel(ww.grad.cpu(), ref["weights"])}
+    assert h.grad is not None and h.grad.shape == h.shape
+    assert max(errs.values()) < 2e-3, errs
+    w.close()
