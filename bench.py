@@ -546,10 +546,11 @@ def run_grad(args):
                    "step_unit": "one forward+backward iteration of the unroll"},
         "forward_ms": f_ms, "backward_ms": b_ms,
         "forward_cell_updates_per_s": n * n * T / (f_ms / 1e3),
-        # forward 4 per step; backward per step 3 recomputed phases + 5 adjoint
-        # kernels; each segment re-runs its steps but the first; 2 final
-        # kernel-gradient launches
-        "gpu_launches": T * 4 + T * 8 + (T - (T + every - 1) // every) * 4 + 2,
+        # forward 4 per step; the backward re-runs each segment (4 per step,
+        # 3 for a segment's last) and runs 5 adjoint kernels per step; kernel
+        # build 4 + parameter fold 1 in each direction; 2 final kernel-gradient
+        # and 2 ring-gradient launches
+        "gpu_launches": 13 * T - (T + every - 1) // every + 14,
         "loss": float(loss.detach()),
     }
     if rank == 0:
@@ -676,10 +677,10 @@ def run_search(args):
         "iterations_total": warm + iters,
         "mass_drift_max": drift,
         # per candidate and iteration: builder 4, parameter fold 1, forward 4
-        # per step, MSE 2, backward 8 per step, segment recompute 4 per step
-        # but each segment's first, kernel gradient 2, ring gradient 2, Adam 3;
-        # plus the step counter once per iteration
-        "gpu_launches": iters * (ncand * (14 + 16 * T - 4 * ((T + every - 1) // every)) + 1),
+        # per step, MSE 2, segment recompute 4 per step (3 for a segment's
+        # last), backward 5 per step, kernel gradient 2, ring gradient 2, Adam
+        # 3; plus the step counter once per iteration
+        "gpu_launches": iters * (ncand * (13 * T - (T + every - 1) // every + 14) + 1),
         "clocks": clocks,
         "setup_s": {"generate": gen_s},
     }

@@ -461,8 +461,10 @@ cudaError_t launch_backward(const BwdArgs& a, cudaStream_t st) {
     f.err = a.err;
     f.groups = a.groups;
     f.gp = a.gp;
-    cudaError_t e = launch_step<LOGN>(f, kPhaseRowFwd | kPhaseColConv | kPhaseGrowth, st);
-    if (e != cudaSuccess) return e;
+    if (a.recompute) {
+        const cudaError_t e = launch_step<LOGN>(f, kPhaseRowFwd | kPhaseColConv | kPhaseGrowth, st);
+        if (e != cudaSuccess) return e;
+    }
     k_diffusion_bwd<LOGN><<<dim3(G::N / G::TX, G::N / G::TY, a.C), 256, DiffBwdGeo<LOGN>::SMEM,
                             st>>>(a.A, a.x, a.ybar, a.xbar, a.abar, a.temp);
     k_growth_bwd<LOGN><<<dim3(G::N / G::RB, a.K), G::RT, G::R2C_SMEM, st>>>(a.U, a.abar, a.tw,

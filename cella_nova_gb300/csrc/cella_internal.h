@@ -92,6 +92,9 @@ struct BwdArgs {
     KernelGroups groups;
     const GrowthParams* gp;   // device-resident
     const AdjointParams* ap;  // device-resident
+    // true: recompute the row spectra, U and A of x first; false: rowspec, U
+    // and A already hold them (a cached forward step)
+    bool recompute;
 };
 
 // Ring-kernel descriptors for the on-GPU kernel builder (kernels_common.cu).

@@ -201,6 +201,10 @@ struct cg_sim {
     Variants var{};
     float* abar = nullptr;          // backward scratch, allocated on first use
     float* utmp[2] = {nullptr, nullptr};   // cg_unroll scratch states
+    // cg_unroll_backward: each segment step's row spectra, U and A, kept from
+    // the segment's recompute for its backward step (cache_steps of them)
+    void* seg_cache = nullptr;
+    int cache_steps = 0;
     bool bwd_ready = false;
 
     size_t px() const { return size_t(n) * n; }
@@ -260,6 +264,7 @@ void release(cg_sim* s) {
     cudaFree(s->ring_s);
     cudaFree(s->zsum);
     cudaFree(s->abar);
+    cudaFree(s->seg_cache);
     cudaFree(s->utmp[0]);
     cudaFree(s->utmp[1]);
     if (s->own_stream && s->stream) cudaStreamDestroy(s->stream);
@@ -436,6 +441,7 @@ BwdArgs bwd_args(cg_sim* s, const float* x, const float* ybar, float* xbar, doub
     a.groups = s->groups;
     a.gp = &s->dparams->gp;
     a.ap = &s->dparams->ap;
+    a.recompute = true;
     return a;
 }
 
@@ -995,8 +1001,29 @@ int cg_unroll_backward(cg_sim* s, const float* ckpt, int T, int every, const flo
     if (!s || !ckpt || !gT || !g0 || !pgrad || !seg || !gtmp)
         return fail(CG_ERR_ARG, "cg_unroll_backward: NULL argument");
     if (T < 1 || every < 1) return fail(CG_ERR_ARG, "cg_unroll_backward: T=%d, every=%d", T, every);
+    int rc = ensure_backward(s);
+    if (rc != CG_OK) return rc;
     const size_t bytes = sizeof(float) * s->C * s->px();
     const size_t plane = size_t(s->C) * s->px();
+    const size_t half = size_t(s->n / 2) * s->n;
+    // per cached step: row spectra (C half planes), U (K half planes), A
+    const size_t spec_elems = size_t(s->C) * half, u_elems = size_t(s->K) * half;
+    const size_t step_bytes = sizeof(float2) * (spec_elems + u_elems) + bytes;
+    const int span = std::min(every, T);
+    if (s->cache_steps < span) {
+        cudaFree(s->seg_cache);
+        s->seg_cache = nullptr;
+        s->cache_steps = 0;
+        CG_CHECK(cudaMalloc(&s->seg_cache, step_bytes * size_t(span)),
+                 "cudaMalloc(segment cache)");
+        s->cache_steps = span;
+    }
+    auto slot = [&](int i, float2** rowspec, float2** U, float** A) {
+        char* base = static_cast<char*>(s->seg_cache) + step_bytes * size_t(i);
+        *rowspec = reinterpret_cast<float2*>(base);
+        *U = *rowspec + spec_elems;
+        *A = reinterpret_cast<float*>(*U + u_elems);
+    };
     // gradient ping-pong between g0 and gtmp, arranged to end in g0
     float* gb[2] = {(T % 2 == 0) ? g0 : gtmp, (T % 2 == 0) ? gtmp : g0};
     CG_CHECK(cudaMemcpyAsync(gb[0], gT, bytes, cudaMemcpyDeviceToDevice, s->stream), "gradient");
@@ -1004,18 +1031,28 @@ int cg_unroll_backward(cg_sim* s, const float* ckpt, int T, int every, const flo
     const int nseg = (T + every - 1) / every;
     for (int j = nseg - 1; j >= 0; --j) {
         const int t0 = j * every, t1 = std::min(T, t0 + every);
-        // recompute x_{t0} .. x_{t1-1} into seg
+        // recompute x_{t0} .. x_{t1-1} into seg, keeping each step's row
+        // spectra, U and A for its backward step (the last step needs no
+        // diffusion)
         CG_CHECK(cudaMemcpyAsync(seg, ckpt + plane * size_t(j), bytes, cudaMemcpyDeviceToDevice,
                                  s->stream),
                  "segment");
-        for (int t = t0; t + 1 < t1; ++t) {
-            int rc = cg_step_from(s, seg + plane * size_t(t - t0), seg + plane * size_t(t - t0 + 1));
-            if (rc != CG_OK) return rc;
+        for (int t = t0; t < t1; ++t) {
+            StepArgs a = s->args(s->cur, nullptr);
+            slot(t - t0, &a.rowspec, &a.U, &a.A);
+            a.x_in = seg + plane * size_t(t - t0);
+            const bool last = t + 1 == t1;
+            a.x_out = last ? nullptr : seg + plane * size_t(t - t0 + 1);
+            CG_CHECK(s->ops->step(a, last ? (kPhaseRowFwd | kPhaseColConv | kPhaseGrowth) : kPhaseAll,
+                                  s->stream),
+                     "recomputing a segment");
         }
         for (int t = t1 - 1; t >= t0; --t) {
-            int rc = cg_step_backward(s, seg + plane * size_t(t - t0), gb[which], gb[which ^ 1],
-                                      pgrad, kgrad);
-            if (rc != CG_OK) return rc;
+            BwdArgs b = bwd_args(s, seg + plane * size_t(t - t0), gb[which], gb[which ^ 1], pgrad,
+                                 reinterpret_cast<float2*>(kgrad));
+            slot(t - t0, &b.rowspec, &b.U, &b.A);
+            b.recompute = false;
+            CG_CHECK(s->ops->backward(b, s->stream), "launching a backward step");
             which ^= 1;
         }
     }
