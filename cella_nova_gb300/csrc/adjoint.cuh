@@ -5,9 +5,9 @@
 //   u_k = h_k (*) x_{c0[k]},  e_k = exp(-(u_k-mu_k)^2 / (2 sigma_k^2)),
 //   a_c = sum_{c1[k]=c} w_k (2 e_k - 1),  A = exp(temp a),
 //   Z = box(A),  q = x / Z,  P = box(q),  x' = A P.
-// Given ybar = dL/dx', one backward step is five launches:
-//   1. forward recompute of the row spectra, U and A for this x (the step's
-//      own kernels; A and U are not kept from the forward pass),
+// Given ybar = dL/dx', one backward step is four launches, after
+//   1. the row spectra, U and A of this x: recomputed by the step's own
+//      kernels, or (cg_unroll_backward) kept from the segment's recompute,
 //   2. k_diffusion_bwd: qbar = box(ybar A), xbar = qbar / Z,
 //      Zbar = -qbar q / Z, Abar = ybar P + box(Zbar), abar = temp A Abar,
 //   3. k_growth_bwd: u from U by the inverse row FFT; ebar = 2 w abar,
@@ -18,11 +18,12 @@
 //   4. k_col_conv_adj: the adjoint of a convolution with h is a convolution
 //      with h(-m), whose spectrum is conj(K): per input channel, the sum over
 //      its kernels of colFFT(ubar_k) conj(K_k), then one inverse column FFT,
-//      written over the row spectra,
+//      written over the row spectra.  With a kernel-gradient buffer it also
+//      accumulates sum_t colFFT(ubar_k) conj(colFFT(x_c0k)) = 4 FFT2(hbar_k)
+//      (packed like U) from the same column transforms, from which k_col_inv
+//      and k_row_c2r_add (scale 1/(4 n^2)) give the spatial kernel gradient
+//      hbar_k = ubar (*) x(-.),
 //   5. k_row_c2r_add: the inverse row FFT of that, added to xbar.
-// Optionally k_kgrad accumulates sum_t colFFT(ubar_k) conj(colFFT(x_c0k))
-// = 4 FFT2(hbar_k) (packed like U), from which k_col_inv and k_row_c2r_add
-// (scale 1/(4 n^2)) give the spatial kernel gradient hbar_k = ubar (*) x(-.).
 #pragma once
 #include "step_kernels.cuh"
 
@@ -226,6 +227,7 @@ template <int LOGN>
 __device__ __forceinline__ bool col_conv_adj_body(float2* __restrict__ rowspec,
                                                   const float2* __restrict__ kspec,
                                                   const float2* __restrict__ U,
+                                                  float2* __restrict__ kgrad,
                                                   const float2* __restrict__ tw,
                                                   const KernelGroups& groups, int c, int kx0,
                                                   float2* sm, uint64_t* barp, uint32_t& phase,
@@ -234,6 +236,7 @@ __device__ __forceinline__ bool col_conv_adj_body(float2* __restrict__ rowspec,
     constexpr int N = G::N, M = G::M, TW = G::TW, T = G::CT;
     float2* W = sm;
     float2* KS = sm + G::KSOFF;
+    float2* Wx = KS + TW * N;   // with kgrad: colFFT of this channel's row spectra
     uint64_t& bar = *barp;
     const int cnt = groups.in_count[c], base = groups.in_start[c];
     float2* dst = rowspec + (size_t(c) * M + kx0) * N;
@@ -266,6 +269,12 @@ __device__ __forceinline__ bool col_conv_adj_body(float2* __restrict__ rowspec,
     };
     auto ld_in = [&](int s, int i, int, int) { return KS[s * N + i]; };
     SmemRows wrows{W, G::CP};
+    if (kgrad) {   // X = colFFT(row spectra of x), read before dst is overwritten
+        issue(dst);
+        if (!wait_tile()) return false;
+        SmemRows xrows{Wx, G::CP};
+        FftPasses<N, 1, false, T, TW, false>::run(ld_in, xrows, xrows, xrows, tw + G::TW_COL_FWD);
+    }
 
     for (int gi = 0; gi < cnt; ++gi) {
         const int k = groups.in_idx[base + gi];
@@ -276,6 +285,7 @@ __device__ __forceinline__ bool col_conv_adj_body(float2* __restrict__ rowspec,
                                              [&]() { issue(ktile); });
         if (!wait_tile()) return false;
         const float2* kb = kspec + (size_t(k) * (M + 1) + M) * N;
+        float2* kg = kgrad ? kgrad + (size_t(k) * M + kx0) * N : nullptr;
 #pragma unroll
         for (int it = 0; it < IPTL; ++it) {
             const int item = threadIdx.x + it * T;
@@ -286,11 +296,35 @@ __device__ __forceinline__ bool col_conv_adj_body(float2* __restrict__ rowspec,
                     const int i = j + r * JL;
                     const float2 p = W[s * G::CP + pidx(i)];
                     float2 g = cmulc(p, KS[s * N + i]);
+                    float2 pm;
                     if (kx0 + s == 0) {
-                        const float2 pm = cconj(W[pidx((N - i) & (N - 1))]);
+                        pm = cconj(W[pidx((N - i) & (N - 1))]);
                         g = cadd(g, cmulc(pm, __ldg(&kb[i])));
                     }
                     acc[it][r] = cadd(acc[it][r], g);
+                    if (kg) {
+                        // kgrad_k += colFFT(ubar_k) conj(X); column 0 carries the
+                        // kx = 0 and kx = n/2 spectra (FA = (P + conj P(-)) / 2,
+                        // FB = (P - conj P(-)) / (2i)) and stores FA conj(XA) +
+                        // i FB conj(XB)
+                        const float2 px = Wx[s * G::CP + pidx(i)];
+                        float2 v;
+                        if (kx0 + s == 0) {
+                            const float2 pxm = cconj(Wx[pidx((N - i) & (N - 1))]);
+                            const float2 au = make_float2(0.5f * (p.x + pm.x), 0.5f * (p.y + pm.y));
+                            const float2 du = make_float2(0.5f * (p.x - pm.x), 0.5f * (p.y - pm.y));
+                            const float2 bu = make_float2(du.y, -du.x);
+                            const float2 ax = make_float2(0.5f * (px.x + pxm.x), 0.5f * (px.y + pxm.y));
+                            const float2 dx = make_float2(0.5f * (px.x - pxm.x), 0.5f * (px.y - pxm.y));
+                            const float2 bx = make_float2(dx.y, -dx.x);
+                            const float2 g0 = cmulc(au, ax), gm = cmulc(bu, bx);
+                            v = make_float2(g0.x - gm.y, g0.y + gm.x);   // g0 + i gm
+                        } else {
+                            v = cmulc(p, px);
+                        }
+                        float2* q = kg + size_t(s) * N + i;
+                        *q = cadd(*q, v);
+                    }
                 }
             }
         }
@@ -302,10 +336,19 @@ __device__ __forceinline__ bool col_conv_adj_body(float2* __restrict__ rowspec,
     return true;
 }
 
+// Shared memory of the adjoint column pass: the forward pass's W and
+// staging tile, then the row-spectrum transform X for the kernel gradient.
+template <int LOGN>
+struct AdjColGeo {
+    static constexpr size_t SMEM =
+        Geo<LOGN>::COL_SMEM + size_t(Geo<LOGN>::TW) * Geo<LOGN>::CP * sizeof(float2);
+};
+
 template <int LOGN>
 __global__ void __launch_bounds__(256, 2) k_col_conv_adj(float2* __restrict__ rowspec,
                                                           const float2* __restrict__ kspec,
                                                           const float2* __restrict__ U,
+                                                          float2* __restrict__ kgrad,
                                                           const float2* __restrict__ tw,
                                                           const __grid_constant__ KernelGroups groups,
                                                           int* err) {
@@ -313,7 +356,7 @@ __global__ void __launch_bounds__(256, 2) k_col_conv_adj(float2* __restrict__ ro
     __shared__ __align__(8) uint64_t bar;
     init_tile_barrier(&bar);
     uint32_t phase = 0;
-    col_conv_adj_body<LOGN>(rowspec, kspec, U, tw, groups, blockIdx.y,
+    col_conv_adj_body<LOGN>(rowspec, kspec, U, kgrad, tw, groups, blockIdx.y,
                             blockIdx.x * Geo<LOGN>::TW, sm_cadj, &bar, phase, err);
 }
 
@@ -344,67 +387,6 @@ __global__ void __launch_bounds__(512) k_row_c2r_add(const float2* __restrict__ 
     c2r_rows<LOGN>(sm_c2ra, tw, out);
 }
 
-// ---------------------------------------------------------------------------
-// Kernel gradient: per input channel c and TW columns, for every kernel k
-// with c0[k] == c: kgrad_k += colFFT(Ubar_k) conj(colFFT(X_c)), column 0
-// unpacked into its two real-row spectra and repacked.  grid (M/TW, C), CT.
-// ---------------------------------------------------------------------------
-template <int LOGN>
-struct KgradGeo {
-    static constexpr size_t SMEM =
-        (2 * size_t(Geo<LOGN>::TW) * Geo<LOGN>::CP) * sizeof(float2);
-};
-
-template <int LOGN>
-__global__ void __launch_bounds__(256) k_kgrad(const float2* __restrict__ rowspec,
-                                                const float2* __restrict__ U,
-                                                float2* __restrict__ kgrad,
-                                                const float2* __restrict__ tw,
-                                                const __grid_constant__ KernelGroups groups) {
-    using G = Geo<LOGN>;
-    constexpr int N = G::N, M = G::M, TW = G::TW, T = G::CT;
-    extern __shared__ __align__(128) float2 sm_kg[];
-    float2* Wx = sm_kg;
-    float2* Wu = sm_kg + TW * G::CP;
-    const int c = blockIdx.y, kx0 = blockIdx.x * TW;
-    const int cnt = groups.in_count[c], base = groups.in_start[c];
-    if (cnt == 0) return;
-    auto fwd = [&](const float2* src, float2* buf) {
-        auto ld = [&](int s, int i, int, int) { return __ldg(&src[size_t(s) * N + i]); };
-        SmemRows rows{buf, G::CP};
-        FftPasses<N, 1, false, T, TW, false>::run(ld, rows, rows, rows, tw + G::TW_COL_FWD);
-    };
-    fwd(rowspec + (size_t(c) * M + kx0) * N, Wx);
-    for (int gi = 0; gi < cnt; ++gi) {
-        const int k = groups.in_idx[base + gi];
-        fwd(U + (size_t(k) * M + kx0) * N, Wu);
-        float2* g = kgrad + (size_t(k) * M + kx0) * N;
-        for (int e = threadIdx.x; e < TW * N; e += T) {
-            const int s = e / N, i = e % N;
-            float2 v;
-            if (kx0 + s == 0) {
-                const int im = (N - i) & (N - 1);
-                const float2 pu = Wu[pidx(i)], pum = cconj(Wu[pidx(im)]);
-                const float2 px = Wx[pidx(i)], pxm = cconj(Wx[pidx(im)]);
-                // FA = (P + conj P(-)) / 2, FB = (P - conj P(-)) / (2i)
-                const float2 au = make_float2(0.5f * (pu.x + pum.x), 0.5f * (pu.y + pum.y));
-                const float2 du = make_float2(0.5f * (pu.x - pum.x), 0.5f * (pu.y - pum.y));
-                const float2 bu = make_float2(du.y, -du.x);
-                const float2 ax = make_float2(0.5f * (px.x + pxm.x), 0.5f * (px.y + pxm.y));
-                const float2 dx = make_float2(0.5f * (px.x - pxm.x), 0.5f * (px.y - pxm.y));
-                const float2 bx = make_float2(dx.y, -dx.x);
-                const float2 g0 = cmulc(au, ax), gm = cmulc(bu, bx);
-                v = make_float2(g0.x - gm.y, g0.y + gm.x);   // g0 + i gm
-            } else {
-                v = cmulc(Wu[s * G::CP + pidx(i)], Wx[s * G::CP + pidx(i)]);
-            }
-            const float2 old = g[size_t(s) * N + i];
-            g[size_t(s) * N + i] = cadd(old, v);
-        }
-        __syncthreads();
-    }
-}
-
 // Plain inverse column FFT of a kx-major [planes][M][N] spectrum, in place.
 // grid (M/TW, planes), CT.
 template <int LOGN>
@@ -427,16 +409,14 @@ template <int LOGN>
 cudaError_t prepare_backward() {
     using G = Geo<LOGN>;
     cudaError_t e;
-    const void* fns[6] = {reinterpret_cast<const void*>(k_diffusion_bwd<LOGN>),
+    const void* fns[5] = {reinterpret_cast<const void*>(k_diffusion_bwd<LOGN>),
                           reinterpret_cast<const void*>(k_growth_bwd<LOGN>),
                           reinterpret_cast<const void*>(k_col_conv_adj<LOGN>),
                           reinterpret_cast<const void*>(k_row_c2r_add<LOGN>),
-                          reinterpret_cast<const void*>(k_kgrad<LOGN>),
                           reinterpret_cast<const void*>(k_col_inv<LOGN>)};
-    const size_t smem[6] = {DiffBwdGeo<LOGN>::SMEM, G::R2C_SMEM,     G::COL_SMEM,
-                            G::R2C_SMEM,            KgradGeo<LOGN>::SMEM,
-                            size_t(G::TW) * G::CP * sizeof(float2)};
-    for (int i = 0; i < 6; ++i)
+    const size_t smem[5] = {DiffBwdGeo<LOGN>::SMEM, G::R2C_SMEM, AdjColGeo<LOGN>::SMEM,
+                            G::R2C_SMEM, size_t(G::TW) * G::CP * sizeof(float2)};
+    for (int i = 0; i < 5; ++i)
         if ((e = cudaFuncSetAttribute(fns[i], cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       int(smem[i]))) != cudaSuccess)
             return e;
@@ -469,11 +449,8 @@ cudaError_t launch_backward(const BwdArgs& a, cudaStream_t st) {
                             st>>>(a.A, a.x, a.ybar, a.xbar, a.abar, a.temp);
     k_growth_bwd<LOGN><<<dim3(G::N / G::RB, a.K), G::RT, G::R2C_SMEM, st>>>(a.U, a.abar, a.tw,
                                                                            a.ap, a.pgrad, a.K);
-    if (a.kgrad)
-        k_kgrad<LOGN><<<dim3(G::M / G::TW, a.C), G::CT, KgradGeo<LOGN>::SMEM, st>>>(
-            a.rowspec, a.U, a.kgrad, a.tw, a.groups);
-    k_col_conv_adj<LOGN><<<dim3(G::M / G::TW, a.C), G::CT, G::COL_SMEM, st>>>(
-        a.rowspec, a.kspec, a.U, a.tw, a.groups, a.err);
+    k_col_conv_adj<LOGN><<<dim3(G::M / G::TW, a.C), G::CT, AdjColGeo<LOGN>::SMEM, st>>>(
+        a.rowspec, a.kspec, a.U, a.kgrad, a.tw, a.groups, a.err);
     k_row_c2r_add<LOGN><<<dim3(G::N / G::RB, a.C), G::RT, G::R2C_SMEM, st>>>(a.rowspec, a.xbar,
                                                                             a.tw, 1.f, 1);
     return cudaGetLastError();
