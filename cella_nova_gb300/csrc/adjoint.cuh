@@ -33,22 +33,22 @@ namespace cg {
 // ---------------------------------------------------------------------------
 // 2. Diffusion backward (one channel tile per CTA, 256 threads).
 // ---------------------------------------------------------------------------
-template <int LOGN>
+template <int LOGN, int V = 0>
 struct DiffBwdGeo {
-    static constexpr int TX = Geo<LOGN>::TX, TY = Geo<LOGN>::TY;
+    static constexpr int TX = Geo<LOGN, V>::TX, TY = Geo<LOGN, V>::TY;
     static constexpr int AW = TX + 4, AH = TY + 4, HW = TX + 2, QH = TY + 2;
     static constexpr size_t SMEM = size_t(2 * AH * AW + 2 * QH * HW) * sizeof(float);
 };
 
-template <int LOGN>
+template <int LOGN, int V = 0>
 __device__ __forceinline__ void diffusion_bwd_body(const float* __restrict__ A,
                                                    const float* __restrict__ x,
                                                    const float* __restrict__ ybar,
                                                    float* __restrict__ xbar,
                                                    float* __restrict__ abar, float temp, int c,
                                                    int x0, int y0, float* smf) {
-    using D = DiffBwdGeo<LOGN>;
-    constexpr int N = Geo<LOGN>::N, TX = D::TX, TY = D::TY;
+    using D = DiffBwdGeo<LOGN, V>;
+    constexpr int N = Geo<LOGN, V>::N, TX = D::TX, TY = D::TY;
     constexpr int AW = D::AW, AH = D::AH, HW = D::HW, QH = D::QH;
     auto sA = reinterpret_cast<float (*)[AW]>(smf);
     auto sY = reinterpret_cast<float (*)[AW]>(smf + AH * AW);
@@ -97,22 +97,22 @@ __device__ __forceinline__ void diffusion_bwd_body(const float* __restrict__ A,
     }
 }
 
-template <int LOGN>
+template <int LOGN, int V = 0>
 __global__ void __launch_bounds__(256) k_diffusion_bwd(const float* __restrict__ A,
                                                         const float* __restrict__ x,
                                                         const float* __restrict__ ybar,
                                                         float* __restrict__ xbar,
                                                         float* __restrict__ abar, float temp) {
     extern __shared__ __align__(128) float sm_dbwd[];
-    diffusion_bwd_body<LOGN>(A, x, ybar, xbar, abar, temp, blockIdx.z, blockIdx.x * Geo<LOGN>::TX,
-                             blockIdx.y * Geo<LOGN>::TY, sm_dbwd);
+    diffusion_bwd_body<LOGN, V>(A, x, ybar, xbar, abar, temp, blockIdx.z, blockIdx.x * Geo<LOGN, V>::TX,
+                             blockIdx.y * Geo<LOGN, V>::TY, sm_dbwd);
 }
 
 // Gather RB rows of a kx-major spectrum (src[kx * N + s]) into the row
 // buffer (transposed) with per-element async copies; waits for them.
-template <int LOGN>
+template <int LOGN, int V = 0>
 __device__ __forceinline__ void gather_rows(const float2* __restrict__ src, float2* buf) {
-    using G = Geo<LOGN>;
+    using G = Geo<LOGN, V>;
     for (int item = threadIdx.x; item < G::RB * G::M; item += G::RT) {
         const int s = item % G::RB, kx = item / G::RB;
         cp_async8(&buf[s * G::RP + pidx(kx)], &src[size_t(kx) * G::N + s]);
@@ -124,9 +124,9 @@ __device__ __forceinline__ void gather_rows(const float2* __restrict__ src, floa
 
 // Inverse row FFT of RB packed rows in `buf`; `out(s, i, v)` receives the
 // pixel pair (x[2i], x[2i+1]) of row s.
-template <int LOGN, class OUT>
+template <int LOGN, int V, class OUT>
 __device__ __forceinline__ void c2r_rows(float2* buf, const float2* __restrict__ tw, OUT& out) {
-    using G = Geo<LOGN>;
+    using G = Geo<LOGN, V>;
     SmemRows rows{buf, G::RP};
     auto ld0 = [&](int s, int m, int, int) -> float2 {
         const float2* row = buf + s * G::RP;
@@ -160,16 +160,16 @@ __device__ __forceinline__ double block_sum(double v, double* red) {
 // 3. Growth backward, one kernel's RB rows per CTA (RT threads):
 //    U[k] rows -> u -> ubar -> forward row FFT -> written over U[k].
 // ---------------------------------------------------------------------------
-template <int LOGN>
+template <int LOGN, int V = 0>
 __device__ __forceinline__ void growth_bwd_body(float2* __restrict__ U,
                                                 const float* __restrict__ abar,
                                                 const float2* __restrict__ tw,
                                                 const AdjointParams& ap, int k, int cout, int y0,
                                                 double* __restrict__ pgrad, int K, float2* sm,
                                                 double* red) {
-    using G = Geo<LOGN>;
+    using G = Geo<LOGN, V>;
     float2* Uk = U + size_t(k) * G::M * G::N + y0;
-    gather_rows<LOGN>(Uk, sm);
+    gather_rows<LOGN, V>(Uk, sm);
     const float mu = ap.mu[k], w = ap.w[k], is2 = ap.inv_s2[k], is3 = ap.inv_s3[k];
     const float* ab = abar + (size_t(cout) * G::N + y0) * G::N;
     float pw = 0.f, pmu = 0.f, psg = 0.f;
@@ -190,10 +190,10 @@ __device__ __forceinline__ void growth_bwd_body(float2* __restrict__ U,
         }
         sm[s * G::RP + pidx(i)] = make_float2(ub[0], ub[1]);
     };
-    c2r_rows<LOGN>(sm, tw, out);
+    c2r_rows<LOGN, V>(sm, tw, out);
     SmemRows rows{sm, G::RP};
     FftPasses<G::M, 1, false, G::RT, G::RB>::run(rows, rows, rows, rows, tw + G::TW_ROW);
-    r2c_finish<LOGN>(sm, tw, Uk);
+    r2c_finish<LOGN, V>(sm, tw, Uk);
     const double sw = block_sum(double(pw), red);
     const double smu = block_sum(double(pmu), red);
     const double ssg = block_sum(double(psg), red);
@@ -204,8 +204,8 @@ __device__ __forceinline__ void growth_bwd_body(float2* __restrict__ U,
     }
 }
 
-template <int LOGN>
-__global__ void __launch_bounds__(512) k_growth_bwd(float2* __restrict__ U,
+template <int LOGN, int V = 0>
+__global__ void __launch_bounds__(Geo<LOGN, V>::RT, 512 / Geo<LOGN, V>::RT) k_growth_bwd(float2* __restrict__ U,
                                                      const float* __restrict__ abar,
                                                      const float2* __restrict__ tw,
                                                      const AdjointParams* __restrict__ app,
@@ -213,7 +213,7 @@ __global__ void __launch_bounds__(512) k_growth_bwd(float2* __restrict__ U,
     extern __shared__ __align__(128) float2 sm_gbwd[];
     __shared__ double red[16];
     const int k = blockIdx.y;
-    growth_bwd_body<LOGN>(U, abar, tw, *app, k, app->cout[k], blockIdx.x * Geo<LOGN>::RB, pgrad, K,
+    growth_bwd_body<LOGN, V>(U, abar, tw, *app, k, app->cout[k], blockIdx.x * Geo<LOGN, V>::RB, pgrad, K,
                           sm_gbwd, red);
 }
 
@@ -223,7 +223,7 @@ __global__ void __launch_bounds__(512) k_growth_bwd(float2* __restrict__ U,
 //    (column 0: P conj(alpha) + conj P(-ky) conj(beta)), then one inverse
 //    column FFT, written over the row spectra of c.
 // ---------------------------------------------------------------------------
-template <int LOGN>
+template <int LOGN, int V = 0>
 __device__ __forceinline__ bool col_conv_adj_body(float2* __restrict__ rowspec,
                                                   const float2* __restrict__ kspec,
                                                   const float2* __restrict__ U,
@@ -232,7 +232,7 @@ __device__ __forceinline__ bool col_conv_adj_body(float2* __restrict__ rowspec,
                                                   const KernelGroups& groups, int c, int kx0,
                                                   float2* sm, uint64_t* barp, uint32_t& phase,
                                                   int* err) {
-    using G = Geo<LOGN>;
+    using G = Geo<LOGN, V>;
     constexpr int N = G::N, M = G::M, TW = G::TW, T = G::CT;
     float2* W = sm;
     float2* KS = sm + G::KSOFF;
@@ -338,14 +338,14 @@ __device__ __forceinline__ bool col_conv_adj_body(float2* __restrict__ rowspec,
 
 // Shared memory of the adjoint column pass: the forward pass's W and
 // staging tile, then the row-spectrum transform X for the kernel gradient.
-template <int LOGN>
+template <int LOGN, int V = 0>
 struct AdjColGeo {
     static constexpr size_t SMEM =
-        Geo<LOGN>::COL_SMEM + size_t(Geo<LOGN>::TW) * Geo<LOGN>::CP * sizeof(float2);
+        Geo<LOGN, V>::COL_SMEM + size_t(Geo<LOGN, V>::TW) * Geo<LOGN, V>::CP * sizeof(float2);
 };
 
-template <int LOGN>
-__global__ void __launch_bounds__(256, 2) k_col_conv_adj(float2* __restrict__ rowspec,
+template <int LOGN, int V = 0>
+__global__ void __launch_bounds__(Geo<LOGN, V>::CT, 512 / Geo<LOGN, V>::CT) k_col_conv_adj(float2* __restrict__ rowspec,
                                                           const float2* __restrict__ kspec,
                                                           const float2* __restrict__ U,
                                                           float2* __restrict__ kgrad,
@@ -356,23 +356,23 @@ __global__ void __launch_bounds__(256, 2) k_col_conv_adj(float2* __restrict__ ro
     __shared__ __align__(8) uint64_t bar;
     init_tile_barrier(&bar);
     uint32_t phase = 0;
-    col_conv_adj_body<LOGN>(rowspec, kspec, U, kgrad, tw, groups, blockIdx.y,
-                            blockIdx.x * Geo<LOGN>::TW, sm_cadj, &bar, phase, err);
+    col_conv_adj_body<LOGN, V>(rowspec, kspec, U, kgrad, tw, groups, blockIdx.y,
+                            blockIdx.x * Geo<LOGN, V>::TW, sm_cadj, &bar, phase, err);
 }
 
 // ---------------------------------------------------------------------------
 // 5. Inverse row FFT of RB rows of a kx-major spectrum, scaled, written to
 //    (or added to) a real [C or K][n][n] array.  grid (N/RB, planes), RT.
 // ---------------------------------------------------------------------------
-template <int LOGN>
-__global__ void __launch_bounds__(512) k_row_c2r_add(const float2* __restrict__ src,
+template <int LOGN, int V = 0>
+__global__ void __launch_bounds__(Geo<LOGN, V>::RT, 512 / Geo<LOGN, V>::RT) k_row_c2r_add(const float2* __restrict__ src,
                                                       float* __restrict__ dst,
                                                       const float2* __restrict__ tw, float scale,
                                                       int accumulate) {
-    using G = Geo<LOGN>;
+    using G = Geo<LOGN, V>;
     extern __shared__ __align__(128) float2 sm_c2ra[];
     const int c = blockIdx.y, y0 = blockIdx.x * G::RB;
-    gather_rows<LOGN>(src + size_t(c) * G::M * G::N + y0, sm_c2ra);
+    gather_rows<LOGN, V>(src + size_t(c) * G::M * G::N + y0, sm_c2ra);
     float* d = dst + (size_t(c) * G::N + y0) * G::N;
     auto out = [&](int s, int i, float2 v) {
         float2* p = reinterpret_cast<float2*>(d + size_t(s) * G::N) + i;
@@ -384,15 +384,15 @@ __global__ void __launch_bounds__(512) k_row_c2r_add(const float2* __restrict__ 
         }
         *p = o;
     };
-    c2r_rows<LOGN>(sm_c2ra, tw, out);
+    c2r_rows<LOGN, V>(sm_c2ra, tw, out);
 }
 
 // Plain inverse column FFT of a kx-major [planes][M][N] spectrum, in place.
 // grid (M/TW, planes), CT.
-template <int LOGN>
-__global__ void __launch_bounds__(256) k_col_inv(float2* __restrict__ spec,
+template <int LOGN, int V = 0>
+__global__ void __launch_bounds__(Geo<LOGN, V>::CT) k_col_inv(float2* __restrict__ spec,
                                                   const float2* __restrict__ tw) {
-    using G = Geo<LOGN>;
+    using G = Geo<LOGN, V>;
     constexpr int N = G::N, M = G::M, TW = G::TW, T = G::CT;
     extern __shared__ __align__(128) float2 sm_ci[];
     float2* col = spec + (size_t(blockIdx.y) * M + blockIdx.x * TW) * N;
@@ -405,16 +405,16 @@ __global__ void __launch_bounds__(256) k_col_inv(float2* __restrict__ spec,
 // ---------------------------------------------------------------------------
 // Launchers.
 // ---------------------------------------------------------------------------
-template <int LOGN>
-cudaError_t prepare_backward() {
-    using G = Geo<LOGN>;
+template <int LOGN, int V>
+cudaError_t prepare_backward_variant() {
+    using G = Geo<LOGN, V>;
     cudaError_t e;
-    const void* fns[5] = {reinterpret_cast<const void*>(k_diffusion_bwd<LOGN>),
-                          reinterpret_cast<const void*>(k_growth_bwd<LOGN>),
-                          reinterpret_cast<const void*>(k_col_conv_adj<LOGN>),
-                          reinterpret_cast<const void*>(k_row_c2r_add<LOGN>),
-                          reinterpret_cast<const void*>(k_col_inv<LOGN>)};
-    const size_t smem[5] = {DiffBwdGeo<LOGN>::SMEM, G::R2C_SMEM, AdjColGeo<LOGN>::SMEM,
+    const void* fns[5] = {reinterpret_cast<const void*>(k_diffusion_bwd<LOGN, V>),
+                          reinterpret_cast<const void*>(k_growth_bwd<LOGN, V>),
+                          reinterpret_cast<const void*>(k_col_conv_adj<LOGN, V>),
+                          reinterpret_cast<const void*>(k_row_c2r_add<LOGN, V>),
+                          reinterpret_cast<const void*>(k_col_inv<LOGN, V>)};
+    const size_t smem[5] = {DiffBwdGeo<LOGN, V>::SMEM, G::R2C_SMEM, AdjColGeo<LOGN, V>::SMEM,
                             G::R2C_SMEM, size_t(G::TW) * G::CP * sizeof(float2)};
     for (int i = 0; i < 5; ++i)
         if ((e = cudaFuncSetAttribute(fns[i], cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -424,8 +424,45 @@ cudaError_t prepare_backward() {
 }
 
 template <int LOGN>
+cudaError_t prepare_backward() {
+    cudaError_t e = prepare_backward_variant<LOGN, 0>();
+    if (e == cudaSuccess) e = prepare_backward_variant<LOGN, 1>();
+    if (e == cudaSuccess) e = prepare_backward_variant<LOGN, 2>();
+    return e;
+}
+
+// The adjoint kernels take the CTA shapes of the forward phases they mirror
+// (the handle's tuned variants; all variants give the same bits): diffusion
+// for the diffusion adjoint, the inverse row pass for the growth adjoint and
+// the final row transform, the column pass for the adjoint column pass.
+template <int LOGN, int V>
+void launch_diff_bwd(const BwdArgs& a, cudaStream_t st) {
+    using G = Geo<LOGN, V>;
+    k_diffusion_bwd<LOGN, V><<<dim3(G::N / G::TX, G::N / G::TY, a.C), 256,
+                               DiffBwdGeo<LOGN, V>::SMEM, st>>>(a.A, a.x, a.ybar, a.xbar, a.abar,
+                                                                a.temp);
+}
+template <int LOGN, int V>
+void launch_growth_bwd(const BwdArgs& a, cudaStream_t st) {
+    using G = Geo<LOGN, V>;
+    k_growth_bwd<LOGN, V><<<dim3(G::N / G::RB, a.K), G::RT, G::R2C_SMEM, st>>>(a.U, a.abar, a.tw,
+                                                                              a.ap, a.pgrad, a.K);
+}
+template <int LOGN, int V>
+void launch_col_adj(const BwdArgs& a, cudaStream_t st) {
+    using G = Geo<LOGN, V>;
+    k_col_conv_adj<LOGN, V><<<dim3(G::M / G::TW, a.C), G::CT, AdjColGeo<LOGN, V>::SMEM, st>>>(
+        a.rowspec, a.kspec, a.U, a.kgrad, a.tw, a.groups, a.err);
+}
+template <int LOGN, int V>
+void launch_c2r_add(const BwdArgs& a, cudaStream_t st) {
+    using G = Geo<LOGN, V>;
+    k_row_c2r_add<LOGN, V><<<dim3(G::N / G::RB, a.C), G::RT, G::R2C_SMEM, st>>>(a.rowspec, a.xbar,
+                                                                               a.tw, 1.f, 1);
+}
+
+template <int LOGN>
 cudaError_t launch_backward(const BwdArgs& a, cudaStream_t st) {
-    using G = Geo<LOGN>;
     StepArgs f{};
     f.C = a.C;
     f.K = a.K;
@@ -441,18 +478,15 @@ cudaError_t launch_backward(const BwdArgs& a, cudaStream_t st) {
     f.err = a.err;
     f.groups = a.groups;
     f.gp = a.gp;
+    f.var = a.var;
     if (a.recompute) {
         const cudaError_t e = launch_step<LOGN>(f, kPhaseRowFwd | kPhaseColConv | kPhaseGrowth, st);
         if (e != cudaSuccess) return e;
     }
-    k_diffusion_bwd<LOGN><<<dim3(G::N / G::TX, G::N / G::TY, a.C), 256, DiffBwdGeo<LOGN>::SMEM,
-                            st>>>(a.A, a.x, a.ybar, a.xbar, a.abar, a.temp);
-    k_growth_bwd<LOGN><<<dim3(G::N / G::RB, a.K), G::RT, G::R2C_SMEM, st>>>(a.U, a.abar, a.tw,
-                                                                           a.ap, a.pgrad, a.K);
-    k_col_conv_adj<LOGN><<<dim3(G::M / G::TW, a.C), G::CT, AdjColGeo<LOGN>::SMEM, st>>>(
-        a.rowspec, a.kspec, a.U, a.kgrad, a.tw, a.groups, a.err);
-    k_row_c2r_add<LOGN><<<dim3(G::N / G::RB, a.C), G::RT, G::R2C_SMEM, st>>>(a.rowspec, a.xbar,
-                                                                            a.tw, 1.f, 1);
+    CG_VARIANT_SWITCH(a.var.diff, launch_diff_bwd, a, st)
+    CG_VARIANT_SWITCH(a.var.c2r, launch_growth_bwd, a, st)
+    CG_VARIANT_SWITCH(a.var.col, launch_col_adj, a, st)
+    CG_VARIANT_SWITCH(a.var.c2r, launch_c2r_add, a, st)
     return cudaGetLastError();
 }
 
@@ -462,9 +496,9 @@ template <int LOGN>
 cudaError_t launch_kgrad_final(float2* kgrad, float* hbar, int K, const float2* tw,
                                cudaStream_t st) {
     using G = Geo<LOGN>;
-    k_col_inv<LOGN><<<dim3(G::M / G::TW, K), G::CT, size_t(G::TW) * G::CP * sizeof(float2), st>>>(
+    k_col_inv<LOGN, 0><<<dim3(G::M / G::TW, K), G::CT, size_t(G::TW) * G::CP * sizeof(float2), st>>>(
         kgrad, tw);
-    k_row_c2r_add<LOGN><<<dim3(G::N / G::RB, K), G::RT, G::R2C_SMEM, st>>>(
+    k_row_c2r_add<LOGN, 0><<<dim3(G::N / G::RB, K), G::RT, G::R2C_SMEM, st>>>(
         kgrad, hbar, tw, 1.f / (4.f * float(G::N) * float(G::N)), 0);
     return cudaGetLastError();
 }

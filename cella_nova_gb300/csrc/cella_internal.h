@@ -95,6 +95,7 @@ struct BwdArgs {
     // true: recompute the row spectra, U and A of x first; false: rowspec, U
     // and A already hold them (a cached forward step)
     bool recompute;
+    Variants var;   // CTA shapes (the forward phases' tuned variants)
 };
 
 // Ring-kernel descriptors for the on-GPU kernel builder (kernels_common.cu).

@@ -442,6 +442,7 @@ BwdArgs bwd_args(cg_sim* s, const float* x, const float* ybar, float* xbar, doub
     a.gp = &s->dparams->gp;
     a.ap = &s->dparams->ap;
     a.recompute = true;
+    a.var = s->var;
     return a;
 }
 
