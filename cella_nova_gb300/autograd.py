@@ -62,6 +62,19 @@ class LeniaWorld:
             check(self.lib.cg_destroy(self.h))
             self.h = None
 
+    def autotune(self, reps: int = 5):
+        """Pick the fastest CTA shape of every phase (cg_autotune); the adjoint
+        kernels follow the forward phases' choice.  Returns the variants."""
+        ms = np.zeros(12, dtype=np.float64)
+        chosen = (ctypes.c_int * 4)()
+        check(self.lib.cg_autotune(self.h, int(reps), ms.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                   chosen))
+        return list(chosen)
+
+    def set_variants(self, v):
+        arr = (ctypes.c_int * 4)(*[int(x) for x in v])
+        check(self.lib.cg_set_variants(self.h, arr))
+
     def __del__(self):
         try:
             self.close()
@@ -221,10 +234,12 @@ class DiffusionLeniaGPU(torch.nn.Module):
     here per kernel in the orchestrator's c0/c1 order) plus the ring weights
     of each kernel."""
 
-    def __init__(self, creature, device="cuda"):
+    def __init__(self, creature, device="cuda", autotune=True):
         super().__init__()
         cr = creature
         self.world = LeniaWorld(cr.n, cr.C, cr.c0, cr.c1, cr.temp, device)
+        if autotune:
+            self.world.autotune()
         f32 = dict(dtype=torch.float32, device=device)
         self.seed = torch.nn.Parameter(torch.tensor(cr.seed, **f32))
         self.mu = torch.nn.Parameter(torch.tensor(np.asarray(cr.mu), **f32))

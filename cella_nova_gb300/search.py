@@ -98,13 +98,23 @@ class _Candidate:
             check(lib.cg_destroy(self.h))
             self.h = None
 
+    def autotune(self, lib, reps: int = 5):
+        ms = np.zeros(12, dtype=np.float64)
+        chosen = (ctypes.c_int * 4)()
+        check(lib.cg_autotune(self.h, int(reps), ms.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                              chosen))
+        return list(chosen)
+
+    def set_variants(self, lib, v):
+        check(lib.cg_set_variants(self.h, (ctypes.c_int * 4)(*v)))
+
 
 class GradientSearch:
     """Candidates (creatures of :func:`cella_nova_gb300.creature.make_creature`)
     optimised towards their targets with Adam, one CUDA graph per iteration."""
 
     def __init__(self, creatures, targets, T: int = 128, every: int = 16,
-                 adam: AdamConfig | None = None, n_streams: int = 4):
+                 adam: AdamConfig | None = None, n_streams: int = 4, autotune: bool = True):
         self.lib = _abi.load()
         self.T, self.every = int(T), int(every)
         self.adam = adam or AdamConfig()
@@ -115,6 +125,13 @@ class GradientSearch:
         self.step = torch.zeros(1, dtype=torch.int32, device="cuda")
         self.graph = None
         self.iterations = 0
+        if autotune:   # one tuning per grid side, shared by its candidates
+            chosen = {}
+            for c in self.cands:
+                if c.cr.n not in chosen:
+                    chosen[c.cr.n] = c.autotune(self.lib)
+                else:
+                    c.set_variants(self.lib, chosen[c.cr.n])
 
     def close(self):
         for c in self.cands:
