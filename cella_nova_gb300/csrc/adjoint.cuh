@@ -141,7 +141,7 @@ __device__ __forceinline__ void c2r_rows(float2* buf, const float2* __restrict__
         return make_float2(E.x - O.y, E.y + O.x);
     };
     auto st = [&](int s, int i, float2 v, int, int) { out(s, i, v); };
-    FftPasses<G::M, 1, true, G::RT, G::RB>::run(ld0, rows, rows, st, tw + G::TW_ROW);
+    FftPasses<G::M, 1, true, G::RT, G::RB, false, G::ROW_MR>::run(ld0, rows, rows, st, tw + G::TW_ROW);
 }
 
 __device__ __forceinline__ double block_sum(double v, double* red) {
@@ -192,7 +192,7 @@ __device__ __forceinline__ void growth_bwd_body(float2* __restrict__ U,
     };
     c2r_rows<LOGN, V>(sm, tw, out);
     SmemRows rows{sm, G::RP};
-    FftPasses<G::M, 1, false, G::RT, G::RB>::run(rows, rows, rows, rows, tw + G::TW_ROW);
+    FftPasses<G::M, 1, false, G::RT, G::RB, false, G::ROW_MR>::run(rows, rows, rows, rows, tw + G::TW_ROW);
     r2c_finish<LOGN, V>(sm, tw, Uk);
     const double sw = block_sum(double(pw), red);
     const double smu = block_sum(double(pmu), red);
@@ -432,7 +432,7 @@ cudaError_t prepare_backward() {
 }
 
 // The adjoint kernels take the CTA shapes of the forward phases they mirror
-// (the handle's tuned variants; all variants give the same bits): diffusion
+// (the handle's tuned variants, radix included): diffusion
 // for the diffusion adjoint, the inverse row pass for the growth adjoint and
 // the final row transform, the column pass for the adjoint column pass.
 template <int LOGN, int V>

@@ -103,44 +103,51 @@ struct Dft<1, INV> {
     __device__ __forceinline__ static void run(float2*) {}
 };
 
-// Radix of the pass that starts at sub-transform size NS.  Greedy plans use
-// radix 16 until fewer than 16 remain (16,16,...,rem); REMFIRST plans put
-// the remainder first (rem,16,16,...), so the first pass of a REMFIRST
-// inverse sees exactly the index sets the last pass of a greedy forward
-// transform left in each thread's registers.
-__host__ __device__ constexpr int rem_radix(int L) {
+// Radix of the pass that starts at sub-transform size NS, for plans of
+// maximum radix MR (16 or 8).  Greedy plans use radix MR until fewer than MR
+// remain (MR,MR,...,rem); REMFIRST plans put the remainder first
+// (rem,MR,MR,...), so the first pass of a REMFIRST inverse sees exactly the
+// index sets the last pass of a greedy forward transform left in each
+// thread's registers.
+__host__ __device__ constexpr int log2_of(int v) {
     int b = 0;
-    while ((1 << b) < L) ++b;
-    return (b % 4) == 0 ? (L >= 16 ? 16 : L) : (1 << (b % 4));
+    while ((1 << b) < v) ++b;
+    return b;
 }
-__host__ __device__ constexpr int plan_radix(int L, int ns, bool remfirst) {
-    return (remfirst && ns == 1) ? rem_radix(L) : ((L / ns >= 16) ? 16 : (L / ns));
+__host__ __device__ constexpr int rem_radix(int L, int MR = 16) {
+    const int b = log2_of(L), g = log2_of(MR);
+    return (b % g) == 0 ? (L >= MR ? MR : L) : (1 << (b % g));
 }
-template <int L, int NS, bool REMFIRST = false>
+__host__ __device__ constexpr int plan_radix(int L, int ns, bool remfirst, int MR = 16) {
+    return (remfirst && ns == 1) ? rem_radix(L, MR) : ((L / ns >= MR) ? MR : (L / ns));
+}
+template <int L, int NS, bool REMFIRST = false, int MR = 16>
 struct PassRadix {
-    static constexpr int R = plan_radix(L, NS, REMFIRST);
+    static constexpr int R = plan_radix(L, NS, REMFIRST, MR);
 };
 
 // Per-pass twiddle tables.  The pass starting at sub-transform size NS > 1
 // with radix R reads W_{NS*R}^{r*k} for r in [1, R), k in [0, NS), stored at
 // tw_offset(L, plan, NS) + (r-1)*NS + k: consecutive butterflies read
 // consecutive entries (one or two L1 wavefronts per warp).
-__host__ __device__ constexpr int tw_offset(int L, bool remfirst, int NS) {
+__host__ __device__ constexpr int tw_offset(int L, bool remfirst, int NS, int MR = 16) {
     int off = 0, ns = 1;
     while (ns < NS) {
-        const int R = plan_radix(L, ns, remfirst);
+        const int R = plan_radix(L, ns, remfirst, MR);
         if (ns > 1) off += (R - 1) * ns;
         ns *= R;
     }
     return off;
 }
-__host__ __device__ constexpr int tw_size(int L, bool remfirst) { return tw_offset(L, remfirst, L); }
+__host__ __device__ constexpr int tw_size(int L, bool remfirst, int MR = 16) {
+    return tw_offset(L, remfirst, L, MR);
+}
 
-// Radix of the last pass of a length-L transform.
-__host__ __device__ constexpr int last_radix(int L) {
+// Radix of the last pass of a greedy length-L transform.
+__host__ __device__ constexpr int last_radix(int L, int MR = 16) {
     int ns = 1, r = 1;
     while (ns < L) {
-        r = (L / ns >= 16) ? 16 : L / ns;
+        r = (L / ns >= MR) ? MR : L / ns;
         ns *= r;
     }
     return r;
@@ -209,18 +216,18 @@ __device__ __forceinline__ void stockham_pass(LD& ld, ST& st, const float2* __re
 // Full length-L transform: first pass reads through `ld`, middle passes use
 // shared memory through smld/smst, the last pass writes through `stl`.
 // `tab` is the plan's twiddle table (tw_offset layout).
-template <int L, int NS, bool INV, int T, int S, bool REMFIRST = false>
+template <int L, int NS, bool INV, int T, int S, bool REMFIRST = false, int MR = 16>
 struct FftPasses {
     template <class LD, class SMLD, class SMST, class STL>
     __device__ __forceinline__ static void run(LD& ld, SMLD& smld, SMST& smst, STL& stl,
                                                const float2* __restrict__ tab) {
-        constexpr int R = PassRadix<L, NS, REMFIRST>::R;
-        const float2* twp = tab + tw_offset(L, REMFIRST, NS);
+        constexpr int R = PassRadix<L, NS, REMFIRST, MR>::R;
+        const float2* twp = tab + tw_offset(L, REMFIRST, NS, MR);
         if constexpr (NS * R == L) {
             stockham_pass<L, R, NS, INV, T, S>(ld, stl, twp);
         } else {
             stockham_pass<L, R, NS, INV, T, S>(ld, smst, twp);
-            FftPasses<L, NS * R, INV, T, S, REMFIRST>::run(smld, smld, smst, stl, tab);
+            FftPasses<L, NS * R, INV, T, S, REMFIRST, MR>::run(smld, smld, smst, stl, tab);
         }
     }
 };

@@ -73,12 +73,12 @@ int cuda_fail(cudaError_t e, const char* what) {
 // first) and the row plan (greedy, length n/2).  Every entry is rounded once
 // from double; the reference builds its table from an f32 angle
 // (convolution.rs:19-30).
-static void fill_plan(int L, bool remfirst, float2* out) {
+static void fill_plan(int L, bool remfirst, int MR, float2* out) {
     int ns = 1;
     while (ns < L) {
-        const int R = plan_radix(L, ns, remfirst);
+        const int R = plan_radix(L, ns, remfirst, MR);
         if (ns > 1) {
-            float2* t = out + tw_offset(L, remfirst, ns);
+            float2* t = out + tw_offset(L, remfirst, ns, MR);
             for (int r = 1; r < R; ++r)
                 for (int k = 0; k < ns; ++k) {
                     const double a = -2.0 * M_PI * double(r) * double(k) / double(ns * R);
@@ -95,11 +95,13 @@ void build_twiddle_tables(int n, float2* out) {
         out[m] = make_float2(float(std::cos(a)), float(std::sin(a)));
     }
     float2* p = out + n;
-    fill_plan(n, false, p);
+    fill_plan(n, false, 16, p);
     p += tw_size(n, false);
-    fill_plan(n, true, p);
+    fill_plan(n, true, 16, p);
     p += tw_size(n, true);
-    fill_plan(n / 2, false, p);
+    fill_plan(n / 2, false, 16, p);
+    p += tw_size(n / 2, false);
+    fill_plan(n / 2, false, 8, p);
 }
 
 static bool finite(float v) { return std::isfinite(v); }

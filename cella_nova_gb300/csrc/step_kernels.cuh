@@ -40,10 +40,15 @@ struct Geo {
     // kx-major transposes conflict-free: odd for RB >= 16 (a half-warp reads
     // 16 rows of one column), 2 mod 16 for RB = 8 (8 rows x 2 columns),
     // 4 mod 16 for RB = 4.
+    // Variant 2 of the row passes is variant 1's shape with radix-8 FFT
+    // passes (ROW_MR): one more pass through shared memory, half the values
+    // per butterfly in registers.  It rounds differently from the radix-16
+    // plans (the other variants of every phase compute the same bits).
     static constexpr int RB0 = 8192 / M;
     static constexpr int RB1 = RB0 < 8 ? 8 : (RB0 > N ? N : RB0);
-    static constexpr int RB = (V == 1 && RB1 > 4) ? RB1 / 2 : RB1;
-    static constexpr int RT = (V == 1) ? 256 : 512;
+    static constexpr int RB = (V >= 1 && RB1 > 4) ? RB1 / 2 : RB1;
+    static constexpr int RT = (V >= 1) ? 256 : 512;
+    static constexpr int ROW_MR = (V == 2) ? 8 : 16;
     static constexpr int RP = padded_len(M) + (RB >= 16 ? 1 : (RB == 8 ? 2 : 4));
     static constexpr size_t R2C_SMEM = size_t(RB) * RP * sizeof(float2);
     static constexpr size_t C2R_SMEM = 2 * R2C_SMEM;    // double-buffered input
@@ -67,11 +72,14 @@ struct Geo {
     static_assert((KSOFF * sizeof(float2)) % 16 == 0, "bulk-copy destination alignment");
     static constexpr size_t COL_SMEM = (size_t(KSOFF) + size_t(TW) * N) * sizeof(float2);
     // Twiddle buffer: W_N^m (m < N), then the pass tables of the column
-    // forward plan, the column inverse plan and the row plan.
+    // forward plan, the column inverse plan, the row plan and the radix-8
+    // row plan; TW_ROWV is this variant's row table.
     static constexpr int TW_COL_FWD = N;
     static constexpr int TW_COL_INV = TW_COL_FWD + tw_size(N, false);
-    static constexpr int TW_ROW = TW_COL_INV + tw_size(N, true);
-    static constexpr int TW_TOTAL = TW_ROW + tw_size(M, false);
+    static constexpr int TW_ROW16 = TW_COL_INV + tw_size(N, true);
+    static constexpr int TW_ROW8 = TW_ROW16 + tw_size(M, false);
+    static constexpr int TW_TOTAL = TW_ROW8 + tw_size(M, false, 8);
+    static constexpr int TW_ROW = (ROW_MR == 8) ? TW_ROW8 : TW_ROW16;
     // Diffusion tile.
     static constexpr int TX = N < 64 ? N : 64;
     static constexpr int TY0 = (V == 1) ? 16 : (V == 2 ? 64 : 32);
@@ -100,7 +108,7 @@ __device__ __forceinline__ void row_r2c_body(const float* __restrict__ state,
         reinterpret_cast<const float2*>(state + (size_t(c) * G::N + y0) * G::N);
     auto ld0 = [&](int s, int i, int, int) { return __ldg(&src[size_t(s) * G::M + i]); };
     SmemRows rows{sm, G::RP};
-    FftPasses<G::M, 1, false, G::RT, G::RB>::run(ld0, rows, rows, rows, tw + G::TW_ROW);
+    FftPasses<G::M, 1, false, G::RT, G::RB, false, G::ROW_MR>::run(ld0, rows, rows, rows, tw + G::TW_ROW);
     r2c_finish<LOGN, V>(sm, tw, rowspec + size_t(c) * G::M * G::N + y0);
 }
 
@@ -324,7 +332,7 @@ __device__ __forceinline__ void row_c2r_growth_body(const float2* __restrict__ U
                                                     float* __restrict__ udbg, float udbg_scale,
                                                     int c, int y0, float2* sm) {
     using G = Geo<LOGN, V>;
-    constexpr int RL = last_radix(G::M);
+    constexpr int RL = last_radix(G::M, G::ROW_MR);
     constexpr int JL = G::M / RL;
     constexpr int ITEMS = G::RB * JL;
     constexpr int IPT = (ITEMS + G::RT - 1) / G::RT;
@@ -384,7 +392,7 @@ __device__ __forceinline__ void row_c2r_growth_body(const float2* __restrict__ U
                     make_float2(v.x * udbg_scale, v.y * udbg_scale);
             }
         };
-        FftPasses<G::M, 1, true, G::RT, G::RB>::run(ld0, rows, rows, gst, tw + G::TW_ROW);
+        FftPasses<G::M, 1, true, G::RT, G::RB, false, G::ROW_MR>::run(ld0, rows, rows, gst, tw + G::TW_ROW);
     }
 
     float* Ac = A + (size_t(c) * G::N + y0) * G::N;

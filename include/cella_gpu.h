@@ -150,10 +150,13 @@ int cg_download_affinity(cg_sim* sim, float* out);
  * copy (always 0: the state is ping-ponged, no copy exists). */
 int cg_timed_iterate(cg_sim* sim, double ms[4]);
 
-/* Autotuner (no reference counterpart).  Each phase has three CTA-shape
- * variants (rows per CTA and threads for the row FFTs, columns per CTA and
- * threads for the column pass, tile rows for diffusion); they give
- * bit-identical results.  cg_autotune times every variant of every phase
+/* Autotuner (no reference counterpart).  Each phase has three variants:
+ * CTA shapes (rows per CTA and threads for the row FFTs, columns per CTA and
+ * threads for the column pass, tile rows and columns per thread for
+ * diffusion) and, for the row FFTs, the FFT radix (variant 2: radix-8
+ * passes, the others radix 16).  All variants give bit-identical results
+ * except the radix-8 row plan, which differs by FP32 rounding (about 1e-7).
+ * cg_autotune times every variant of every phase
  * `reps` times on the live handle (the state is not advanced), keeps the
  * fastest per phase and re-captures the step graphs.  ms_out[12]
  * (phase-major: [row FFT v0..v2, column v0..v2, inverse row + growth
@@ -327,7 +330,7 @@ int cg_batch_stream(cg_batch* b, cg_stream_t* out);
 int cg_batch_info(cg_batch* b, int* items4, int* grid4);
 
 /* Autotuner of the batch: per grid side present and per phase, times the
- * three CTA-shape variants (those of cg_autotune; all give the same bits) on
+ * three variants (those of cg_autotune) on
  * the live batch without stepping it, keeps the fastest and re-captures the
  * step graphs.  chosen[6*4] and ms[6*4*3] (either may be NULL) are indexed
  * by grid side 64, 128, ..., 2048, then phase, then variant; sides the batch
