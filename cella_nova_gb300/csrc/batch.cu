@@ -249,33 +249,50 @@ cudaError_t launch_phase(cg_batch* b, int phase, int parity, cudaStream_t st) {
     return cudaGetLastError();
 }
 
-cudaError_t enqueue_step(cg_batch* b, int parity, cudaStream_t st) {
-    cudaError_t e = cudaSuccess;
-    for (int p = 0; p < 4 && e == cudaSuccess; ++p) e = launch_phase(b, p, parity, st);
-    return e;
-}
-
 // One graph per ping-pong parity, (re)captured from the current variants.
+// The size classes share no data, so each runs its four phases on a forked
+// stream of its own: one class's phase tails overlap the other's work.
 cudaError_t capture_batch_graphs(cg_batch* b) {
     for (auto& g : b->graph)
         if (g) {
             cudaGraphExecDestroy(g);
             g = nullptr;
         }
-    cudaStream_t cap = nullptr;
-    cudaError_t e = cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking);
+    const size_t nc = b->classes.size();
+    std::vector<cudaStream_t> st(nc, nullptr);
+    std::vector<cudaEvent_t> done(nc, nullptr);
+    cudaEvent_t fork = nullptr;
+    cudaError_t e = cudaEventCreateWithFlags(&fork, cudaEventDisableTiming);
+    for (size_t i = 0; i < nc && e == cudaSuccess; ++i) {
+        e = cudaStreamCreateWithFlags(&st[i], cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&done[i], cudaEventDisableTiming);
+    }
     for (int p = 0; p < 2 && e == cudaSuccess; ++p) {
         cudaGraph_t g = nullptr;
-        e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
+        e = cudaStreamBeginCapture(st[0], cudaStreamCaptureModeThreadLocal);
         if (e == cudaSuccess) {
-            cudaError_t le = enqueue_step(b, p, cap);
-            e = cudaStreamEndCapture(cap, &g);
+            cudaError_t le = cudaEventRecord(fork, st[0]);
+            for (size_t i = 1; i < nc && le == cudaSuccess; ++i)
+                le = cudaStreamWaitEvent(st[i], fork, 0);
+            for (size_t i = 0; i < nc && le == cudaSuccess; ++i)
+                for (int ph = 0; ph < 4 && le == cudaSuccess; ++ph)
+                    le = launch_class_phase(b, b->classes[i], ph, b->classes[i].var[ph], p, st[i]);
+            for (size_t i = 1; i < nc && le == cudaSuccess; ++i) {
+                le = cudaEventRecord(done[i], st[i]);
+                if (le == cudaSuccess) le = cudaStreamWaitEvent(st[0], done[i], 0);
+            }
+            if (le == cudaSuccess) le = cudaGetLastError();
+            e = cudaStreamEndCapture(st[0], &g);
             if (le != cudaSuccess) e = le;
         }
         if (e == cudaSuccess) e = cudaGraphInstantiate(&b->graph[p], g, 0);
         if (g) cudaGraphDestroy(g);
     }
-    if (cap) cudaStreamDestroy(cap);
+    for (size_t i = 0; i < nc; ++i) {
+        if (st[i]) cudaStreamDestroy(st[i]);
+        if (done[i]) cudaEventDestroy(done[i]);
+    }
+    if (fork) cudaEventDestroy(fork);
     return e;
 }
 
