@@ -1,0 +1,75 @@
+"""Error returns of the C ABI on a live handle: the call fails with its
+status code and leaves the world usable."""
+import numpy as np
+import pytest
+
+from cella_nova_gb300 import CellaError, GpuMaceLenia
+from cella_nova_gb300.creature import make_creature
+from cella_nova_gb300.orchestrator import creature_ring_specs
+
+pytestmark = pytest.mark.gpu
+
+ARG, IO = -1, -5
+
+
+def world(seed=3):
+    cr = make_creature(64, 2, seed=seed, radius=(4, 12), seed_box=32)
+    return cr, GpuMaceLenia.from_creature(cr)
+
+
+def assert_code(code, fn, *args, **kw):
+    with pytest.raises(CellaError) as e:
+        fn(*args, **kw)
+    assert e.value.code == code, e.value
+
+
+def test_bad_ring_specs_are_rejected():
+    cr, sim = world()
+    with sim:
+        specs, _ = creature_ring_specs(cr)
+        bad_family = [(5, 1, 8.0, 0.0)] + specs[1:]
+        too_many = [(0, 9, 8.0, 0.0)] + specs[1:]
+        no_radius = [(0, 1, 0.0, 0.0)] + specs[1:]
+        no_width = [(1, 1, 8.0, 0.0)] + specs[1:]
+        for bad in (bad_family, too_many, no_radius, no_width):
+            assert_code(ARG, sim.build_ring_kernels, bad)
+        x = sim.state()
+        sim.iterate()    # still steps
+        assert np.isfinite(sim.state()).all() and not np.array_equal(sim.state(), x)
+
+
+def test_frame_stream_to_an_invalid_descriptor_fails_cleanly():
+    cr, sim = world(4)
+    with sim:
+        assert_code(ARG, sim.stream_frames, -1, 2)
+        # a descriptor number far above any open one: write() fails (EBADF)
+        assert_code(IO, sim.stream_frames, 1 << 20, 2)
+        sim.run_steps(3)    # the world keeps stepping
+        assert np.isfinite(sim.state()).all()
+
+
+def test_parameter_and_variant_errors_leave_the_world_unchanged():
+    cr, sim = world(5)
+    _, twin = world(5)
+    with sim, twin:
+        bad_sigma = np.asarray(cr.sigma, np.float32).copy()
+        bad_sigma[0] = np.nan
+        assert_code(ARG, sim.set_params, cr.mu, bad_sigma, cr.weights)
+        assert_code(ARG, sim.set_variants, [0, 3, 0, 0])
+        sim.run_steps(4)
+        twin.run_steps(4)
+        np.testing.assert_array_equal(sim.state(), twin.state())
+
+
+def test_unroll_argument_errors():
+    import ctypes
+    torch = pytest.importorskip("torch")
+    from cella_nova_gb300.autograd import LeniaWorld
+    cr = make_creature(64, 2, seed=6, radius=(4, 12), seed_box=32)
+    w = LeniaWorld(cr.n, cr.C, cr.c0, cr.c1, cr.temp)
+    x = torch.zeros((cr.C, 64, 64), device="cuda")
+    P = lambda t: ctypes.c_void_p(t.data_ptr())
+    assert w.lib.cg_unroll(w.h, P(x), 0, 4, P(x), P(x)) == ARG
+    assert w.lib.cg_unroll(w.h, P(x), 4, 0, P(x), P(x)) == ARG
+    assert w.lib.cg_unroll(w.h, None, 4, 4, P(x), P(x)) == ARG
+    w.close()
