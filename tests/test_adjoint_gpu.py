@@ -86,7 +86,7 @@ def test_unroll_forward_equals_graph_steps():
     path with the same kernels."""
     from cella_nova_gb300.orchestrator import creature_ring_specs
     cr = make_creature(128, 3, seed=60, radius=(8, 20), seed_box=64)
-    m = DiffusionLeniaGPU(cr)
+    m = DiffusionLeniaGPU(cr, autotune=False)   # the graph path below is untuned too
     with torch.no_grad():
         xT = m(7, 3)
     specs, w = creature_ring_specs(cr)
