@@ -113,10 +113,9 @@ __global__ void __launch_bounds__(256) k_diffusion_bwd(const float* __restrict__
 template <int LOGN, int V = 0>
 __device__ __forceinline__ void gather_rows(const float2* __restrict__ src, float2* buf) {
     using G = Geo<LOGN, V>;
-    for (int item = threadIdx.x; item < G::RB * G::M; item += G::RT) {
-        const int s = item % G::RB, kx = item / G::RB;
-        cp_async8(&buf[s * G::RP + pidx(kx)], &src[size_t(kx) * G::N + s]);
-    }
+    for_row_tile<LOGN, V>([&](int s, int kx, int pk) {
+        cp_async8(&buf[s * G::RP + pk], &src[size_t(kx) * G::N + s]);
+    });
     cp_async_commit();
     cp_async_wait<0>();
     __syncthreads();

@@ -94,6 +94,26 @@ struct Geo {
 // X[M] are real and share slot 0.  Output scale: 2 x rfft.
 // grid (N/RB, C), block RT.
 // ---------------------------------------------------------------------------
+// Visit the RB x M elements (row s, column kx) of a kx-major row tile with
+// the RT threads of a row kernel: thread t owns row s = t % RB and columns
+// t / RB + i * (RT / RB), so both the padded shared index pidx(kx) and the
+// global address advance by constants (pidx(kx + STEP) = pidx(kx) +
+// pidx(STEP) when STEP is a multiple of 16).  f(s, kx, pidx(kx)).
+template <int LOGN, int V, class F>
+__device__ __forceinline__ void for_row_tile(F f) {
+    using G = Geo<LOGN, V>;
+    static_assert(G::RT % G::RB == 0, "a thread keeps one row");
+    constexpr int STEP = G::RT / G::RB;
+    const int s = threadIdx.x % G::RB, kx0 = threadIdx.x / G::RB;
+    if constexpr (G::M % STEP == 0 && STEP % 16 == 0) {
+        const int pk0 = pidx(kx0);
+#pragma unroll
+        for (int i = 0; i < G::M / STEP; ++i) f(s, kx0 + i * STEP, pk0 + i * pidx(STEP));
+    } else {
+        for (int kx = kx0; kx < G::M; kx += STEP) f(s, kx, pidx(kx));
+    }
+}
+
 template <int LOGN, int V = 0>
 __device__ __forceinline__ void r2c_finish(float2* sm, const float2* __restrict__ tw,
                                            float2* __restrict__ dst);
@@ -138,10 +158,8 @@ __device__ __forceinline__ void r2c_finish(float2* sm, const float2* __restrict_
     }
     __syncthreads();
 
-    for (int item = threadIdx.x; item < G::RB * G::M; item += G::RT) {
-        const int s = item % G::RB, kx = item / G::RB;
-        dst[size_t(kx) * G::N + s] = sm[s * G::RP + pidx(kx)];
-    }
+    for_row_tile<LOGN, V>(
+        [&](int s, int kx, int pk) { dst[size_t(kx) * G::N + s] = sm[s * G::RP + pk]; });
 }
 
 template <int LOGN, int V = 0>
@@ -342,10 +360,9 @@ __device__ __forceinline__ void row_c2r_growth_body(const float2* __restrict__ U
     auto gather = [&](int gi, float2* buf) {
         const int k = groups.out_idx[base + gi];
         const float2* src = U + size_t(k) * G::M * G::N + y0;
-        for (int item = threadIdx.x; item < G::RB * G::M; item += G::RT) {
-            const int s = item % G::RB, kx = item / G::RB;
-            cp_async8(&buf[s * G::RP + pidx(kx)], &src[size_t(kx) * G::N + s]);
-        }
+        for_row_tile<LOGN, V>([&](int s, int kx, int pk) {
+            cp_async8(&buf[s * G::RP + pk], &src[size_t(kx) * G::N + s]);
+        });
         cp_async_commit();
     };
 
