@@ -171,6 +171,7 @@ cudaError_t launch_f64_to_f32(const double* in, float* out, size_t count, cudaSt
 cudaError_t launch_mass_f64(const float* x, int C, size_t px, double* partial, int nblocks,
                             double* out, cudaStream_t s);
 cudaError_t launch_render(const float* x, int C, size_t px, unsigned* out, cudaStream_t s);
+cudaError_t launch_wait_check(int* err, int timeout_ms, cudaStream_t s);
 cudaError_t launch_rgb24(const unsigned* in, unsigned char* out, size_t px, cudaStream_t s);
 cudaError_t launch_fold_params(const float* mu, const float* sigma, const float* w, int C, int K,
                                const KernelGroups& g, DeviceParams* p, cudaStream_t s);

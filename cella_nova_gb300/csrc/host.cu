@@ -958,6 +958,15 @@ int cg_step_backward(cg_sim* s, const float* x, const float* ybar, float* xbar, 
     return CG_OK;
 }
 
+int cg_check_bounded_wait(cg_sim* s, int timeout_ms) {
+    if (!s) return fail(CG_ERR_ARG, "cg_check_bounded_wait: NULL handle");
+    if (timeout_ms < 1 || timeout_ms > 2000)
+        return fail(CG_ERR_ARG, "cg_check_bounded_wait: timeout %d ms outside [1, 2000]", timeout_ms);
+    CG_CHECK(launch_wait_check(s->err, timeout_ms, s->stream), "launching the wait check");
+    CG_CHECK(cudaStreamSynchronize(s->stream), "cudaStreamSynchronize");
+    return check_device_error(s);   // CG_ERR_TIMEOUT, and the word is cleared
+}
+
 int cg_zero_grads(cg_sim* s, double* pgrad, float* kgrad) {
     if (!s || !pgrad) return fail(CG_ERR_ARG, "cg_zero_grads: NULL argument");
     CG_CHECK(cudaMemsetAsync(pgrad, 0, sizeof(double) * 3 * s->K, s->stream), "zeroing pgrad");

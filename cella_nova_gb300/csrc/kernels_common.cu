@@ -2,6 +2,7 @@
 #include <mutex>
 #include <unordered_map>
 
+#include "async_copy.cuh"
 #include "cella_gpu.h"
 #include "cella_internal.h"
 #include "render.cuh"
@@ -320,6 +321,28 @@ cudaError_t launch_ring_grad(int n, int K, const RingSet& rs, const float* ring_
                              const double* zsum, float* grad, cudaStream_t s) {
     k_ring_grad<<<dim3(kRingBlocks, K), 256, 0, s>>>(n, rs, hbar, partial);
     k_ring_grad_final<<<K, 32, 0, s>>>(rs, ring_w, partial, kRingBlocks, ring_s, zsum, grad);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Check of the bounded-wait path: one CTA waits on an mbarrier that no copy
+// and no thread ever completes, through the same mbar_wait the step kernels
+// use, with a short limit.  The wait gives up, records the timeout in the
+// error word and the kernel returns: no hang, no fault.
+// ---------------------------------------------------------------------------
+__global__ void k_wait_check(int* err, unsigned long long limit_ns) {
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        fence_barrier_init();
+    }
+    __syncthreads();
+    mbar_wait(&bar, 0, err, limit_ns);   // phase 0 never completes
+    __syncthreads();
+}
+
+cudaError_t launch_wait_check(int* err, int timeout_ms, cudaStream_t s) {
+    k_wait_check<<<1, 32, 0, s>>>(err, 1000000ull * unsigned(timeout_ms));
     return cudaGetLastError();
 }
 

@@ -174,6 +174,13 @@ class GpuMaceLenia:
         written (main.rs:239-303's loop, to a file or a pipe)."""
         check(self._lib.cg_stream_frames(self._h, int(fd), int(nframes), int(steps_per_frame)))
 
+    def check_bounded_wait(self, timeout_ms: int = 20):
+        """Run the failure-path check: a kernel whose device-side wait can
+        never complete gives up after timeout_ms and records the timeout.
+        Raises CellaError(CG_ERR_TIMEOUT), as a step whose copy never landed
+        would; the world is untouched and stays usable."""
+        check(self._lib.cg_check_bounded_wait(self._h, int(timeout_ms)))
+
     def render_ptr(self) -> int:
         """Device address of the render buffer (n*n uint32)."""
         p = ctypes.c_void_p()

@@ -123,6 +123,13 @@ int cg_download_render(cg_sim* sim, uint8_t* rgb24);
  * Blocking; CG_ERR_IO if a write fails. */
 int cg_stream_frames(cg_sim* sim, int fd, int nframes, int steps_per_frame);
 
+/* Failure-path check: runs a kernel whose bounded device-side wait can never
+ * complete (an mbarrier nothing arrives on), through the same wait the step
+ * kernels use but limited to timeout_ms (1..2000).  The kernel gives up and
+ * records the timeout, and this call returns CG_ERR_TIMEOUT exactly as a step
+ * whose copy never landed would; the handle stays usable.  Blocking. */
+int cg_check_bounded_wait(cg_sim* sim, int timeout_ms);
+
 /* The packed render words themselves (n*n uint32_t), blocking. */
 int cg_download_render_packed(cg_sim* sim, uint32_t* out);
 

@@ -73,3 +73,22 @@ def test_unroll_argument_errors():
     assert w.lib.cg_unroll(w.h, P(x), 4, 0, P(x), P(x)) == ARG
     assert w.lib.cg_unroll(w.h, None, 4, 4, P(x), P(x)) == ARG
     w.close()
+
+
+def test_bounded_wait_gives_up_and_reports_timeout():
+    """A device-side wait that nothing completes (an mbarrier no thread or
+    copy arrives on) ends at its limit with the timeout status; the context
+    and the handle stay usable, and the world steps exactly as its twin."""
+    TIMEOUT = -4
+    cr, sim = world(7)
+    _, twin = world(7)
+    with sim, twin:
+        sim.run_steps(2)
+        twin.run_steps(2)
+        for ms in (5, 50):
+            assert_code(TIMEOUT, sim.check_bounded_wait, ms)
+        assert_code(ARG, sim.check_bounded_wait, 0)
+        assert_code(ARG, sim.check_bounded_wait, 5000)
+        sim.run_steps(3)      # the error word was cleared: steps report OK
+        twin.run_steps(3)
+        np.testing.assert_array_equal(sim.state(), twin.state())
