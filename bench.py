@@ -164,9 +164,11 @@ def barrier(dist, world):
         dist.barrier()
 
 
-def cpu_baseline(cr, budget_s=20.0, nthreads=None):
+def cpu_baseline(cr, budget_s=20.0, nthreads=None, forms=True):
     """The FP32 C restatement of example.rs (faithful: FFT per kernel), all
-    host threads, one step of the full workload (a bounded sample)."""
+    host threads, one step of the full workload (a bounded sample).  With
+    forms, one step more in each of the other forms: one thread (example.rs
+    is serial) and FP64, each timed once."""
     from oracle import oracle as O
     nthreads = nthreads or os.cpu_count() or 1
     st = cr.seed.astype(np.float32)
@@ -182,9 +184,20 @@ def cpu_baseline(cr, budget_s=20.0, nthreads=None):
         if time.perf_counter() - t_start > budget_s or len(times) >= 3:
             break
     t = min(times)
-    return {"value": cr.n * cr.n / t, "unit": UNIT, "cores": nthreads, "kind": "port",
-            "sample": f"{len(times)} step(s) of the {cr.n}^2 C={cr.C} K={cr.K} workload, "
-                      f"f32 C port of example.rs (FFT per kernel), OpenMP, best {t:.2f} s/step"}
+    out = {"value": cr.n * cr.n / t, "unit": UNIT, "cores": nthreads, "kind": "port",
+           "sample": f"{len(times)} step(s) of the {cr.n}^2 C={cr.C} K={cr.K} workload, "
+                     f"f32 C port of example.rs (FFT per kernel), OpenMP, best {t:.2f} s/step"}
+    if forms:
+        rows = [{"threads": nthreads, "dtype": "f32", "s_per_step": round(t, 3)}]
+        for dt, nt in ((np.float64, nthreads), (np.float32, 1), (np.float64, 1)):
+            t0 = time.perf_counter()
+            O.step_c(cr.seed.astype(dt), ks, *args, dtype=dt, faithful=True, nthreads=nt)
+            rows.append({"threads": nt, "dtype": "f32" if dt == np.float32 else "f64",
+                         "s_per_step": round(time.perf_counter() - t0, 3)})
+        for r in rows:
+            r["cell_updates_per_s"] = cr.n * cr.n / r["s_per_step"]
+        out["forms"] = rows
+    return out
 
 
 def step_error_vs_fp64(sim, cr):

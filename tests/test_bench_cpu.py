@@ -23,3 +23,19 @@ def test_reference_arm_line():
     assert e2e["value"] == line["value"] and e2e["h2d_bytes_per_step"] == 0
     assert e2e["d2h_bytes_per_step"] == 0 and e2e["unit"] == line["unit"]
     assert line["config"]["n"] == 2048 and line["config"]["kernels"] == 9
+
+
+def test_cpu_baseline_forms_small():
+    """The cpu_baseline object with its other forms (one thread, FP64), on a
+    64^2 creature."""
+    sys.path.insert(0, ROOT)
+    import bench
+    from cella_nova_gb300.creature import make_creature
+    from oracle import oracle as O
+    O.build()
+    cr = make_creature(64, 2, seed=1, radius=(4, 12), seed_box=32)
+    cpu = bench.cpu_baseline(cr, budget_s=1.0, nthreads=2)
+    assert cpu["kind"] == "port" and cpu["cores"] == 2 and cpu["value"] > 0
+    forms = {(f["threads"], f["dtype"]) for f in cpu["forms"]}
+    assert forms == {(2, "f32"), (2, "f64"), (1, "f32"), (1, "f64")}
+    assert all(f["cell_updates_per_s"] > 0 for f in cpu["forms"])
