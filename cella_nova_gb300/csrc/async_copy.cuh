@@ -56,6 +56,28 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t by
         : "memory");
 }
 
+// 2-D tiled tensor copy global -> shared (TMA engine): the box of `map` at
+// element coordinates (x, y), x innermost, lands dense in shared memory and
+// completes on `bar`.  `map` is the address of a CUtensorMap in kernel
+// parameter space (__grid_constant__) or global memory; x times the element
+// size must be a multiple of 16 bytes, dst 128-byte aligned.
+__device__ __forceinline__ void tensor2d_g2s(void* dst, const void* map, int x, int y,
+                                             uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%2, %3}], [%4];" ::"r"(smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
+        : "memory");
+}
+
+// Before the TMA engine reads a tensor map held in global memory: order its
+// (host-written) bytes before the tensor-map proxy's reads.
+__device__ __forceinline__ void tensormap_acquire(const void* map) {
+    asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(
+                     reinterpret_cast<uint64_t>(map))
+                 : "memory");
+}
+
 __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
     uint32_t ok;
     asm volatile(

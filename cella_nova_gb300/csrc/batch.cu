@@ -28,6 +28,9 @@ constexpr int kBatchMinLogN = 6;   // 64^2 .. 2048^2 in one batch
 constexpr int kBatchMaxLogN = 11;
 
 struct WorldDesc {
+    // tensor maps of U for the inverse row pass's tile copies: [0] with
+    // variant 0's rows per tile, [1] with variants 1 and 2's
+    CUtensorMap umap[2];
     int logn, C, K;
     float temp;
     float* state[2];
@@ -39,6 +42,22 @@ struct WorldDesc {
     KernelGroups groups;
     GrowthParams gp;
 };
+
+// Rows per inverse-row-pass tile of a size and variant (Geo<LOGN, V>::RB).
+template <int LOGN>
+int row_tile_rows(int v) {
+    return v == 0 ? Geo<LOGN, 0>::RB : Geo<LOGN, 1>::RB;
+}
+int row_tile_rows(int logn, int v) {
+    switch (logn) {
+        case 6: return row_tile_rows<6>(v);
+        case 7: return row_tile_rows<7>(v);
+        case 8: return row_tile_rows<8>(v);
+        case 9: return row_tile_rows<9>(v);
+        case 10: return row_tile_rows<10>(v);
+        default: return row_tile_rows<11>(v);
+    }
+}
 
 struct WorkItem {
     int world, c, a, b;   // a, b: row/column offsets of the unit
@@ -86,14 +105,19 @@ __global__ void __launch_bounds__(Geo<LOGN, V>::CT, 512 / Geo<LOGN, V>::CT)
 template <int LOGN, int V>
 __global__ void __launch_bounds__(Geo<LOGN, V>::RT, 512 / Geo<LOGN, V>::RT)
     kb_row_c2r_growth(const WorldDesc* __restrict__ worlds, const WorkItem* __restrict__ items,
-                      int count) {
+                      int count, int* err) {
     extern __shared__ __align__(128) float2 smb_c2r[];
+    __shared__ __align__(8) uint64_t bar;
+    init_tile_barrier(&bar);
+    uint32_t phase = 0;
     for (int i = blockIdx.x; i < count; i += gridDim.x) {
         __syncthreads();
         const WorkItem it = items[i];
         const WorldDesc& w = worlds[it.world];
-        row_c2r_growth_body<LOGN, V>(w.U, w.A, w.tw, w.groups, w.gp, w.temp, nullptr, 0.f, it.c,
-                                     it.a, smb_c2r);
+        if (!row_c2r_growth_body<LOGN, V>(&w.umap[V == 0 ? 0 : 1], true, w.A, w.tw, w.groups, w.gp,
+                                          w.temp, nullptr, 0.f, it.c, it.a, smb_c2r, &bar, phase,
+                                          err))
+            return;   // a bounded wait timed out (uniform across the block)
     }
 }
 
@@ -235,8 +259,8 @@ cudaError_t launch_class_phase(cg_batch* b, const cg_batch::SizeClass& sc, int p
     args[0] = &worlds;
     args[1] = &items;
     args[2] = &count;
-    if (phase == 1) args[3] = &b->err;
-    else args[3] = &parity;   // (the c2r kernel takes only three)
+    if (phase == 1 || phase == 2) args[3] = &b->err;   // the bulk-copy phases
+    else args[3] = &parity;
     return cudaLaunchKernel(pv.fn, dim3(sc.grid[phase][v]), dim3(pv.threads), args, pv.smem, st);
 }
 
@@ -416,6 +440,10 @@ int cg_batch_create(int n_worlds, const int* n, const int* C, const int* K, cons
         d.tw = b->tw_by_logn[W.logn];
         d.groups = W.groups;
         d.gp = W.gp;
+        static_assert(kVariants == 3, "variants 1 and 2 share the row tile");
+        for (int m = 0; m < 2 && rc == CG_OK; ++m)
+            chk(encode_u_map(&d.umap[m], W.U, W.n, W.K, row_tile_rows(W.logn, m)),
+                "encoding a tensor map of U");
     }
     if (rc == CG_OK && chk(cudaMalloc(&b->d_worlds, sizeof(WorldDesc) * n_worlds), "cudaMalloc"))
         chk(cudaMemcpy(b->d_worlds, descs.data(), sizeof(WorldDesc) * n_worlds,

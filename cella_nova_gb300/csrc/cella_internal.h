@@ -1,5 +1,6 @@
 // cella_internal.h — types shared by the host orchestrator and the kernels.
 #pragma once
+#include <cuda.h>   // CUtensorMap (the encoder is reached through the runtime)
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -171,6 +172,9 @@ cudaError_t launch_f64_to_f32(const double* in, float* out, size_t count, cudaSt
 cudaError_t launch_mass_f64(const float* x, int C, size_t px, double* partial, int nblocks,
                             double* out, cudaStream_t s);
 cudaError_t launch_render(const float* x, int C, size_t px, unsigned* out, cudaStream_t s);
+// Tensor map over U (K kernels x n/2 rows kx x n float2 y, kx-major) for the
+// inverse row pass's 2-D tile loads: boxes of rb values of y by up to 256 kx.
+cudaError_t encode_u_map(CUtensorMap* map, const float2* U, int n, int K, int rb);
 cudaError_t launch_wait_check(int* err, int timeout_ms, cudaStream_t s);
 cudaError_t launch_rgb24(const unsigned* in, unsigned char* out, size_t px, cudaStream_t s);
 cudaError_t launch_fold_params(const float* mu, const float* sigma, const float* w, int C, int K,

@@ -154,15 +154,29 @@ __host__ __device__ constexpr int last_radix(int L, int MR = 16) {
 }
 
 // One Stockham pass (radix R, sub-transform size NS) over S sequences of
-// length L, with T threads.  Work item `item` = (sequence s, butterfly j);
-// thread t owns items t, t+T, ...  It loads v[r] = x[j + r*L/R], applies
+// length L, with T threads.  Work item `item` = (sequence s, butterfly j):
+// s = item / J, j = item % J, or with SFAST the sequence index runs fastest,
+// s = item % S, j = item / S (a warp then spans S sequences at the same few
+// butterflies, which suits inputs stored element-major, x[j][s]); thread t
+// owns items t, t+T, ...  It loads v[r] = x[j + r*L/R], applies
 // W_{NS*R}^{r*(j mod NS)}, runs DFT-R and stores v[q] at
 // (j div NS)*NS*R + (j mod NS) + q*NS.  All loads finish (barrier) before any
 // store, so in-place passes are safe; a second barrier closes the pass.
 //   twp : this pass's table (tw_offset layout).
 //   ld(s, i, it, q)         -> float2
 //   st(s, i, v, it, q)      (it, q) name the register slot of the value.
-template <int L, int R, int NS, bool INV, int T, int S, class LD, class ST>
+template <int S, int J, bool SFAST>
+__device__ __forceinline__ void item_pos(int item, int& s, int& j) {
+    if constexpr (SFAST) {
+        s = item % S;
+        j = item / S;
+    } else {
+        s = item / J;
+        j = item % J;
+    }
+}
+
+template <int L, int R, int NS, bool INV, int T, int S, bool SFAST = false, class LD, class ST>
 __device__ __forceinline__ void stockham_pass(LD& ld, ST& st, const float2* __restrict__ twp) {
     constexpr int J = L / R;
     constexpr int ITEMS = S * J;
@@ -172,7 +186,8 @@ __device__ __forceinline__ void stockham_pass(LD& ld, ST& st, const float2* __re
     for (int it = 0; it < IPT; ++it) {
         const int item = threadIdx.x + it * T;
         if (ITEMS % T == 0 || item < ITEMS) {
-            const int s = item / J, j = item % J;
+            int s, j;
+            item_pos<S, J, SFAST>(item, s, j);
             if constexpr (is_smem_rows<LD>::value) {
                 const float2* b = ld.buf + s * ld.pitch + pidx(j);
 #pragma unroll
@@ -188,7 +203,8 @@ __device__ __forceinline__ void stockham_pass(LD& ld, ST& st, const float2* __re
     for (int it = 0; it < IPT; ++it) {
         const int item = threadIdx.x + it * T;
         if (ITEMS % T == 0 || item < ITEMS) {
-            const int s = item / J, j = item % J;
+            int s, j;
+            item_pos<S, J, SFAST>(item, s, j);
             const int k = j % NS;
             if (NS > 1) {
 #pragma unroll
@@ -215,8 +231,10 @@ __device__ __forceinline__ void stockham_pass(LD& ld, ST& st, const float2* __re
 
 // Full length-L transform: first pass reads through `ld`, middle passes use
 // shared memory through smld/smst, the last pass writes through `stl`.
-// `tab` is the plan's twiddle table (tw_offset layout).
-template <int L, int NS, bool INV, int T, int S, bool REMFIRST = false, int MR = 16>
+// `tab` is the plan's twiddle table (tw_offset layout); SFAST selects the
+// item order of every pass (stockham_pass).
+template <int L, int NS, bool INV, int T, int S, bool REMFIRST = false, int MR = 16,
+          bool SFAST = false>
 struct FftPasses {
     template <class LD, class SMLD, class SMST, class STL>
     __device__ __forceinline__ static void run(LD& ld, SMLD& smld, SMST& smst, STL& stl,
@@ -224,10 +242,10 @@ struct FftPasses {
         constexpr int R = PassRadix<L, NS, REMFIRST, MR>::R;
         const float2* twp = tab + tw_offset(L, REMFIRST, NS, MR);
         if constexpr (NS * R == L) {
-            stockham_pass<L, R, NS, INV, T, S>(ld, stl, twp);
+            stockham_pass<L, R, NS, INV, T, S, SFAST>(ld, stl, twp);
         } else {
-            stockham_pass<L, R, NS, INV, T, S>(ld, smst, twp);
-            FftPasses<L, NS * R, INV, T, S, REMFIRST, MR>::run(smld, smld, smst, stl, tab);
+            stockham_pass<L, R, NS, INV, T, S, SFAST>(ld, smst, twp);
+            FftPasses<L, NS * R, INV, T, S, REMFIRST, MR, SFAST>::run(smld, smld, smst, stl, tab);
         }
     }
 };

@@ -325,6 +325,49 @@ cudaError_t launch_ring_grad(int n, int K, const RingSet& rs, const float* ring_
 }
 
 // ---------------------------------------------------------------------------
+// Tensor maps.  cuTensorMapEncodeTiled is a driver function; the runtime
+// hands out its address, so the library links no driver library itself.
+// U is viewed as a 2-D array of floats: rows = K * n/2 (kernel, kx), each
+// 2n floats (n float2 over y), so a box of 2 rb floats by R rows is the
+// tile (rb values of y) x (R values of kx) the inverse row pass needs,
+// landing kx-major in shared memory.
+// ---------------------------------------------------------------------------
+namespace {
+using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
+                                   const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
+                                   const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                   CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+EncodeTiledFn encode_tiled_fn() {
+    static EncodeTiledFn fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000,
+                                             cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiledFn>(p);
+    });
+    return fn;
+}
+}  // namespace
+
+cudaError_t encode_u_map(CUtensorMap* map, const float2* U, int n, int K, int rb) {
+    const EncodeTiledFn fn = encode_tiled_fn();
+    if (!fn) return cudaErrorNotSupported;
+    const int M = n / 2;
+    const cuuint64_t dims[2] = {cuuint64_t(2) * n, cuuint64_t(K) * M};
+    const cuuint64_t strides[1] = {cuuint64_t(n) * sizeof(float2)};
+    const cuuint32_t box[2] = {cuuint32_t(2 * rb), cuuint32_t(M < 256 ? M : 256)};
+    const cuuint32_t estr[2] = {1, 1};
+    const CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float2*>(U), dims,
+                          strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                          CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+}
+
+// ---------------------------------------------------------------------------
 // Check of the bounded-wait path: one CTA waits on an mbarrier that no copy
 // and no thread ever completes, through the same mbar_wait the step kernels
 // use, with a short limit.  The wait gives up, records the timeout in the

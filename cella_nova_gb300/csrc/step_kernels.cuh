@@ -51,7 +51,16 @@ struct Geo {
     static constexpr int ROW_MR = (V == 2) ? 8 : 16;
     static constexpr int RP = padded_len(M) + (RB >= 16 ? 1 : (RB == 8 ? 2 : 4));
     static constexpr size_t R2C_SMEM = size_t(RB) * RP * sizeof(float2);
-    static constexpr size_t C2R_SMEM = 2 * R2C_SMEM;    // double-buffered input
+    // Inverse row pass: the padded work rows, then one landing tile for a
+    // kernel's U tile (RB values of y by M values of kx, kx-major), filled by
+    // 2-D tensor copies of boxes of UBOX kx; 128-byte aligned.
+    static constexpr int UBOX = M < 256 ? M : 256;
+    static constexpr int C2R_LAND = (RB * RP + 15) & ~15;
+    static constexpr int C2R_TILE = RB * M;
+    static_assert((C2R_TILE * sizeof(float2)) % 128 == 0 && (RB * UBOX * sizeof(float2)) % 128 == 0,
+                  "tensor-copy destination alignment");
+    static constexpr size_t C2R_SMEM = (size_t(C2R_LAND) + size_t(C2R_TILE)) * sizeof(float2);
+    static_assert(C2R_SMEM <= 227 * 1024, "inverse row pass shared memory");
     // Column kernel: TW columns per CTA, CT threads; a padded work buffer
     // and an unpadded staging tile that bulk copies fill.  TW = 4096/N keeps
     // 256 butterflies per radix-16 pass (one per thread) at every size.
@@ -173,18 +182,18 @@ __global__ void __launch_bounds__(Geo<LOGN, V>::RT, 512 / Geo<LOGN, V>::RT) k_ro
 }
 
 // Run the first pass of a transform, then `hook()`, then the rest.
-template <int L, bool INV, int T, int S, bool REMFIRST, class LD, class SMLD, class SMST,
-          class STL, class HOOK>
+template <int L, bool INV, int T, int S, bool REMFIRST, int MR = 16, bool SFAST = false,
+          class LD, class SMLD, class SMST, class STL, class HOOK>
 __device__ __forceinline__ void fft_with_hook(LD& ld, SMLD& smld, SMST& smst, STL& stl,
                                               const float2* __restrict__ tab, HOOK hook) {
-    constexpr int R = PassRadix<L, 1, REMFIRST>::R;
+    constexpr int R = PassRadix<L, 1, REMFIRST, MR>::R;
     if constexpr (R == L) {
-        stockham_pass<L, R, 1, INV, T, S>(ld, stl, tab);
+        stockham_pass<L, R, 1, INV, T, S, SFAST>(ld, stl, tab);
         hook();
     } else {
-        stockham_pass<L, R, 1, INV, T, S>(ld, smst, tab);
+        stockham_pass<L, R, 1, INV, T, S, SFAST>(ld, smst, tab);
         hook();
-        FftPasses<L, R, INV, T, S, REMFIRST>::run(smld, smld, smst, stl, tab);
+        FftPasses<L, R, INV, T, S, REMFIRST, MR, SFAST>::run(smld, smld, smst, stl, tab);
     }
 }
 
@@ -337,33 +346,64 @@ __global__ void __launch_bounds__(Geo<LOGN, V>::CT, Geo<LOGN, V>::COL_MINB)
 // host-folded scale c2 = -log2(e) / (2 sigma^2).
 // C2R: Z[m] = E + i O, E = X[m] + conj X[M-m], O = (X[m] - conj X[M-m]) W_N^-m,
 // z = IFFT_M(Z) = (x[2j], x[2j+1]).
-// The next kernel's U tile is gathered (a transpose, per-element cp.async)
-// into the second buffer while the current one is transformed.
+// The tile of U[k] a CTA needs (RB values of y for every kx; U is kx-major)
+// arrives by 2-D tensor copies (TMA): the transpose happens in the copy
+// engine, the tile lands kx-major (element (kx, s) at kx * RB + s) and an
+// mbarrier tracks it.  The next kernel's tile is issued into the same
+// landing tile as soon as the first FFT pass has read it, and lands while
+// the remaining passes and the growth run.  The FFT runs with the row
+// index fastest (SFAST), so a warp's first-pass reads from the landing tile
+// are contiguous and its exchanges through the padded work rows stay free
+// of bank conflicts.  `umap` is encode_u_map's map of U (kernel parameter
+// space, or global memory with `umap_global`).
+// Returns false if a bounded wait timed out (the error word is set).  `bar`
+// is an initialised mbarrier owned by the caller and `phase` counts its
+// completed phases, so one CTA can run many tiles back to back.
 // grid (N/RB, C), block RT.
 // ---------------------------------------------------------------------------
 template <int LOGN, int V = 0>
-__device__ __forceinline__ void row_c2r_growth_body(const float2* __restrict__ U,
+__device__ __forceinline__ bool row_c2r_growth_body(const CUtensorMap* umap, bool umap_global,
                                                     float* __restrict__ A,
                                                     const float2* __restrict__ tw,
                                                     const KernelGroups& groups,
                                                     const GrowthParams& gp, float temp,
                                                     float* __restrict__ udbg, float udbg_scale,
-                                                    int c, int y0, float2* sm) {
+                                                    int c, int y0, float2* sm, uint64_t* barp,
+                                                    uint32_t& phase, int* err) {
     using G = Geo<LOGN, V>;
-    constexpr int RL = last_radix(G::M, G::ROW_MR);
-    constexpr int JL = G::M / RL;
-    constexpr int ITEMS = G::RB * JL;
+    constexpr int M = G::M, RB = G::RB;
+    constexpr int RL = last_radix(M, G::ROW_MR);
+    constexpr int JL = M / RL;
+    constexpr int ITEMS = RB * JL;
     constexpr int IPT = (ITEMS + G::RT - 1) / G::RT;
-    constexpr int BUF = G::RB * G::RP;
+    constexpr uint32_t kTileBytes = uint32_t(G::C2R_TILE) * sizeof(float2);
+    static_assert(G::RT % RB == 0, "a thread keeps one row in every pass");
     const int cnt = groups.out_count[c], base = groups.out_start[c];
+    float2* land = sm + G::C2R_LAND;
+    uint64_t& bar = *barp;
+    if (umap_global && threadIdx.x == 0) tensormap_acquire(umap);
 
-    auto gather = [&](int gi, float2* buf) {
+    auto issue = [&](int gi) {   // all threads call; thread 0 copies
         const int k = groups.out_idx[base + gi];
-        const float2* src = U + size_t(k) * G::M * G::N + y0;
-        for_row_tile<LOGN, V>([&](int s, int kx, int pk) {
-            cp_async8(&buf[s * G::RP + pk], &src[size_t(kx) * G::N + s]);
-        });
-        cp_async_commit();
+        fence_proxy_async_smem();
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            mbar_arrive_expect_tx(&bar, kTileBytes);
+#pragma unroll
+            for (int q = 0; q < M / G::UBOX; ++q)
+                tensor2d_g2s(land + q * G::UBOX * RB, umap, 2 * y0, k * M + q * G::UBOX, &bar);
+        }
+    };
+    auto wait_tile = [&]() -> bool {
+        const bool ok = mbar_wait(&bar, phase & 1u, err);
+        if (__syncthreads_or(!ok)) {
+            // give the copy in flight one more bounded chance to land before
+            // this CTA's shared memory is released
+            mbar_wait(&bar, phase & 1u, nullptr);
+            return false;
+        }
+        ++phase;
+        return true;
     };
 
     float2 acc[IPT][RL];
@@ -372,25 +412,20 @@ __device__ __forceinline__ void row_c2r_growth_body(const float2* __restrict__ U
 #pragma unroll
         for (int r = 0; r < RL; ++r) acc[it][r] = make_float2(0.f, 0.f);
 
-    if (cnt > 0) gather(0, sm);
+    // this thread's row: the same in every pass (RT is a multiple of RB)
+    const int srow = threadIdx.x % RB;
+    SmemRows rows{sm, G::RP};
+    if (cnt > 0) issue(0);
     for (int gi = 0; gi < cnt; ++gi) {
-        float2* buf = sm + (gi & 1) * BUF;
-        if (gi + 1 < cnt) {
-            gather(gi + 1, sm + ((gi + 1) & 1) * BUF);
-            cp_async_wait<1>();
-        } else {
-            cp_async_wait<0>();
-        }
-        __syncthreads();
-        SmemRows rows{buf, G::RP};
-        auto ld0 = [&](int s, int m, int, int) -> float2 {
-            const float2* row = buf + s * G::RP;
+        if (!wait_tile()) return false;
+        const float2* lt = land + srow;   // lt[kx * RB]
+        auto ld0 = [&](int, int m, int, int) -> float2 {
             if (m == 0) {
-                const float2 x = row[0];
+                const float2 x = lt[0];
                 return make_float2(x.x + x.y, x.x - x.y);
             }
-            const float2 a = row[pidx(m)];
-            const float2 b = cconj(row[pidx(G::M - m)]);
+            const float2 a = lt[m * RB];
+            const float2 b = cconj(lt[(M - m) * RB]);
             const float2 E = cadd(a, b);
             const float2 O = cmulc(csub(a, b), __ldg(&tw[m]));
             return make_float2(E.x - O.y, E.y + O.x);
@@ -409,7 +444,10 @@ __device__ __forceinline__ void row_c2r_growth_body(const float2* __restrict__ U
                     make_float2(v.x * udbg_scale, v.y * udbg_scale);
             }
         };
-        FftPasses<G::M, 1, true, G::RT, G::RB, false, G::ROW_MR>::run(ld0, rows, rows, gst, tw + G::TW_ROW);
+        fft_with_hook<M, true, G::RT, RB, false, G::ROW_MR, true>(
+            ld0, rows, rows, gst, tw + G::TW_ROW, [&]() {
+                if (gi + 1 < cnt) issue(gi + 1);   // the first pass has read the tile
+            });
     }
 
     float* Ac = A + (size_t(c) * G::N + y0) * G::N;
@@ -418,7 +456,8 @@ __device__ __forceinline__ void row_c2r_growth_body(const float2* __restrict__ U
     for (int it = 0; it < IPT; ++it) {
         const int item = threadIdx.x + it * G::RT;
         if (ITEMS % G::RT == 0 || item < ITEMS) {
-            const int s = item / JL, j = item % JL;
+            int s, j;
+            item_pos<RB, JL, true>(item, s, j);
 #pragma unroll
             for (int r = 0; r < RL; ++r) {
                 const int i = j + r * JL;
@@ -428,19 +467,24 @@ __device__ __forceinline__ void row_c2r_growth_body(const float2* __restrict__ U
             }
         }
     }
+    return true;
 }
 
 template <int LOGN, int V = 0>
-__global__ void __launch_bounds__(Geo<LOGN, V>::RT, 512 / Geo<LOGN, V>::RT) k_row_c2r_growth(const float2* __restrict__ U,
+__global__ void __launch_bounds__(Geo<LOGN, V>::RT, 512 / Geo<LOGN, V>::RT) k_row_c2r_growth(const __grid_constant__ CUtensorMap umap,
                                                          float* __restrict__ A,
                                                          const float2* __restrict__ tw,
                                                          const __grid_constant__ KernelGroups groups,
                                                          const GrowthParams* __restrict__ gp,
                                                          float temp, float* __restrict__ udbg,
-                                                         float udbg_scale, int cbase) {
+                                                         float udbg_scale, int* err, int cbase) {
     extern __shared__ __align__(128) float2 sm_c2r[];
-    row_c2r_growth_body<LOGN, V>(U, A, tw, groups, *gp, temp, udbg, udbg_scale,
-                                 blockIdx.y + cbase, blockIdx.x * Geo<LOGN, V>::RB, sm_c2r);
+    __shared__ __align__(8) uint64_t bar;
+    init_tile_barrier(&bar);
+    uint32_t phase = 0;
+    row_c2r_growth_body<LOGN, V>(&umap, false, A, tw, groups, *gp, temp, udbg, udbg_scale,
+                                 blockIdx.y + cbase, blockIdx.x * Geo<LOGN, V>::RB, sm_c2r, &bar,
+                                 phase, err);
 }
 
 // ---------------------------------------------------------------------------
@@ -847,10 +891,14 @@ void launch_col(const StepArgs& a, int c_lo, int nc, cudaStream_t st) {
         a.rowspec, a.kspec, a.U, a.tw, a.groups, a.err, c_lo);
 }
 template <int LOGN, int V>
-void launch_c2r(const StepArgs& a, int c_lo, int nc, cudaStream_t st) {
+cudaError_t launch_c2r(const StepArgs& a, int c_lo, int nc, cudaStream_t st) {
     using G = Geo<LOGN, V>;
+    CUtensorMap umap;   // passed by value: a graph capture keeps its own copy
+    const cudaError_t e = encode_u_map(&umap, a.U, G::N, a.K, G::RB);
+    if (e != cudaSuccess) return e;
     k_row_c2r_growth<LOGN, V><<<dim3(G::N / G::RB, nc), G::RT, G::C2R_SMEM, st>>>(
-        a.U, a.A, a.tw, a.groups, a.gp, a.temp, a.udbg, float(G::N) * float(G::N), c_lo);
+        umap, a.A, a.tw, a.groups, a.gp, a.temp, a.udbg, float(G::N) * float(G::N), a.err, c_lo);
+    return cudaSuccess;
 }
 template <int LOGN, int V>
 void launch_diff(const StepArgs& a, int c_lo, int nc, cudaStream_t st) {
@@ -876,7 +924,15 @@ cudaError_t launch_step_range(const StepArgs& a, int phases, int c_lo, int c_hi,
     if (nc <= 0) return cudaSuccess;
     if (phases & kPhaseRowFwd) { CG_VARIANT_SWITCH(a.var.r2c, launch_r2c, a, c_lo, nc, st) }
     if (phases & kPhaseColConv) { CG_VARIANT_SWITCH(a.var.col, launch_col, a, c_lo, nc, st) }
-    if (phases & kPhaseGrowth) { CG_VARIANT_SWITCH(a.var.c2r, launch_c2r, a, c_lo, nc, st) }
+    if (phases & kPhaseGrowth) {
+        cudaError_t e;
+        switch (a.var.c2r) {
+            case 1: e = launch_c2r<LOGN, 1>(a, c_lo, nc, st); break;
+            case 2: e = launch_c2r<LOGN, 2>(a, c_lo, nc, st); break;
+            default: e = launch_c2r<LOGN, 0>(a, c_lo, nc, st); break;
+        }
+        if (e != cudaSuccess) return e;
+    }
     if (phases & kPhaseDiffusion) { CG_VARIANT_SWITCH(a.var.diff, launch_diff, a, c_lo, nc, st) }
     return cudaGetLastError();
 }
