@@ -78,6 +78,8 @@ SIGNATURES = {
     "cg_render_ptr": ([_P, ctypes.POINTER(_P)], _I),
     "cg_stream_frames": ([_P, _I, _I, _I], _I),
     "cg_check_bounded_wait": ([_P, _I], _I),
+    "cg_step_host_async": ([_P, _DP, _FP, _I], _I),
+    "cg_host_wait": ([_P], _I),
     "cg_step_from": ([_P, _P, _P], _I),
     "cg_step_backward": ([_P, _P, _P, _P, _P, _P], _I),
     "cg_kernel_grad_spatial": ([_P, _P, _P], _I),

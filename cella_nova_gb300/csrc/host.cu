@@ -166,6 +166,19 @@ void build_groups(int C, int K, const uint32_t* c0, const uint32_t* c1, const fl
 
 using namespace cg;
 
+// Host-buffer pipeline of cg_step_host_async: uploads on `up` into one of two
+// staging buffers, conversion and steps on the sim's stream, downloads on
+// `down`.
+struct HostPipe {
+    cudaStream_t up = nullptr, down = nullptr;
+    double* stage[2] = {nullptr, nullptr};   // C * n * n f64 each
+    cudaEvent_t up_done[2] = {nullptr, nullptr};
+    cudaEvent_t conv_done[2] = {nullptr, nullptr};
+    cudaEvent_t step_done = nullptr, down_done = nullptr;
+    int slot = 0;
+    bool ready = false;
+};
+
 struct cg_sim {
     int n = 0, logn = 0, C = 0, K = 0;
     float temp = 1.f;
@@ -196,6 +209,7 @@ struct cg_sim {
     double* ring_s = nullptr;         // K * kMaxRings per-ring sums of the last build
     double* zsum = nullptr;           // K normalisers of the last build
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    HostPipe pipe;
     KernelGroups groups{};
     GrowthParams gp{};          // host copies of the folded parameters
     AdjointParams ap{};
@@ -269,6 +283,13 @@ void release(cg_sim* s) {
     cudaFree(s->seg_cache);
     cudaFree(s->utmp[0]);
     cudaFree(s->utmp[1]);
+    HostPipe& p = s->pipe;
+    for (auto* st : {p.up, p.down})
+        if (st) cudaStreamDestroy(st);
+    for (auto* b : p.stage) cudaFree(b);
+    for (auto* e : {p.up_done[0], p.up_done[1], p.conv_done[0], p.conv_done[1], p.step_done,
+                    p.down_done})
+        if (e) cudaEventDestroy(e);
     if (s->own_stream && s->stream) cudaStreamDestroy(s->stream);
     delete s;
 }
@@ -742,6 +763,80 @@ int cg_download_channels(cg_sim* s, float* out) {
                              cudaMemcpyDeviceToHost, s->stream),
              "downloading channels");
     CG_CHECK(cudaStreamSynchronize(s->stream), "cudaStreamSynchronize");
+    CG_SYNC_CHECK(s);
+    return CG_OK;
+}
+
+// Page-locked host memory (cudaHostAlloc / cudaHostRegister): the pipeline's
+// copies must not block on a pageable staging copy.
+static bool page_locked(const void* ptr) {
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, ptr) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeHost;
+}
+
+static int ensure_pipe(cg_sim* s) {
+    HostPipe& p = s->pipe;
+    if (p.ready) return CG_OK;
+    const size_t bytes = sizeof(double) * s->C * s->px();
+    if (!p.up) CG_CHECK(cudaStreamCreateWithFlags(&p.up, cudaStreamNonBlocking), "creating a stream");
+    if (!p.down)
+        CG_CHECK(cudaStreamCreateWithFlags(&p.down, cudaStreamNonBlocking), "creating a stream");
+    for (auto& b : p.stage)
+        if (!b) CG_CHECK(cudaMalloc(&b, bytes), "cudaMalloc(host pipeline staging)");
+    for (auto* e : {&p.up_done[0], &p.up_done[1], &p.conv_done[0], &p.conv_done[1], &p.step_done,
+                    &p.down_done})
+        if (!*e) CG_CHECK(cudaEventCreateWithFlags(e, cudaEventDisableTiming), "creating an event");
+    p.ready = true;
+    return CG_OK;
+}
+
+int cg_step_host_async(cg_sim* s, const double* in, float* out, int nsteps) {
+    if (!s || !in || !out) return fail(CG_ERR_ARG, "cg_step_host_async: NULL argument");
+    if (nsteps < 0) return fail(CG_ERR_ARG, "negative step count %d", nsteps);
+    if (!page_locked(in) || !page_locked(out))
+        return fail(CG_ERR_ARG, "cg_step_host_async: host buffers must be page-locked "
+                                "(cudaHostAlloc or cudaHostRegister)");
+    int rc = ensure_pipe(s);
+    if (rc != CG_OK) return rc;
+    HostPipe& p = s->pipe;
+    const int b = p.slot;
+    p.slot ^= 1;
+    const size_t count = size_t(s->C) * s->px();
+    // upload into staging slot b once the conversion of two calls ago has read it
+    CG_CHECK(cudaStreamWaitEvent(p.up, p.conv_done[b], 0), "cudaStreamWaitEvent");
+    CG_CHECK(cudaMemcpyAsync(p.stage[b], in, sizeof(double) * count, cudaMemcpyHostToDevice, p.up),
+             "uploading channels");
+    CG_CHECK(cudaEventRecord(p.up_done[b], p.up), "cudaEventRecord");
+    // convert and step in the sim's stream (already ordered after the
+    // previous call's download)
+    CG_CHECK(cudaStreamWaitEvent(s->stream, p.up_done[b], 0), "cudaStreamWaitEvent");
+    CG_CHECK(launch_f64_to_f32(p.stage[b], s->state[s->cur], count, s->stream),
+             "converting channels");
+    CG_CHECK(cudaEventRecord(p.conv_done[b], s->stream), "cudaEventRecord");
+    rc = cg_step(s, nsteps);
+    if (rc != CG_OK) return rc;
+    CG_CHECK(cudaEventRecord(p.step_done, s->stream), "cudaEventRecord");
+    // download, then order everything later in the sim's stream after it
+    CG_CHECK(cudaStreamWaitEvent(p.down, p.step_done, 0), "cudaStreamWaitEvent");
+    CG_CHECK(cudaMemcpyAsync(out, s->state[s->cur], sizeof(float) * count, cudaMemcpyDeviceToHost,
+                             p.down),
+             "downloading channels");
+    CG_CHECK(cudaEventRecord(p.down_done, p.down), "cudaEventRecord");
+    CG_CHECK(cudaStreamWaitEvent(s->stream, p.down_done, 0), "cudaStreamWaitEvent");
+    return CG_OK;
+}
+
+int cg_host_wait(cg_sim* s) {
+    if (!s) return fail(CG_ERR_ARG, "cg_host_wait: NULL handle");
+    CG_CHECK(cudaStreamSynchronize(s->stream), "cudaStreamSynchronize");
+    if (s->pipe.ready) {
+        CG_CHECK(cudaStreamSynchronize(s->pipe.down), "cudaStreamSynchronize");
+        CG_CHECK(cudaStreamSynchronize(s->pipe.up), "cudaStreamSynchronize");
+    }
     CG_SYNC_CHECK(s);
     return CG_OK;
 }

@@ -174,6 +174,23 @@ class GpuMaceLenia:
         written (main.rs:239-303's loop, to a file or a pipe)."""
         check(self._lib.cg_stream_frames(self._h, int(fd), int(nframes), int(steps_per_frame)))
 
+    def step_host_async(self, host_in, host_out, nsteps: int = 1):
+        """Upload all channels from host_in (C*n*n float64), run nsteps steps
+        and download the state into host_out (C*n*n float32), pipelined with
+        the calls before and after it; returns at once.  Both arrays must be
+        page-locked (e.g. numpy views of torch pin_memory tensors) and stay
+        untouched until host_wait()."""
+        for a, dt in ((host_in, np.float64), (host_out, np.float32)):
+            if a.dtype != dt or a.size != self.num_channels * self.total_elements \
+                    or not a.flags["C_CONTIGUOUS"]:
+                raise ValueError(f"expected a contiguous {np.dtype(dt).name} array of "
+                                 f"{self.num_channels * self.total_elements} values")
+        check(self._lib.cg_step_host_async(self._h, dptr(host_in), fptr(host_out), int(nsteps)))
+
+    def host_wait(self):
+        """Wait for every step_host_async enqueued so far."""
+        check(self._lib.cg_host_wait(self._h))
+
     def check_bounded_wait(self, timeout_ms: int = 20):
         """Run the failure-path check: a kernel whose device-side wait can
         never complete gives up after timeout_ms and records the timeout.

@@ -123,6 +123,22 @@ int cg_download_render(cg_sim* sim, uint8_t* rgb24);
  * Blocking; CG_ERR_IO if a write fails. */
 int cg_stream_frames(cg_sim* sim, int fd, int nframes, int steps_per_frame);
 
+/* Host buffers in, host buffers out, pipelined: enqueue the upload of `in`
+ * (C*n*n f64, what cg_upload_channel takes, all channels), nsteps steps and
+ * the download of the resulting state to `out` (C*n*n f32, as
+ * cg_download_channels gives it), and return without waiting.  Uploads run
+ * on a copy stream into one of two staging buffers, so the upload of the next
+ * call overlaps this call's steps and download; the link carries both
+ * directions at once.  Replaces a loop of upload_channel / run_steps /
+ * download_all_channels (ml-rs/orchestrator/mod.rs:217-263) where the host
+ * feeds many inputs.  `in` and `out` must be page-locked (cudaHostAlloc or
+ * cudaHostRegister; CG_ERR_ARG otherwise) and stay untouched until
+ * cg_host_wait.  Later calls on the handle are ordered after the download. */
+int cg_step_host_async(cg_sim* sim, const double* in, float* out, int nsteps);
+/* Wait for every cg_step_host_async enqueued so far (and the handle's
+ * stream); reports a device-side timeout like the other synchronising calls. */
+int cg_host_wait(cg_sim* sim);
+
 /* Failure-path check: runs a kernel whose bounded device-side wait can never
  * complete (an mbarrier nothing arrives on), through the same wait the step
  * kernels use but limited to timeout_ms (1..2000).  The kernel gives up and
