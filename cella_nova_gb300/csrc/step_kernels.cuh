@@ -343,7 +343,8 @@ __global__ void __launch_bounds__(Geo<LOGN, V>::CT, Geo<LOGN, V>::COL_MINB)
 //   g = 2 exp(-(u-mu)^2 / (2 sigma^2)) - 1,  acc += w g;
 // then A[c] = exp(temp * acc) (diffusion.rs:58-66 applies temp inside exp).
 // The exponential of the bump is ex2.approx (a few ulp, like expf) on a
-// host-folded scale c2 = -log2(e) / (2 sigma^2).
+// host-folded scale c2 = -log2(e) / (2 sigma^2); so is A, as
+// 2^(temp log2(e) acc - temp log2(e) sum(w)) with one fma for the argument.
 // C2R: Z[m] = E + i O, E = X[m] + conj X[M-m], O = (X[m] - conj X[M-m]) W_N^-m,
 // z = IFFT_M(Z) = (x[2j], x[2j+1]).
 // The tile of U[k] a CTA needs (RB values of y for every kx; U is kx-major)
@@ -451,7 +452,8 @@ __device__ __forceinline__ bool row_c2r_growth_body(const CUtensorMap* umap, boo
     }
 
     float* Ac = A + (size_t(c) * G::N + y0) * G::N;
-    const float wsum = gp.wsum[c];
+    const float tl = temp * 1.44269504088896341f;   // temp log2(e)
+    const float toff = -tl * gp.wsum[c];
 #pragma unroll
     for (int it = 0; it < IPT; ++it) {
         const int item = threadIdx.x + it * G::RT;
@@ -462,8 +464,8 @@ __device__ __forceinline__ bool row_c2r_growth_body(const CUtensorMap* umap, boo
             for (int r = 0; r < RL; ++r) {
                 const int i = j + r * JL;
                 reinterpret_cast<float2*>(Ac + size_t(s) * G::N)[i] =
-                    make_float2(expf(temp * (acc[it][r].x - wsum)),
-                                expf(temp * (acc[it][r].y - wsum)));
+                    make_float2(ex2_approx(fmaf(tl, acc[it][r].x, toff)),
+                                ex2_approx(fmaf(tl, acc[it][r].y, toff)));
             }
         }
     }
