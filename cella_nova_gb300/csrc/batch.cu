@@ -28,9 +28,9 @@ constexpr int kBatchMinLogN = 6;   // 64^2 .. 2048^2 in one batch
 constexpr int kBatchMaxLogN = 11;
 
 struct WorldDesc {
-    // tensor maps of U for the inverse row pass's tile copies: [0] with
-    // variant 0's rows per tile, [1] with variants 1 and 2's
-    CUtensorMap umap[2];
+    // tensor maps of U for the inverse row pass's tile copies, one per
+    // variant (rows per tile)
+    CUtensorMap umap[3];
     int logn, C, K;
     float temp;
     float* state[2];
@@ -46,7 +46,7 @@ struct WorldDesc {
 // Rows per inverse-row-pass tile of a size and variant (Geo<LOGN, V>::RB).
 template <int LOGN>
 int row_tile_rows(int v) {
-    return v == 0 ? Geo<LOGN, 0>::RB : Geo<LOGN, 1>::RB;
+    return v == 0 ? Geo<LOGN, 0>::RB : (v == 1 ? Geo<LOGN, 1>::RB : Geo<LOGN, 2>::RB);
 }
 int row_tile_rows(int logn, int v) {
     switch (logn) {
@@ -114,7 +114,7 @@ __global__ void __launch_bounds__(Geo<LOGN, V>::RT, 512 / Geo<LOGN, V>::RT)
         __syncthreads();
         const WorkItem it = items[i];
         const WorldDesc& w = worlds[it.world];
-        if (!row_c2r_growth_body<LOGN, V>(&w.umap[V == 0 ? 0 : 1], true, w.A, w.tw, w.groups, w.gp,
+        if (!row_c2r_growth_body<LOGN, V>(&w.umap[V], true, w.A, w.tw, w.groups, w.gp,
                                           w.temp, nullptr, 0.f, it.c, it.a, smb_c2r, &bar, phase,
                                           err))
             return;   // a bounded wait timed out (uniform across the block)
@@ -440,8 +440,8 @@ int cg_batch_create(int n_worlds, const int* n, const int* C, const int* K, cons
         d.tw = b->tw_by_logn[W.logn];
         d.groups = W.groups;
         d.gp = W.gp;
-        static_assert(kVariants == 3, "variants 1 and 2 share the row tile");
-        for (int m = 0; m < 2 && rc == CG_OK; ++m)
+        static_assert(kVariants == 3, "one map per variant");
+        for (int m = 0; m < kVariants && rc == CG_OK; ++m)
             chk(encode_u_map(&d.umap[m], W.U, W.n, W.K, row_tile_rows(W.logn, m)),
                 "encoding a tensor map of U");
     }

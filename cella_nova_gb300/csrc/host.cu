@@ -100,8 +100,6 @@ void build_twiddle_tables(int n, float2* out) {
     fill_plan(n, true, 16, p);
     p += tw_size(n, true);
     fill_plan(n / 2, false, 16, p);
-    p += tw_size(n / 2, false);
-    fill_plan(n / 2, false, 8, p);
 }
 
 static bool finite(float v) { return std::isfinite(v); }

@@ -28,28 +28,27 @@
 namespace cg {
 
 // Geometry of one grid size.  V selects a variant of the CTA shapes (the
-// autotuner times them): row kernels V=1 halve the rows per CTA and the
-// threads; the column kernel V=1 halves and V=2 doubles the columns and the
-// threads per CTA (work per thread is unchanged); diffusion V=1/V=2 use
-// 16 / 64 tile rows instead of 32.  Layouts in memory do not depend on V.
+// autotuner times them): row kernels V=1 / V=2 halve / quarter the rows per
+// CTA and the threads; the column kernel V=1 halves and V=2 doubles the
+// columns and the threads per CTA (work per thread is unchanged); diffusion
+// V=1/V=2 use 16 / 64 tile rows instead of 32.  Layouts in memory do not
+// depend on V, and every variant computes the same bits.
 template <int LOGN, int V = 0>
 struct Geo {
     static constexpr int N = 1 << LOGN;
     static constexpr int M = N / 2;
-    // Row kernels: RB rows per CTA, RT threads.  The row pitch RP keeps the
-    // kx-major transposes conflict-free: odd for RB >= 16 (a half-warp reads
-    // 16 rows of one column), 2 mod 16 for RB = 8 (8 rows x 2 columns),
-    // 4 mod 16 for RB = 4.
-    // Variant 2 of the row passes is variant 1's shape with radix-8 FFT
-    // passes (ROW_MR): one more pass through shared memory, half the values
-    // per butterfly in registers.  It rounds differently from the radix-16
-    // plans (the other variants of every phase compute the same bits).
+    // Row kernels: RB rows per CTA, RT threads, radix-16 plans (ROW_MR).  The
+    // row pitch RP keeps the accesses of a half-warp that spans the rows
+    // (kx-major transposes, and the row-fastest passes of the inverse row
+    // pass) conflict-free: odd for RB >= 16 (16 rows of one column), 2 mod 16
+    // for RB = 8 (8 rows x 2 columns), 4 mod 16 for RB = 4, 8 mod 16 for
+    // RB = 2 (2 rows x 8 columns).
     static constexpr int RB0 = 8192 / M;
     static constexpr int RB1 = RB0 < 8 ? 8 : (RB0 > N ? N : RB0);
-    static constexpr int RB = (V >= 1 && RB1 > 4) ? RB1 / 2 : RB1;
-    static constexpr int RT = (V >= 1) ? 256 : 512;
-    static constexpr int ROW_MR = (V == 2) ? 8 : 16;
-    static constexpr int RP = padded_len(M) + (RB >= 16 ? 1 : (RB == 8 ? 2 : 4));
+    static constexpr int RB = (V == 1) ? RB1 / 2 : (V == 2 ? RB1 / 4 : RB1);
+    static constexpr int RT = (V == 0) ? 512 : (V == 1 ? 256 : 128);
+    static constexpr int ROW_MR = 16;
+    static constexpr int RP = padded_len(M) + (RB >= 16 ? 1 : (RB == 8 ? 2 : (RB == 4 ? 4 : 8)));
     static constexpr size_t R2C_SMEM = size_t(RB) * RP * sizeof(float2);
     // Inverse row pass: the padded work rows, then one landing tile for a
     // kernel's U tile (RB values of y by M values of kx, kx-major), filled by
@@ -81,14 +80,11 @@ struct Geo {
     static_assert((KSOFF * sizeof(float2)) % 16 == 0, "bulk-copy destination alignment");
     static constexpr size_t COL_SMEM = (size_t(KSOFF) + size_t(TW) * N) * sizeof(float2);
     // Twiddle buffer: W_N^m (m < N), then the pass tables of the column
-    // forward plan, the column inverse plan, the row plan and the radix-8
-    // row plan; TW_ROWV is this variant's row table.
+    // forward plan, the column inverse plan and the row plan.
     static constexpr int TW_COL_FWD = N;
     static constexpr int TW_COL_INV = TW_COL_FWD + tw_size(N, false);
-    static constexpr int TW_ROW16 = TW_COL_INV + tw_size(N, true);
-    static constexpr int TW_ROW8 = TW_ROW16 + tw_size(M, false);
-    static constexpr int TW_TOTAL = TW_ROW8 + tw_size(M, false, 8);
-    static constexpr int TW_ROW = (ROW_MR == 8) ? TW_ROW8 : TW_ROW16;
+    static constexpr int TW_ROW = TW_COL_INV + tw_size(N, true);
+    static constexpr int TW_TOTAL = TW_ROW + tw_size(M, false);
     // Diffusion tile.
     static constexpr int TX = N < 64 ? N : 64;
     static constexpr int TY0 = (V == 1) ? 16 : (V == 2 ? 64 : 32);

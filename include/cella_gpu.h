@@ -176,9 +176,7 @@ int cg_timed_iterate(cg_sim* sim, double ms[4]);
 /* Autotuner (no reference counterpart).  Each phase has three variants:
  * CTA shapes (rows per CTA and threads for the row FFTs, columns per CTA and
  * threads for the column pass, tile rows and columns per thread for
- * diffusion) and, for the row FFTs, the FFT radix (variant 2: radix-8
- * passes, the others radix 16).  All variants give bit-identical results
- * except the radix-8 row plan, which differs by FP32 rounding (about 1e-7).
+ * diffusion).  All variants give bit-identical results.
  * cg_autotune times every variant of every phase
  * `reps` times on the live handle (the state is not advanced), keeps the
  * fastest per phase and re-captures the step graphs.  ms_out[12]

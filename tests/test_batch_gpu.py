@@ -67,8 +67,7 @@ def test_batch_rejects_bad_world():
 
 def test_batch_autotune_keeps_the_results():
     """The batch's autotuner picks per grid side among variants that agree
-    (bit for bit, or within FP32 rounding for the radix-8 row plan), and does
-    not step the worlds."""
+    bit for bit, and does not step the worlds."""
     crs = mixed_creatures()
     with GpuMaceLeniaBatch(crs) as a, GpuMaceLeniaBatch(crs) as b:
         x0 = [b.state(i) for i in range(len(crs))]
@@ -81,4 +80,4 @@ def test_batch_autotune_keeps_the_results():
         a.run_steps(4)
         b.run_steps(4)
         for i in range(len(crs)):
-            assert np.abs(b.state(i) - a.state(i)).max() <= 1e-5, i
+            np.testing.assert_array_equal(b.state(i), a.state(i), err_msg=str(i))

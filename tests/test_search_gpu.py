@@ -96,8 +96,7 @@ def test_mse_grad_and_loss():
 def test_graph_replays_equal_eager_iterations_and_conserve_mass():
     crs, tgs = candidates(64, 3, 3)
     adam = AdamConfig(lr_seed=1e-2, lr_params=1e-3, lr_rings=1e-2)
-    # untuned (both on the same variants): two tunings could pick FFT plans of
-    # different radix, which round differently
+    # untuned: both on the same variants, and no tuning time in the test
     with GradientSearch(crs, tgs, T=8, every=4, adam=adam, n_streams=2, autotune=False) as a, \
             GradientSearch(crs, tgs, T=8, every=4, adam=adam, n_streams=2, autotune=False) as b:
         a.run(5)          # one eager iteration, then four replays of the captured graph
