@@ -154,8 +154,8 @@ void fill_variant(PhaseVariant (&pv)[4][kVariants]) {
     pv[1][V] = {reinterpret_cast<const void*>(kb_col_conv<LOGN, V>), G::CT, G::COL_SMEM, G::TW, 0};
     pv[2][V] = {reinterpret_cast<const void*>(kb_row_c2r_growth<LOGN, V>), G::RT, G::C2R_SMEM,
                 G::RB, 0};
-    pv[3][V] = {reinterpret_cast<const void*>(kb_diffusion<LOGN, V>), D::THREADS, D::SMEM, G::TX,
-                G::TY};
+    pv[3][V] = {reinterpret_cast<const void*>(kb_diffusion<LOGN, V>), D::THREADS, D::SMEM, D::TX,
+                D::TY};
 }
 template <int LOGN>
 void fill_size(PhaseVariant (&pv)[4][kVariants]) {

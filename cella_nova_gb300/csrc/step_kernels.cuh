@@ -31,8 +31,10 @@ namespace cg {
 // autotuner times them): row kernels V=1 / V=2 halve / quarter the rows per
 // CTA and the threads; the column kernel V=1 halves and V=2 doubles the
 // columns and the threads per CTA (work per thread is unchanged); diffusion
-// V=1/V=2 use 16 / 64 tile rows instead of 32.  Layouts in memory do not
-// depend on V, and every variant computes the same bits.
+// V=1 keeps its sums in registers (DiffGeoReg) and V=2 uses 64 tile rows
+// with two columns per thread instead of 32 rows (the diffusion adjoint
+// takes V=1 as 16 tile rows).  Layouts in memory do not depend on V, and
+// every variant computes the same bits.
 template <int LOGN, int V = 0>
 struct Geo {
     static constexpr int N = 1 << LOGN;
@@ -789,12 +791,124 @@ __device__ __forceinline__ void diffusion_pair_body(const float* __restrict__ A,
     }
 }
 
-// Variant 2 of the diffusion phase is the column-pair body.
+// The same arithmetic without shared memory: a thread owns 4 adjacent columns
+// and walks down TYR rows.  Per row it loads A at its columns +-2 and the
+// state at +-1 with three 16-byte loads each (the side ones overlap its
+// neighbours' and hit L1), splits A into heads and tails, and keeps the
+// horizontal 3-sums of the last three rows (heads, tails, q) in registers;
+// the vertical sums come from those slots.  Every sum keeps the order of
+// diffusion2_body, so the bits are the same.  A CTA is RS strips of TX/4
+// threads: TX columns by RS * TYR rows.
+template <int LOGN>
+struct DiffGeoReg {
+    static constexpr int N = 1 << LOGN;
+    static constexpr int TX = N < 128 ? N : 128;
+    static constexpr int TYR = N / 4 < 16 ? N / 4 : 16;
+    static constexpr int RS = 4;
+    static constexpr int TY = RS * TYR;
+    static constexpr int THREADS = TX / 4 * RS;
+    static_assert(TX % 4 == 0 && N % TY == 0, "tile shape");
+};
+
+template <int LOGN>
+__device__ __forceinline__ void diffusion_reg_body(const float* __restrict__ A,
+                                                   const float* __restrict__ x,
+                                                   float* __restrict__ out, int c, int x0, int y0,
+                                                   unsigned char* render, int nch) {
+    using D = DiffGeoReg<LOGN>;
+    constexpr int N = D::N, MASK = N * N - 1;
+    const int col = x0 + 4 * (threadIdx.x % (D::TX / 4));   // first of this thread's columns
+    const int ys = y0 + (threadIdx.x / (D::TX / 4)) * D::TYR;
+    const float* Ac = A + size_t(c) * N * N;
+    const float* xc = x + size_t(c) * N * N;
+    float* oc = out + size_t(c) * N * N;
+    const int cl = (col - 4) & (N - 1), cr = (col + 4) & (N - 1);
+    const bool draw = render != nullptr && c < 3;
+    // columns col-4 .. col+7 of row y (toroidal)
+    auto ld3 = [&](const float* p, int y, float4& l, float4& m, float4& r) {
+        const float* row = p + ((y * N) & MASK);
+        l = __ldg(reinterpret_cast<const float4*>(row + cl));
+        m = __ldg(reinterpret_cast<const float4*>(row + col));
+        r = __ldg(reinterpret_cast<const float4*>(row + cr));
+    };
+
+    // slot k % 3 holds the sums of iteration k: heads / tails over Z columns
+    // col-1 .. col+4 (hs, ls), q over output columns col .. col+3 (qs), and
+    // A at the output columns (am)
+    float hs[3][6], ls[3][6], qs[3][4];
+    float4 am[3];
+#pragma unroll
+    for (int k = 0; k < D::TYR + 4; ++k) {
+        const int ya = ys - 2 + k;   // A row of this iteration
+        const int b = k % 3;
+        {
+            float4 al, ac, ar;
+            ld3(Ac, ya, al, ac, ar);
+            const float a[8] = {al.z, al.w, ac.x, ac.y, ac.z, ac.w, ar.x, ar.y};
+            float H[8], L[8];
+#pragma unroll
+            for (int i = 0; i < 8; ++i) {
+                H[i] = head12(a[i]);
+                L[i] = a[i] - H[i];
+            }
+#pragma unroll
+            for (int j = 0; j < 6; ++j) {
+                hs[b][j] = H[j] + H[j + 1] + H[j + 2];
+                ls[b][j] = L[j] + L[j + 1] + L[j + 2];
+            }
+            am[b] = ac;
+        }
+        if (k >= 2) {   // Z and q at row ya - 1
+            const int t0 = (k - 2) % 3, t1 = (k - 1) % 3;
+            float4 xl, xm, xr;
+            ld3(xc, ya - 1, xl, xm, xr);
+            const float xv[6] = {xl.w, xm.x, xm.y, xm.z, xm.w, xr.x};
+            float q[6];
+#pragma unroll
+            for (int j = 0; j < 6; ++j) {
+                const float zh = hs[t0][j] + hs[t1][j] + hs[b][j];
+                const float zt = ls[t0][j] + ls[t1][j] + ls[b][j];
+                const float z = zh + zt;
+                const float zl = zt - (z - zh);
+                const float rz = rcp_approx(z);
+                const float q0 = xv[j] * rz;
+                const float rem = fmaf(-q0, z, xv[j]);
+                q[j] = fmaf(rem - q0 * zl, rz, q0);
+            }
+#pragma unroll
+            for (int o = 0; o < 4; ++o) qs[b][o] = q[o] + q[o + 1] + q[o + 2];
+        }
+        if (k >= 4) {   // output row ya - 2
+            const int s0 = (k - 2) % 3, s1 = (k - 1) % 3;
+            const float4 a = am[s0];
+            const float4 v = make_float4(a.x * ((qs[s0][0] + qs[s1][0]) + qs[b][0]),
+                                         a.y * ((qs[s0][1] + qs[s1][1]) + qs[b][1]),
+                                         a.z * ((qs[s0][2] + qs[s1][2]) + qs[b][2]),
+                                         a.w * ((qs[s0][3] + qs[s1][3]) + qs[b][3]));
+            const int p = (ya - 2) * N + col;
+            *reinterpret_cast<float4*>(oc + p) = v;
+            if (draw) {
+                render_store(render, nch, c, size_t(p), v.x);
+                render_store(render, nch, c, size_t(p + 1), v.y);
+                render_store(render, nch, c, size_t(p + 2), v.z);
+                render_store(render, nch, c, size_t(p + 3), v.w);
+            }
+        }
+    }
+}
+
+// Variant 1 of the diffusion phase is the register body, variant 2 the
+// column-pair body.  TX x TY is the tile of one CTA (one work item).
 template <int LOGN, int V>
 struct DiffTile {
     static constexpr bool PAIR = (V == 2);
-    static constexpr int THREADS = PAIR ? DiffGeoPair<LOGN, V>::THREADS : DiffGeo2<LOGN, V>::THREADS;
-    static constexpr size_t SMEM = PAIR ? DiffGeoPair<LOGN, V>::SMEM : DiffGeo2<LOGN, V>::SMEM;
+    static constexpr bool REG = (V == 1);
+    static constexpr int THREADS = REG ? DiffGeoReg<LOGN>::THREADS
+                                 : (PAIR ? DiffGeoPair<LOGN, V>::THREADS : DiffGeo2<LOGN, V>::THREADS);
+    static constexpr size_t SMEM =
+        REG ? 0 : (PAIR ? DiffGeoPair<LOGN, V>::SMEM : DiffGeo2<LOGN, V>::SMEM);
+    static constexpr int TX = REG ? DiffGeoReg<LOGN>::TX : Geo<LOGN, V>::TX;
+    static constexpr int TY = REG ? DiffGeoReg<LOGN>::TY : Geo<LOGN, V>::TY;
 };
 
 template <int LOGN, int V>
@@ -802,7 +916,9 @@ __device__ __forceinline__ void diffusion_tile(const float* __restrict__ A,
                                                const float* __restrict__ x,
                                                float* __restrict__ out, int c, int x0, int y0,
                                                float* smf, unsigned char* render, int nch) {
-    if constexpr (DiffTile<LOGN, V>::PAIR)
+    if constexpr (DiffTile<LOGN, V>::REG)
+        diffusion_reg_body<LOGN>(A, x, out, c, x0, y0, render, nch);
+    else if constexpr (DiffTile<LOGN, V>::PAIR)
         diffusion_pair_body<LOGN, V>(A, x, out, c, x0, y0, smf, render, nch);
     else
         diffusion2_body<LOGN, V>(A, x, out, c, x0, y0, smf, render, nch);
@@ -813,8 +929,8 @@ __global__ void __launch_bounds__(DiffTile<LOGN, V>::THREADS)
     k_diffusion(const float* __restrict__ A, const float* __restrict__ x, float* __restrict__ out,
                 int cbase, unsigned char* __restrict__ render, int nch) {
     extern __shared__ __align__(128) float sm_diff[];
-    diffusion_tile<LOGN, V>(A, x, out, blockIdx.z + cbase, blockIdx.x * Geo<LOGN, V>::TX,
-                            blockIdx.y * Geo<LOGN, V>::TY, sm_diff, render, nch);
+    diffusion_tile<LOGN, V>(A, x, out, blockIdx.z + cbase, blockIdx.x * DiffTile<LOGN, V>::TX,
+                            blockIdx.y * DiffTile<LOGN, V>::TY, sm_diff, render, nch);
 }
 
 // ---------------------------------------------------------------------------
@@ -902,7 +1018,7 @@ template <int LOGN, int V>
 void launch_diff(const StepArgs& a, int c_lo, int nc, cudaStream_t st) {
     using G = Geo<LOGN, V>;
     using D = DiffTile<LOGN, V>;
-    k_diffusion<LOGN, V><<<dim3(G::N / G::TX, G::N / G::TY, nc), D::THREADS, D::SMEM, st>>>(
+    k_diffusion<LOGN, V><<<dim3(G::N / D::TX, G::N / D::TY, nc), D::THREADS, D::SMEM, st>>>(
         a.A, a.x_in, a.x_out, c_lo, a.render, a.C);
 }
 
