@@ -837,13 +837,19 @@ __device__ __forceinline__ void diffusion_reg_body(const float* __restrict__ A,
     // A at the output columns (am)
     float hs[3][6], ls[3][6], qs[3][4];
     float4 am[3];
+    // the loads of the next row are issued before this row's arithmetic
+    float4 nal, nac, nar;
+    float4 nxl = make_float4(0.f, 0.f, 0.f, 0.f), nxm = nxl, nxr = nxl;
+    ld3(Ac, ys - 2, nal, nac, nar);
 #pragma unroll
     for (int k = 0; k < D::TYR + 4; ++k) {
         const int ya = ys - 2 + k;   // A row of this iteration
         const int b = k % 3;
+        const float4 al = nal, ac = nac, ar = nar;
+        const float4 xl = nxl, xm = nxm, xr = nxr;   // state row ya - 1 (k >= 2)
+        if (k + 1 < D::TYR + 4) ld3(Ac, ya + 1, nal, nac, nar);
+        if (k + 1 >= 2 && k + 1 < D::TYR + 4) ld3(xc, ya, nxl, nxm, nxr);
         {
-            float4 al, ac, ar;
-            ld3(Ac, ya, al, ac, ar);
             const float a[8] = {al.z, al.w, ac.x, ac.y, ac.z, ac.w, ar.x, ar.y};
             float H[8], L[8];
 #pragma unroll
@@ -860,8 +866,6 @@ __device__ __forceinline__ void diffusion_reg_body(const float* __restrict__ A,
         }
         if (k >= 2) {   // Z and q at row ya - 1
             const int t0 = (k - 2) % 3, t1 = (k - 1) % 3;
-            float4 xl, xm, xr;
-            ld3(xc, ya - 1, xl, xm, xr);
             const float xv[6] = {xl.w, xm.x, xm.y, xm.z, xm.w, xr.x};
             float q[6];
 #pragma unroll
