@@ -33,11 +33,15 @@ namespace cg {
 // ---------------------------------------------------------------------------
 // 2. Diffusion backward (one channel tile per CTA, 256 threads).
 // ---------------------------------------------------------------------------
+// A and ybar (2-pixel halo) and the state (1-pixel halo) arrive by 16-byte
+// loads: their tiles reach 4 pixels past the tile on each side, so every
+// load stays aligned (n is a multiple of 4, also across the toroidal wrap).
 template <int LOGN, int V = 0>
 struct DiffBwdGeo {
     static constexpr int TX = Geo<LOGN, V>::TX, TY = Geo<LOGN, V>::TY;
-    static constexpr int AW = TX + 4, AH = TY + 4, HW = TX + 2, QH = TY + 2;
-    static constexpr size_t SMEM = size_t(2 * AH * AW + 2 * QH * HW) * sizeof(float);
+    static constexpr int AS = TX + 8, AH = TY + 4, HW = TX + 2, QH = TY + 2, V4 = AS / 4;
+    static constexpr size_t SMEM = size_t(2 * AH * AS + QH * AS + 2 * QH * HW) * sizeof(float);
+    static_assert(TX % 4 == 0, "tile shape");
 };
 
 template <int LOGN, int V = 0>
@@ -49,17 +53,26 @@ __device__ __forceinline__ void diffusion_bwd_body(const float* __restrict__ A,
                                                    int x0, int y0, float* smf) {
     using D = DiffBwdGeo<LOGN, V>;
     constexpr int N = Geo<LOGN, V>::N, TX = D::TX, TY = D::TY;
-    constexpr int AW = D::AW, AH = D::AH, HW = D::HW, QH = D::QH;
-    auto sA = reinterpret_cast<float (*)[AW]>(smf);
-    auto sY = reinterpret_cast<float (*)[AW]>(smf + AH * AW);
-    auto sQ = reinterpret_cast<float (*)[HW]>(smf + 2 * AH * AW);
-    auto sZb = reinterpret_cast<float (*)[HW]>(smf + 2 * AH * AW + QH * HW);
+    constexpr int AS = D::AS, AH = D::AH, HW = D::HW, QH = D::QH, V4 = D::V4;
+    // sA, sY: row r <-> y0 + r - 2; sX: row r <-> y0 + r - 1; column q <-> x0 - 4 + q
+    auto sA = reinterpret_cast<float (*)[AS]>(smf);
+    auto sY = reinterpret_cast<float (*)[AS]>(smf + AH * AS);
+    auto sX = reinterpret_cast<float (*)[AS]>(smf + 2 * AH * AS);
+    auto sQ = reinterpret_cast<float (*)[HW]>(smf + 2 * AH * AS + QH * AS);
+    auto sZb = reinterpret_cast<float (*)[HW]>(smf + 2 * AH * AS + QH * AS + QH * HW);
     const size_t plane = size_t(c) * N * N;
-    for (int i = threadIdx.x; i < AH * AW; i += blockDim.x) {
-        const int r = i / AW, q = i % AW;
-        const size_t g = plane + size_t((y0 + r - 2) & (N - 1)) * N + ((x0 + q - 2) & (N - 1));
-        sA[r][q] = __ldg(&A[g]);
-        sY[r][q] = __ldg(&ybar[g]);
+    const float* Ap = A + plane;
+    const float* Yp = ybar + plane;
+    const float* Xp = x + plane;
+    for (int i = threadIdx.x; i < AH * V4; i += blockDim.x) {
+        const int r = i / V4, v = i % V4;
+        const int cx = (x0 - 4 + 4 * v) & (N - 1);
+        const size_t g = size_t((y0 + r - 2) & (N - 1)) * N + cx;
+        *reinterpret_cast<float4*>(&sA[r][4 * v]) = __ldg(reinterpret_cast<const float4*>(Ap + g));
+        *reinterpret_cast<float4*>(&sY[r][4 * v]) = __ldg(reinterpret_cast<const float4*>(Yp + g));
+        if (r < QH)
+            *reinterpret_cast<float4*>(&sX[r][4 * v]) = __ldg(reinterpret_cast<const float4*>(
+                Xp + size_t((y0 + r - 1) & (N - 1)) * N + cx));
     }
     __syncthreads();
     for (int i = threadIdx.x; i < QH * HW; i += blockDim.x) {
@@ -69,12 +82,12 @@ __device__ __forceinline__ void diffusion_bwd_body(const float* __restrict__ A,
         for (int di = 0; di < 3; ++di)
 #pragma unroll
             for (int dj = 0; dj < 3; ++dj) {
-                const float a = sA[r + di][q + dj];
+                const float a = sA[r + di][q + dj + 2];
                 z += a;
-                qb = fmaf(sY[r + di][q + dj], a, qb);
+                qb = fmaf(sY[r + di][q + dj + 2], a, qb);
             }
         const int gy = (y0 + r - 1) & (N - 1), gx = (x0 + q - 1) & (N - 1);
-        const float xv = __ldg(&x[plane + size_t(gy) * N + gx]);
+        const float xv = sX[r][q + 3];
         const float qv = xv / z;
         sQ[r][q] = qv;
         sZb[r][q] = -qb * qv / z;
@@ -91,8 +104,8 @@ __device__ __forceinline__ void diffusion_bwd_body(const float* __restrict__ A,
                 P += sQ[r + di][q + dj];
                 SZ += sZb[r + di][q + dj];
             }
-        const float a = sA[r + 2][q + 2];
-        const float Ab = fmaf(sY[r + 2][q + 2], P, SZ);
+        const float a = sA[r + 2][q + 4];
+        const float Ab = fmaf(sY[r + 2][q + 4], P, SZ);
         abar[plane + size_t(y0 + r) * N + x0 + q] = temp * a * Ab;
     }
 }
@@ -277,6 +290,21 @@ __device__ __forceinline__ bool col_conv_adj_body(float2* __restrict__ rowspec,
 
     for (int gi = 0; gi < cnt; ++gi) {
         const int k = groups.in_idx[base + gi];
+        float2* kg = kgrad ? kgrad + (size_t(k) * M + kx0) * N : nullptr;
+        // this thread's kernel-gradient values, loaded now so that they land
+        // during the column FFT below (only this CTA touches them)
+        float2 kgv[IPTL][RL];
+        if (kg) {
+#pragma unroll
+            for (int it = 0; it < IPTL; ++it) {
+                const int item = threadIdx.x + it * T;
+                if ((TW * JL) % T == 0 || item < TW * JL) {
+                    const int s = item / JL, j = item % JL;
+#pragma unroll
+                    for (int r = 0; r < RL; ++r) kgv[it][r] = kg[size_t(s) * N + j + r * JL];
+                }
+            }
+        }
         issue(U + (size_t(k) * M + kx0) * N);
         if (!wait_tile()) return false;
         const float2* ktile = kspec + (size_t(k) * (M + 1) + kx0) * N;
@@ -284,7 +312,6 @@ __device__ __forceinline__ bool col_conv_adj_body(float2* __restrict__ rowspec,
                                              [&]() { issue(ktile); });
         if (!wait_tile()) return false;
         const float2* kb = kspec + (size_t(k) * (M + 1) + M) * N;
-        float2* kg = kgrad ? kgrad + (size_t(k) * M + kx0) * N : nullptr;
 #pragma unroll
         for (int it = 0; it < IPTL; ++it) {
             const int item = threadIdx.x + it * T;
@@ -321,8 +348,7 @@ __device__ __forceinline__ bool col_conv_adj_body(float2* __restrict__ rowspec,
                         } else {
                             v = cmulc(p, px);
                         }
-                        float2* q = kg + size_t(s) * N + i;
-                        *q = cadd(*q, v);
+                        kg[size_t(s) * N + i] = cadd(kgv[it][r], v);
                     }
                 }
             }
