@@ -140,33 +140,31 @@ __device__ __forceinline__ void row_r2c_body(const float* __restrict__ state,
 }
 
 // Even/odd split of RB transformed rows in shared memory (X[k] from Z[k],
-// Z[M-k]; X[0], X[M] packed in slot 0), then the kx-major transposed store
-// of the RB rows to dst[kx * N + s].
+// Z[M-k]; X[0], X[M] packed in slot 0), stored straight to the kx-major
+// rows dst[kx * N + s].  The row index runs fastest over the threads, so RB
+// consecutive lanes write one column's RB rows (a full sector for RB = 4),
+// and the shared reads stay conflict-free with the row pitch RP.
 template <int LOGN, int V>
 __device__ __forceinline__ void r2c_finish(float2* sm, const float2* __restrict__ tw,
                                            float2* __restrict__ dst) {
     using G = Geo<LOGN, V>;
     constexpr int H = G::M / 2;
     for (int item = threadIdx.x; item < G::RB * (H + 1); item += G::RT) {
-        const int s = item / (H + 1), k = item % (H + 1);
-        float2* row = sm + s * G::RP;
+        const int s = item % G::RB, k = item / G::RB;
+        const float2* row = sm + s * G::RP;
         if (k == 0) {
             const float2 z = row[0];
-            row[0] = make_float2(2.f * (z.x + z.y), 2.f * (z.x - z.y));
+            dst[s] = make_float2(2.f * (z.x + z.y), 2.f * (z.x - z.y));
         } else {
             const float2 a = row[pidx(k)], b = row[pidx(G::M - k)];
             const float2 E = make_float2(a.x + b.x, a.y - b.y);
             const float2 D = make_float2(a.x - b.x, a.y + b.y);
             const float2 O = make_float2(D.y, -D.x);
             const float2 wo = cmul(__ldg(&tw[k]), O);
-            row[pidx(k)] = cadd(E, wo);
-            if (k != H) row[pidx(G::M - k)] = cconj(csub(E, wo));
+            dst[size_t(k) * G::N + s] = cadd(E, wo);
+            if (k != H) dst[size_t(G::M - k) * G::N + s] = cconj(csub(E, wo));
         }
     }
-    __syncthreads();
-
-    for_row_tile<LOGN, V>(
-        [&](int s, int kx, int pk) { dst[size_t(kx) * G::N + s] = sm[s * G::RP + pk]; });
 }
 
 template <int LOGN, int V = 0>
