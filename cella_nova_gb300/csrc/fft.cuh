@@ -161,7 +161,10 @@ __host__ __device__ constexpr int last_radix(int L, int MR = 16) {
 // owns items t, t+T, ...  It loads v[r] = x[j + r*L/R], applies
 // W_{NS*R}^{r*(j mod NS)}, runs DFT-R and stores v[q] at
 // (j div NS)*NS*R + (j mod NS) + q*NS.  All loads finish (barrier) before any
-// store, so in-place passes are safe; a second barrier closes the pass.
+// store, so in-place passes are safe; a second barrier closes the pass.  A
+// caller whose loads and stores of this pass cannot touch the same shared
+// memory (loads from global memory or another buffer, or stores to registers
+// or global memory) passes MIDBAR = false and skips the first barrier.
 //   twp : this pass's table (tw_offset layout).
 //   ld(s, i, it, q)         -> float2
 //   st(s, i, v, it, q)      (it, q) name the register slot of the value.
@@ -176,7 +179,8 @@ __device__ __forceinline__ void item_pos(int item, int& s, int& j) {
     }
 }
 
-template <int L, int R, int NS, bool INV, int T, int S, bool SFAST = false, class LD, class ST>
+template <int L, int R, int NS, bool INV, int T, int S, bool SFAST = false, bool MIDBAR = true,
+          class LD, class ST>
 __device__ __forceinline__ void stockham_pass(LD& ld, ST& st, const float2* __restrict__ twp) {
     constexpr int J = L / R;
     constexpr int ITEMS = S * J;
@@ -198,7 +202,7 @@ __device__ __forceinline__ void stockham_pass(LD& ld, ST& st, const float2* __re
             }
         }
     }
-    __syncthreads();
+    if constexpr (MIDBAR) __syncthreads();
 #pragma unroll
     for (int it = 0; it < IPT; ++it) {
         const int item = threadIdx.x + it * T;
@@ -232,20 +236,27 @@ __device__ __forceinline__ void stockham_pass(LD& ld, ST& st, const float2* __re
 // Full length-L transform: first pass reads through `ld`, middle passes use
 // shared memory through smld/smst, the last pass writes through `stl`.
 // `tab` is the plan's twiddle table (tw_offset layout); SFAST selects the
-// item order of every pass (stockham_pass).
+// item order of every pass (stockham_pass).  FIRSTBAR / LASTBAR = false
+// drop the load-store barrier of the first / last pass (stockham_pass's
+// MIDBAR): for a first pass whose `ld` reads no shared memory that smst
+// writes, and a last pass whose `stl` writes no shared memory smld reads.
 template <int L, int NS, bool INV, int T, int S, bool REMFIRST = false, int MR = 16,
-          bool SFAST = false>
+          bool SFAST = false, bool FIRSTBAR = true, bool LASTBAR = true>
 struct FftPasses {
     template <class LD, class SMLD, class SMST, class STL>
     __device__ __forceinline__ static void run(LD& ld, SMLD& smld, SMST& smst, STL& stl,
                                                const float2* __restrict__ tab) {
         constexpr int R = PassRadix<L, NS, REMFIRST, MR>::R;
+        constexpr bool FIRST = (NS == 1), LAST = (NS * R == L);
+        constexpr bool BAR = FIRST && LAST ? (FIRSTBAR || LASTBAR)
+                                           : (FIRST ? FIRSTBAR : (LAST ? LASTBAR : true));
         const float2* twp = tab + tw_offset(L, REMFIRST, NS, MR);
-        if constexpr (NS * R == L) {
-            stockham_pass<L, R, NS, INV, T, S, SFAST>(ld, stl, twp);
+        if constexpr (LAST) {
+            stockham_pass<L, R, NS, INV, T, S, SFAST, BAR>(ld, stl, twp);
         } else {
-            stockham_pass<L, R, NS, INV, T, S, SFAST>(ld, smst, twp);
-            FftPasses<L, NS * R, INV, T, S, REMFIRST, MR, SFAST>::run(smld, smld, smst, stl, tab);
+            stockham_pass<L, R, NS, INV, T, S, SFAST, BAR>(ld, smst, twp);
+            FftPasses<L, NS * R, INV, T, S, REMFIRST, MR, SFAST, FIRSTBAR, LASTBAR>::run(
+                smld, smld, smst, stl, tab);
         }
     }
 };

@@ -135,7 +135,9 @@ __device__ __forceinline__ void row_r2c_body(const float* __restrict__ state,
         reinterpret_cast<const float2*>(state + (size_t(c) * G::N + y0) * G::N);
     auto ld0 = [&](int s, int i, int, int) { return __ldg(&src[size_t(s) * G::M + i]); };
     SmemRows rows{sm, G::RP};
-    FftPasses<G::M, 1, false, G::RT, G::RB, false, G::ROW_MR>::run(ld0, rows, rows, rows, tw + G::TW_ROW);
+    // the first pass reads global memory: no load-store barrier
+    FftPasses<G::M, 1, false, G::RT, G::RB, false, G::ROW_MR, false, false, true>::run(
+        ld0, rows, rows, rows, tw + G::TW_ROW);
     r2c_finish<LOGN, V>(sm, tw, rowspec + size_t(c) * G::M * G::N + y0);
 }
 
@@ -178,18 +180,21 @@ __global__ void __launch_bounds__(Geo<LOGN, V>::RT, 512 / Geo<LOGN, V>::RT) k_ro
 }
 
 // Run the first pass of a transform, then `hook()`, then the rest.
+// FIRSTBAR / LASTBAR as in FftPasses.
 template <int L, bool INV, int T, int S, bool REMFIRST, int MR = 16, bool SFAST = false,
-          class LD, class SMLD, class SMST, class STL, class HOOK>
+          bool FIRSTBAR = true, bool LASTBAR = true, class LD, class SMLD, class SMST, class STL,
+          class HOOK>
 __device__ __forceinline__ void fft_with_hook(LD& ld, SMLD& smld, SMST& smst, STL& stl,
                                               const float2* __restrict__ tab, HOOK hook) {
     constexpr int R = PassRadix<L, 1, REMFIRST, MR>::R;
     if constexpr (R == L) {
-        stockham_pass<L, R, 1, INV, T, S, SFAST>(ld, stl, tab);
+        stockham_pass<L, R, 1, INV, T, S, SFAST, FIRSTBAR || LASTBAR>(ld, stl, tab);
         hook();
     } else {
-        stockham_pass<L, R, 1, INV, T, S, SFAST>(ld, smst, tab);
+        stockham_pass<L, R, 1, INV, T, S, SFAST, FIRSTBAR>(ld, smst, tab);
         hook();
-        FftPasses<L, R, INV, T, S, REMFIRST, MR, SFAST>::run(smld, smld, smst, stl, tab);
+        FftPasses<L, R, INV, T, S, REMFIRST, MR, SFAST, true, LASTBAR>::run(smld, smld, smst, stl,
+                                                                             tab);
     }
 }
 
@@ -270,8 +275,10 @@ __device__ __forceinline__ bool col_conv_body(const float2* __restrict__ rowspec
     auto ld_in = [&](int s, int i, int, int) { return KS[s * N + i]; };
     SmemRows wrows{W, G::CP};
     auto keep = [&](int, int, float2 v, int it, int r) { F[it][r] = v; };
-    fft_with_hook<N, false, T, TW, false>(ld_in, wrows, wrows, keep, tw + G::TW_COL_FWD,
-                                         [&]() { issue(kernel_tile(0)); });
+    // forward: the first pass reads the staging tile, the last one keeps its
+    // values in registers (no load-store barriers)
+    fft_with_hook<N, false, T, TW, false, 16, false, false, false>(
+        ld_in, wrows, wrows, keep, tw + G::TW_COL_FWD, [&]() { issue(kernel_tile(0)); });
 
     for (int gi = 0; gi < cnt; ++gi) {
         if (!wait_tile()) return false;
@@ -301,7 +308,10 @@ __device__ __forceinline__ bool col_conv_body(const float2* __restrict__ rowspec
         };
         float2* dst = U + (size_t(k) * M + kx0) * N;
         auto gst = [&](int s, int i, float2 v, int, int) { dst[size_t(s) * N + i] = v; };
-        fft_with_hook<N, true, T, TW, true>(ld_mul, wrows, wrows, gst, tw + G::TW_COL_INV, [&]() {
+        // inverse: the first pass reads W for column 0, so it keeps its
+        // barrier; the last one writes global memory
+        fft_with_hook<N, true, T, TW, true, 16, false, true, false>(
+            ld_mul, wrows, wrows, gst, tw + G::TW_COL_INV, [&]() {
             if (gi + 1 < cnt) issue(kernel_tile(gi + 1));
         });
     }
@@ -441,7 +451,9 @@ __device__ __forceinline__ bool row_c2r_growth_body(const CUtensorMap* umap, boo
                     make_float2(v.x * udbg_scale, v.y * udbg_scale);
             }
         };
-        fft_with_hook<M, true, G::RT, RB, false, G::ROW_MR, true>(
+        // the first pass reads the landing tile and the last one keeps its
+        // values in registers: neither needs its load-store barrier
+        fft_with_hook<M, true, G::RT, RB, false, G::ROW_MR, true, false, false>(
             ld0, rows, rows, gst, tw + G::TW_ROW, [&]() {
                 if (gi + 1 < cnt) issue(gi + 1);   // the first pass has read the tile
             });
