@@ -180,7 +180,9 @@ def cpu_baseline(cr, budget_s=20.0, nthreads=None, forms=True):
     """The FP32 C restatement of example.rs (faithful: FFT per kernel), all
     host threads, one step of the full workload (a bounded sample).  With
     forms, one step more in each of the other forms: one thread (example.rs
-    is serial) and FP64, each timed once."""
+    is serial) and FP64, each timed once, and the torch CPU model
+    (train/diff_lenia_org.py's step, restated in oracle/autograd_ref.py) in
+    FP32 on torch's own threads."""
     from oracle import oracle as O
     nthreads = nthreads or os.cpu_count() or 1
     st = cr.seed.astype(np.float32)
@@ -201,11 +203,28 @@ def cpu_baseline(cr, budget_s=20.0, nthreads=None, forms=True):
                      f"f32 C port of example.rs (FFT per kernel), OpenMP, best {t:.2f} s/step"}
     if forms:
         rows = [{"threads": nthreads, "dtype": "f32", "s_per_step": round(t, 3)}]
+        for r in rows:
+            r["impl"] = "C port of example.rs"
         for dt, nt in ((np.float64, nthreads), (np.float32, 1), (np.float64, 1)):
             t0 = time.perf_counter()
             O.step_c(cr.seed.astype(dt), ks, *args, dtype=dt, faithful=True, nthreads=nt)
             rows.append({"threads": nt, "dtype": "f32" if dt == np.float32 else "f64",
+                         "impl": "C port of example.rs",
                          "s_per_step": round(time.perf_counter() - t0, 3)})
+        try:
+            import torch
+            from oracle import autograd_ref as R
+        except ImportError:
+            torch = None
+        if torch is not None:
+            xt = torch.tensor(np.asarray(cr.seed, np.float32))
+            kt = torch.tensor(np.asarray(cr.kspec, np.complex64))
+            with torch.no_grad():
+                t0 = time.perf_counter()
+                R.step(xt, kt, cr.c0, cr.c1, cr.mu, cr.sigma, cr.weights, cr.temp)
+                rows.append({"threads": torch.get_num_threads(), "dtype": "f32",
+                             "impl": "torch CPU (train/diff_lenia_org.py step)",
+                             "s_per_step": round(time.perf_counter() - t0, 3)})
         for r in rows:
             r["cell_updates_per_s"] = cr.n * cr.n / r["s_per_step"]
         out["forms"] = rows

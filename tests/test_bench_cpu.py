@@ -26,8 +26,8 @@ def test_reference_arm_line():
 
 
 def test_cpu_baseline_forms_small():
-    """The cpu_baseline object with its other forms (one thread, FP64), on a
-    64^2 creature."""
+    """The cpu_baseline object with its other forms (one thread, FP64, and the
+    torch CPU model), on a 64^2 creature."""
     sys.path.insert(0, ROOT)
     import bench
     from cella_nova_gb300.creature import make_creature
@@ -36,6 +36,8 @@ def test_cpu_baseline_forms_small():
     cr = make_creature(64, 2, seed=1, radius=(4, 12), seed_box=32)
     cpu = bench.cpu_baseline(cr, budget_s=1.0, nthreads=2)
     assert cpu["kind"] == "port" and cpu["cores"] == 2 and cpu["value"] > 0
-    forms = {(f["threads"], f["dtype"]) for f in cpu["forms"]}
-    assert forms == {(2, "f32"), (2, "f64"), (1, "f32"), (1, "f64")}
+    c_forms = {(f["threads"], f["dtype"]) for f in cpu["forms"] if f["impl"].startswith("C port")}
+    assert c_forms == {(2, "f32"), (2, "f64"), (1, "f32"), (1, "f64")}
+    torch_forms = [f for f in cpu["forms"] if f["impl"].startswith("torch")]
+    assert len(torch_forms) == 1 and torch_forms[0]["threads"] >= 1
     assert all(f["cell_updates_per_s"] > 0 for f in cpu["forms"])
