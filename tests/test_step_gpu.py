@@ -178,7 +178,7 @@ def test_kernel_reupload_and_zero_kernel():
         assert np.abs(conv[0]).max() > 0.0
 
 
-@pytest.mark.parametrize("n", [64, 256, 1024, 2048])
+@pytest.mark.parametrize("n", [16, 32, 64, 256, 1024, 2048])
 def test_variants_agree_and_autotune(n):
     """Every CTA-shape variant computes the same bits, so the autotuner never
     changes results."""
