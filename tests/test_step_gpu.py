@@ -230,3 +230,36 @@ def test_random_worlds(trial):
                        radius=(max(2.0, n / 16), max(3.0, n / 5)), seed_box=n // 2,
                        temp=float(rng.uniform(0.5, 2.0)))
     check_steps(cr, steps=2)
+
+
+def grey_frame(x):
+    """The frame the reference's integration test compares
+    (train/save_frames_png.py:202-210, ml-rs/save_pngs.rs): the channel sum,
+    min-max normalised to 0..255 and truncated to 8 bits."""
+    img = x.sum(axis=0).astype(np.float64)
+    lo, hi = img.min(), img.max()
+    if hi <= lo:
+        return np.zeros(img.shape, np.uint8)
+    return ((img - lo) / (hi - lo) * 255).astype(np.uint8)
+
+
+@pytest.mark.parametrize("n", [256, 512])
+def test_fifty_steps_within_one_grey_level(n):
+    """The reference's acceptance test (scripts/integration.sh:8-46,
+    train/compare_pngs.py:72-78): 50 free-running steps, and every frame's
+    8-bit grey image within one grey level of the FP64 oracle's."""
+    cr = make_creature(n, 3, seed=2024 + n, radius=(n / 40, n / 16), seed_box=n // 2)
+    ks = cr.kspec.astype(np.complex128)
+    args = (cr.c0, cr.c1, cr.mu.astype(np.float64), cr.sigma.astype(np.float64),
+            cr.weights.astype(np.float64), cr.temp)
+    x64 = cr.seed.astype(np.float64)
+    worst = 0
+    with GpuMaceLenia.from_creature(cr) as sim:
+        for _ in range(50):
+            sim.iterate()
+            x64, _, _ = O.step_c(x64, ks, *args, dtype=np.float64, nthreads=os.cpu_count() or 1)
+            d = np.abs(grey_frame(sim.state()).astype(int) - grey_frame(x64).astype(int)).max()
+            worst = max(worst, int(d))
+        drift = float(np.abs(sim.state() - x64).max())
+    assert worst <= 1, worst
+    assert drift <= 1e-4, drift
