@@ -74,6 +74,28 @@ def kernel_bytes_per_px(C, K):
             12 * C)                      # read A and the state, write the new state
 
 
+def roofline_object(kms, n, C, K, peak, peak_kind, traffic=None):
+    """The `roofline` object of the bench line: every step kernel's
+    algorithmic bytes per launch (kernel_bytes_per_px x n^2) over its
+    measured duration (kms, ms per step, in KERNEL_NAMES order) against the
+    peak, and the kernel with the largest device time reported on top.
+    `traffic` maps "<kernel>_<n>" to an ncu capture's DRAM bytes per launch."""
+    traffic = traffic or {}
+    px = n * n
+    per_kernel = []
+    for name, b, t in zip(KERNEL_NAMES, kernel_bytes_per_px(C, K), kms):
+        ach = b * px / (t / 1e3) / 1e9
+        per_kernel.append({"kernel": name, "algorithmic_bytes": b * px, "kernel_ms": t,
+                           "achieved": ach, "frac": ach / peak,
+                           "traffic": traffic.get(f"{name}_{n}", {}).get("dram_bytes_per_launch")})
+    top = max(per_kernel, key=lambda r: r["kernel_ms"])
+    return {"bound": "hbm", "kernel": top["kernel"], "achieved": top["achieved"], "peak": peak,
+            "unit": "GB/s", "frac": top["frac"], "traffic": top["traffic"],
+            "algorithmic_bytes": top["algorithmic_bytes"], "kernel_ms": top["kernel_ms"],
+            "peak_source": peak_kind, "selection": "the step kernel with the largest device time",
+            "kernels": per_kernel}
+
+
 def peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -362,17 +384,6 @@ def run_ours(args):
     peak, peak_kind = peaks()
     bpp = bytes_per_px(C_CH, K_KER)
     step_s = ms / 1e3 / args.steps
-    # every step kernel against the roofline; the object reported is the
-    # kernel with the largest share of the step's device time
-    traffic_all = load_traffic()
-    per_kernel = []
-    for name, b, t in zip(KERNEL_NAMES, kernel_bytes_per_px(C_CH, K_KER), kms):
-        ach = b * px / (t / 1e3) / 1e9
-        per_kernel.append({"kernel": name, "algorithmic_bytes": b * px, "kernel_ms": t,
-                           "achieved": ach, "frac": ach / peak,
-                           "traffic": traffic_all.get(f"{name}_{N_GRID}", {})
-                                                 .get("dram_bytes_per_launch")})
-    top = max(per_kernel, key=lambda r: r["kernel_ms"])
     value = world * px * args.steps / (ms / 1e3)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -382,12 +393,9 @@ def run_ours(args):
         "config": {"workload": WORKLOAD, "n": N_GRID, "channels": C_CH, "kernels": K_KER,
                    "parallelism": f"replicas x{world}",
                    "l2": "no flush: each step streams ~0.75 GB (> 129 MB L2)"},
-        "roofline": {"bound": "hbm", "kernel": top["kernel"], "achieved": top["achieved"],
-                     "peak": peak, "unit": "GB/s", "frac": top["frac"], "traffic": top["traffic"],
-                     "algorithmic_bytes": top["algorithmic_bytes"], "kernel_ms": top["kernel_ms"],
-                     "peak_source": peak_kind,
-                     "selection": "the step kernel with the largest device time",
-                     "kernels": per_kernel},
+        # every step kernel against the roofline; the kernel with the
+        # largest share of the step's device time on top
+        "roofline": roofline_object(kms, N_GRID, C_CH, K_KER, peak, peak_kind, load_traffic()),
         "step_hbm": {"bytes_per_step": bpp * px, "achieved_gbs": bpp * px / step_s / 1e9,
                      "frac": bpp * px / step_s / 1e9 / peak, "peak_source": peak_kind,
                      "bytes_per_step_as_built": bytes_per_px_as_built(C_CH, K_KER) * px,

@@ -41,3 +41,21 @@ def test_cpu_baseline_forms_small():
     torch_forms = [f for f in cpu["forms"] if f["impl"].startswith("torch")]
     assert len(torch_forms) == 1 and torch_forms[0]["threads"] >= 1
     assert all(f["cell_updates_per_s"] > 0 for f in cpu["forms"])
+
+
+def test_roofline_object_reports_the_slowest_kernel():
+    """bench.py's roofline object: algorithmic bytes over each kernel's time,
+    the kernel with the largest device time on top, traffic from the ncu
+    summary."""
+    sys.path.insert(0, ROOT)
+    import bench
+    kms = [0.030, 0.068, 0.070, 0.040]     # ms per step: r2c, col_conv, c2r, diffusion
+    traffic = {"k_row_c2r_growth_2048": {"dram_bytes_per_launch": 1.8e8}}
+    r = bench.roofline_object(kms, 2048, 3, 9, 6790.0, "measured", traffic)
+    assert r["kernel"] == "k_row_c2r_growth" and r["kernel_ms"] == 0.070
+    px = 2048 * 2048
+    assert r["algorithmic_bytes"] == (4 * 9 + 4 * 3) * px
+    assert abs(r["achieved"] - r["algorithmic_bytes"] / 0.070e-3 / 1e9) < 1e-6
+    assert abs(r["frac"] - r["achieved"] / 6790.0) < 1e-12 and r["traffic"] == 1.8e8
+    assert [k["kernel"] for k in r["kernels"]] == list(bench.KERNEL_NAMES)
+    assert sum(k["algorithmic_bytes"] for k in r["kernels"]) == bench.bytes_per_px_as_built(3, 9) * px
