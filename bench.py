@@ -143,15 +143,22 @@ class ClockSampler:
         if self.thread:
             self.thread.join(timeout=5)
 
-    def summary(self, t0=None, t1=None):
-        rows = [r for t, r in self.rows if (t0 is None or t >= t0) and (t1 is None or t <= t1)]
-        if not rows:
-            rows = [r for _, r in self.rows]
+    def summary(self, t0=None, t1=None, busy=None):
+        """Median SM clock, its maximum and the throttle reasons seen in
+        [t0, t1].  A timed region shorter than the 100 ms sampling period
+        holds no sample; then the samples over `busy` = (start, end, label),
+        a span in which the GPU ran this program's work, stand in, and
+        `window` says so."""
+        def pick(a, b):
+            return [r for t, r in self.rows if (a is None or t >= a) and (b is None or t <= b)]
+        rows, window = pick(t0, t1), "timed region"
+        if not rows and busy is not None:
+            rows, window = pick(busy[0], busy[1]), f"GPU-busy span: {busy[2]}"
         if not rows:
             why = ("nvidia-smi printed no sample (the run may be shorter than its start-up)"
                    if self.proc else "nvidia-smi unavailable")
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0,
-                    "note": why}
+                    "window": window, "note": why}
         sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
         mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
@@ -159,7 +166,7 @@ class ClockSampler:
                           if len(r) > 5 + i and r[5 + i].lower() == "active"})
         return {"sm_mhz": statistics.median(sm) if sm else None,
                 "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
-                "samples": len(rows)}
+                "samples": len(rows), "window": window}
 
 
 def rank_info():
@@ -253,18 +260,34 @@ def cpu_baseline(cr, budget_s=20.0, nthreads=None, forms=True):
     return out
 
 
-def step_error_vs_fp64(sim, cr):
-    """Checker beside the CPU baseline: one GPU step from the GPU's current
-    state against the FP64 oracle's step from the same state (numpy FP64
-    twin of example.rs), max-abs over the whole 2048^2 grid."""
+def oracle_step_error(x, y, cr, nthreads=None):
+    """Max-abs difference between a GPU step (x -> y) and the FP64 oracle's
+    step from the same state x (the C restatement of example.rs, all host
+    threads)."""
     from oracle import oracle as O
+    ref, _, _ = O.step_c(np.asarray(x, np.float64), cr.kspec.astype(np.complex128), cr.c0,
+                         cr.c1, cr.mu.astype(np.float64), cr.sigma.astype(np.float64),
+                         cr.weights.astype(np.float64), cr.temp,
+                         nthreads=nthreads or os.cpu_count() or 1)
+    return float(np.abs(np.asarray(y, np.float64) - ref).max())
+
+
+def sample_step(sim):
+    """(state, state after one more step) of a world, on the host."""
     x = sim.state()
     sim.iterate()
-    y = sim.state()
-    ref, _, _ = O.step_np(x.astype(np.float64), cr.kspec.astype(np.complex128), cr.c0, cr.c1,
-                          cr.mu.astype(np.float64), cr.sigma.astype(np.float64),
-                          cr.weights.astype(np.float64), cr.temp)
-    return float(np.abs(y - ref).max())
+    return x, sim.state()
+
+
+def step_errors(pairs, cr):
+    """Per-step max-abs errors of the sampled GPU steps against the FP64
+    oracle (teacher-forced: each oracle step starts from the GPU's state)."""
+    out = {}
+    for label, (x, y) in pairs.items():
+        out[label] = oracle_step_error(x, y, cr)
+    return {"max_abs": max(out.values()), "bar": 1e-5, "steps": out,
+            "how": "teacher-forced: a GPU step against the FP64 oracle's step from the same "
+                   "state, at the points of the run named in `steps`"}
 
 
 def run_reference(args):
@@ -282,8 +305,11 @@ def run_reference(args):
     ks = cr.kspec.astype(np.complex128)
     a = (cr.c0, cr.c1, cr.mu.astype(np.float64), cr.sigma.astype(np.float64),
          cr.weights.astype(np.float64), cr.temp)
-    for _ in range(min(args.warmup, 1)):
+    # the same warm-up count as the GPU arm, within a bounded time
+    warm, tw = 0, time.perf_counter()
+    while warm < args.warmup and time.perf_counter() - tw < 60.0:
         st, _, _ = O.step_c(st, ks, *a, dtype=np.float32, faithful=True, nthreads=nthreads)
+        warm += 1
     budget = 150.0
     done, t0 = 0, time.perf_counter()
     while done < args.steps:
@@ -293,21 +319,27 @@ def run_reference(args):
             break
     el = time.perf_counter() - t0
     value = N_GRID * N_GRID * done / el
-    sample = (f"{done} of {args.steps} requested steps (150 s budget), f32 C port of "
-              f"example.rs, OpenMP {nthreads} threads")
+    sample = (f"{done} of {args.steps} requested steps (150 s budget) after {warm} warm-up "
+              f"steps, f32 C port of example.rs, OpenMP {nthreads} threads")
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
-        "n_gpus": args.gpus, "steps": done, "warmup": min(args.warmup, 1),
+        "n_gpus": args.gpus, "steps": done, "warmup": warm,
         "ms_per_step": 1e3 * el / done, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "n": N_GRID, "channels": C_CH, "kernels": K_KER,
-                   "device": "host CPU"},
+        "config": workload_config(world), "device": "host CPU",
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port",
                          "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
     return 0
+
+
+def workload_config(world):
+    """The `config` object of both arms' lines (the same workload)."""
+    return {"workload": WORKLOAD, "n": N_GRID, "channels": C_CH, "kernels": K_KER,
+            "parallelism": f"replicas x{world}",
+            "l2": "no flush: each step streams ~0.75 GB (> 129 MB L2)"}
 
 
 def load_traffic():
@@ -325,9 +357,15 @@ def run_ours(args):
     from cella_nova_gb300 import GpuMaceLenia
     from cella_nova_gb300.creature import make_creature
 
+    sampler = ClockSampler(local)
+    sampler.start()
+    t_busy0 = time.perf_counter()
     cr = make_creature(N_GRID, C_CH, seed=2048 + rank, temp=1.0)
     sim = GpuMaceLenia.from_creature(cr)
     px = N_GRID * N_GRID
+    checks = {}
+    mass0 = sim.mass_f64()
+    checks["step 1 (from the seed)"] = sample_step(sim)
     tuned = None
     if args.variants:
         sim.set_variants([int(v) for v in args.variants.split(",")])
@@ -336,13 +374,12 @@ def run_ours(args):
         chosen, tms = sim.autotune(reps=10)
         tuned = {"variants": chosen, "ms": np.round(tms, 4).tolist()}
     stream = torch.cuda.ExternalStream(sim.stream())
-    sampler = ClockSampler(local)
-    sampler.start()
 
-    mass0 = sim.mass_f64()
     # warm-up, then K timed graph launches between barriers + syncs
-    sim.run_steps(max(args.warmup, 3))
+    warm = max(args.warmup, 3)
+    sim.run_steps(warm)
     sim.synchronize()
+    checks["after the warm-up"] = sample_step(sim)
     barrier(dist, world)
     torch.cuda.synchronize()
     e0 = torch.cuda.Event(enable_timing=True)
@@ -357,16 +394,18 @@ def run_ours(args):
     barrier(dist, world)
     ms_local = e0.elapsed_time(e1)
     ms = max_over_ranks(ms_local, dist, world)
-    clocks = sampler.summary(t_wall0, t_wall1)
-
-    mass1 = sim.mass_f64()
-    drift = {"steps": max(args.warmup, 3) + args.steps,
-             "max_rel": float(np.abs(mass1 / mass0 - 1).max()), "reduction": "FP64 on the GPU"}
+    checks["after the timed steps"] = sample_step(sim)
 
     # per-kernel device time with events between kernels (same stream)
     prof_steps = min(max(args.steps, 8), 256)
     kms = sim.profile_kernels(prof_steps)
     sim.synchronize()
+    checks[f"after the kernel profile ({prof_steps} more steps)"] = sample_step(sim)
+    mass1 = sim.mass_f64()
+    total_steps = 1 + warm + 1 + args.steps + 1 + prof_steps + 1
+    drift = {"steps": total_steps, "max_rel": float(np.abs(mass1 / mass0 - 1).max()),
+             "reduction": "FP64 on the GPU"}
+    t_busy1 = time.perf_counter()
 
     # end to end through the public API with host buffers: per step, upload
     # the state (f64, as upload_channel takes it) from pinned memory, step,
@@ -374,32 +413,38 @@ def run_ours(args):
     e2e = None
     if not args.no_e2e:
         e2e = e2e_run(sim, cr, args, dist, world)
-    sampler.stop()
+    clocks = sampler.summary(t_wall0, t_wall1,
+                             (t_busy0, t_busy1, "autotune, warm-up, timed and profiled steps"))
 
     cpu = step_err = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(cr)
-        step_err = step_error_vs_fp64(sim, cr)
+        step_err = step_errors(checks, cr)
+    sim.close()
 
     peak, peak_kind = peaks()
     bpp = bytes_per_px(C_CH, K_KER)
     step_s = ms / 1e3 / args.steps
     value = world * px * args.steps / (ms / 1e3)
+    built = bytes_per_px_as_built(C_CH, K_KER) * px
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-        "warmup": max(args.warmup, 3), "ms_per_step": ms / args.steps,
+        "warmup": warm, "ms_per_step": ms / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic",
-        "config": {"workload": WORKLOAD, "n": N_GRID, "channels": C_CH, "kernels": K_KER,
-                   "parallelism": f"replicas x{world}",
-                   "l2": "no flush: each step streams ~0.75 GB (> 129 MB L2)"},
+        "config": workload_config(world),
         # every step kernel against the roofline; the kernel with the
         # largest share of the step's device time on top
         "roofline": roofline_object(kms, N_GRID, C_CH, K_KER, peak, peak_kind, load_traffic()),
-        "step_hbm": {"bytes_per_step": bpp * px, "achieved_gbs": bpp * px / step_s / 1e9,
-                     "frac": bpp * px / step_s / 1e9 / peak, "peak_source": peak_kind,
-                     "bytes_per_step_as_built": bytes_per_px_as_built(C_CH, K_KER) * px,
-                     "frac_as_built": bytes_per_px_as_built(C_CH, K_KER) * px / step_s / 1e9 / peak},
+        # the step against HBM: first on the bytes the built passes move,
+        # then on the survey's pass structure (which adds a forward column
+        # pass of 8C B/px that this build fuses away)
+        "step_hbm": {"bytes_per_step_as_built": built,
+                     "achieved_gbs_as_built": built / step_s / 1e9,
+                     "frac_as_built": built / step_s / 1e9 / peak,
+                     "bytes_per_step_algorithmic": bpp * px,
+                     "frac_algorithmic": bpp * px / step_s / 1e9 / peak,
+                     "peak_gbs": peak, "peak_source": peak_kind},
         "kernel_ms": {"row_r2c": kms[0], "col_conv": kms[1], "row_c2r_growth": kms[2],
                       "diffusion": kms[3]},
         "e2e": e2e,
@@ -412,12 +457,20 @@ def run_ours(args):
     }
     if cpu is not None:
         line["cpu_baseline"] = cpu
-        line["step_error_vs_fp64"] = {"max_abs": step_err, "bar": 1e-5,
-                                      "how": "one step from the GPU state after the timed run, "
-                                             "against the FP64 oracle from the same state"}
+        line["step_error_vs_fp64"] = step_err
+    if rank == 0 and world == 1 and not args.no_configs:
+        # the other benchmark configurations, each with bounded repeats
+        dev = torch.device("cuda", local)
+        check = not args.no_cpu_baseline
+        line["plain_1024"] = measure_plain_1024(dev, sampler, check=check)
+        line["batched"] = measure_batched(dev, sampler, steps=500, warmup=3,
+                                          autotune=not args.no_autotune, check=check)
+        line["grad"] = measure_grad(dev, sampler, iters=10, warmup=3, check=check)
+        line["search"] = measure_search(dev, sampler, iters=3, warmup=3, ncand=args.candidates,
+                                        check=check)
+    sampler.stop()
     if rank == 0:
         print(json.dumps(line), flush=True)
-    sim.close()
     if dist is not None:
         dist.destroy_process_group()
     return 0
@@ -483,84 +536,155 @@ def batched_creatures(device):
     return out
 
 
-def run_batched(args):
-    """Batched forward: every world advanced by one persistent launch per
-    phase, one CUDA graph per step; against the plain per-world path."""
+def timed(stream, fn):
+    """Device ms of fn()'s work on `stream` (CUDA events on that stream)."""
     import torch
-    world, rank, local, dist = dist_setup(args.gpus)
-    torch.cuda.set_device(local)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    fn()
+    e1.record(stream)
+    e1.synchronize()
+    return e0.elapsed_time(e1)
+
+
+def measure_plain_1024(dev, sampler, steps=200, check=True):
+    """The first benchmark configuration: one 1024^2 creature, C=3, K=9,
+    ring radii U[12,30] px, `steps` graph steps (autotuned), with teacher-
+    forced FP64 checks at three points of the run and the FP64 mass drift
+    over all of it."""
+    import torch
+    from cella_nova_gb300 import GpuMaceLenia
+    from cella_nova_gb300.creature import make_creature
+    n = 1024
+    cr = make_creature(n, 3, seed=1024, temp=1.0, device=dev)
+    tb0 = time.perf_counter()
+    sim = GpuMaceLenia.from_creature(cr)
+    m0 = sim.mass_f64()
+    checks = {"step 1": sample_step(sim)}
+    sim.autotune(reps=10)
+    sim.run_steps(3)
+    sim.synchronize()
+    stream = torch.cuda.ExternalStream(sim.stream())
+    tw0 = time.perf_counter()
+    ms = timed(stream, lambda: sim.run_steps(steps))
+    tw1 = time.perf_counter()
+    checks[f"step {steps + 5}"] = sample_step(sim)
+    sim.run_steps(steps - 1)
+    checks[f"step {2 * steps + 5}"] = sample_step(sim)
+    m1 = sim.mass_f64()
+    tb1 = time.perf_counter()
+    variants = sim.variants()
+    sim.close()
+    px = n * n
+    out = {"metric": "cell-updates/s (DiffusionLenia fwd step, 1024^2, C=3, K=9)",
+           "value": px * steps / (ms / 1e3), "unit": UNIT, "steps": steps,
+           "ms_per_step": ms / steps, "variants": variants,
+           "hbm_frac_as_built": bytes_per_px_as_built(3, 9) * px / (ms / 1e3 / steps) / 1e9
+           / peaks()[0],
+           "mass_drift": {"steps": 2 * steps + 6, "max_rel": float(np.abs(m1 / m0 - 1).max()),
+                          "reduction": "FP64 on the GPU"},
+           "clocks": sampler.summary(tw0, tw1, (tb0, tb1, "autotune, warm-up, timed and "
+                                                            "checked steps")),
+           "l2": "no flush: each step streams ~0.2 GB (> 129 MB L2)"}
+    if check:
+        out["step_error_vs_fp64"] = step_errors(checks, cr)
+    return out
+
+
+def measure_batched(dev, sampler, steps=500, warmup=3, autotune=True, check=True,
+                    plain_steps=20):
+    """Batched forward: every world advanced by one persistent launch per
+    phase per grid side, one CUDA graph per step; against the plain
+    single-world path on the same worlds, one world at a time."""
+    import torch
     from cella_nova_gb300 import GpuMaceLenia, GpuMaceLeniaBatch
     t0 = time.perf_counter()
-    crs = batched_creatures(torch.device("cuda", local))
+    crs = batched_creatures(dev)
     gen_s = time.perf_counter() - t0
     cells = sum(cr.n * cr.n for cr in crs)
     b = GpuMaceLeniaBatch(crs)
+    m0 = [b.mass_f64(i) for i in range(len(crs))]
     tuned = None
-    if not args.no_autotune:
+    if autotune:
         tuned = {str(k): {"variants": v[0], "ms": np.round(v[1], 4).tolist()}
                  for k, v in b.autotune(reps=5).items()}
     stream = torch.cuda.ExternalStream(b.stream())
-    sampler = ClockSampler(local)
-    sampler.start()
-    b.run_steps(max(args.warmup, 3))
+    b.run_steps(max(warmup, 3))
     b.synchronize()
-    barrier(dist, world)
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
     tw0 = time.perf_counter()
-    e0.record(stream)
-    b.run_steps(args.steps)
-    e1.record(stream)
-    e1.synchronize()
+    ms = timed(stream, lambda: b.run_steps(steps))
     tw1 = time.perf_counter()
-    ms = max_over_ranks(e0.elapsed_time(e1), dist, world)
     clocks = sampler.summary(tw0, tw1)
-    phase_ms = b.profile(min(max(args.steps, 4), 32))
+    phase_ms = b.profile(min(max(steps, 4), 32))
     items, grid = b.info()
+    # one teacher-forced step of one world of each grid side against FP64
+    checks = {}
+    if check:
+        for side in sorted({cr.n for cr in crs}):
+            w = next(i for i, cr in enumerate(crs) if cr.n == side)
+            x = b.state(w)
+            b.run_steps(1)
+            checks[f"world {w} ({side}^2, C={crs[w].C})"] = oracle_step_error(x, b.state(w),
+                                                                              crs[w])
+    drift = max(float(np.abs(b.mass_f64(i) / m0[i] - 1).max()) for i in range(len(crs)))
     b.close()
     # the plain single-world path on the same worlds, one world at a time
     # (each world autotuned like the batch)
-    plain_steps = max(3, min(args.steps, 20))
     plain_s = 0.0
     for cr in crs:
         s = GpuMaceLenia.from_creature(cr)
-        if not args.no_autotune:
+        if autotune:
             s.autotune(reps=3)
         s.run_steps(2)
         s.synchronize()
-        st = torch.cuda.ExternalStream(s.stream())
-        a0 = torch.cuda.Event(enable_timing=True)
-        a1 = torch.cuda.Event(enable_timing=True)
-        a0.record(st)
-        s.run_steps(plain_steps)
-        a1.record(st)
-        a1.synchronize()
-        plain_s += a0.elapsed_time(a1) / 1e3 / plain_steps
+        plain_s += timed(torch.cuda.ExternalStream(s.stream()),
+                         lambda: s.run_steps(plain_steps)) / 1e3 / plain_steps
         s.close()
-    sampler.stop()
-    value = world * cells * args.steps / (ms / 1e3)
-    line = {
+    out = {
         "metric": "cell-updates/s (batched fwd: 48x1024^2 + 16x2048^2, C in 1..4, K=C^2)",
-        "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-        "warmup": max(args.warmup, 3), "ms_per_step": ms / args.steps,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic",
+        "value": cells * steps / (ms / 1e3), "unit": UNIT, "steps": steps,
+        "warmup": max(warmup, 3), "ms_per_step": ms / steps,
         "config": {"workload": "64 worlds (48 at 1024^2, 16 at 2048^2), channels U{1..4}, "
                                "kernels = all pairs, temp U[0.5,2]; one persistent launch per "
-                               "phase, one CUDA graph per step",
+                               "phase per grid side, one CUDA graph per step",
                    "worlds": len(crs), "cells_per_step": cells,
                    "channels": [cr.C for cr in crs]},
-        "plain_loop": {"value": world * cells / plain_s, "unit": UNIT,
-                       "ms_per_step": 1e3 * plain_s,
-                       "how": "same worlds, the single-world graph path one world at a time"},
-        "batched_over_plain": (cells / (ms / 1e3 / args.steps)) / (cells / plain_s),
+        "plain_loop": {"value": cells / plain_s, "unit": UNIT, "ms_per_step": 1e3 * plain_s,
+                       "how": f"same worlds, the single-world graph path one world at a time, "
+                              f"{plain_steps} steps each"},
+        "batched_over_plain": (1e3 * plain_s) / (ms / steps),
         "phase_ms": {"row_r2c": phase_ms[0], "col_conv": phase_ms[1],
                      "row_c2r_growth": phase_ms[2], "diffusion": phase_ms[3]},
         "work_items": items, "persistent_grid": grid, "autotune": tuned,
+        "mass_drift": {"max_rel": drift, "steps": max(warmup, 3) + steps + 32 + len(checks),
+                       "reduction": "FP64 on the GPU, every world"},
         # one persistent launch per phase per grid size
-        "gpu_launches": 4 * len({cr.n for cr in crs}) * args.steps, "clocks": clocks,
+        "gpu_launches": 4 * len({cr.n for cr in crs}) * steps, "clocks": clocks,
         "setup_s": {"generate": gen_s},
     }
+    if checks:
+        out["step_error_vs_fp64"] = {"max_abs": max(checks.values()), "bar": 1e-5,
+                                     "worlds": checks,
+                                     "how": "teacher-forced batched step of one world per grid "
+                                            "side against the FP64 oracle"}
+    return out
+
+
+def run_batched(args):
+    import torch
+    world, rank, local, dist = dist_setup(args.gpus)
+    torch.cuda.set_device(local)
+    sampler = ClockSampler(local)
+    sampler.start()
+    out = measure_batched(torch.device("cuda", local), sampler, steps=args.steps,
+                          warmup=args.warmup, autotune=not args.no_autotune,
+                          check=not args.no_cpu_baseline)
+    sampler.stop()
+    ms = max_over_ranks(out["ms_per_step"] * out["steps"], dist, world)
+    cells = out["config"]["cells_per_step"]
+    line = dict(out, value=world * cells * out["steps"] / (ms / 1e3), n_gpus=world,
+                ms_per_step=ms / out["steps"], higher_is_better=True, scaling="weak",
+                vs_baseline=None, dtype="f32", data="synthetic")
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist is not None:
@@ -568,20 +692,20 @@ def run_batched(args):
     return 0
 
 
-def run_grad(args):
+def measure_grad(dev, sampler, iters=20, warmup=3, check=True):
     """Differentiable unroll: one 1024^2 creature, C=3, K=9, T=64 steps,
     checkpoints every 8; loss = MSE(x_T, seed shifted by (+16, +8) px);
     gradients for the seed, mu, sigma, weights and ring weights through the
-    adjoint kernels.  fwd+bwd cell-updates/s = n^2 T / (forward + backward)."""
+    adjoint kernels.  fwd+bwd cell-updates/s = n^2 T / (forward + backward).
+    The gradient check runs the same construction on the 128^2 instance
+    (T=64, checkpoints every 8) against FP64 autograd."""
     import torch
-    world, rank, local, dist = dist_setup(args.gpus)
-    torch.cuda.set_device(local)
     from cella_nova_gb300.autograd import DiffusionLeniaGPU
     from cella_nova_gb300.creature import make_creature
     n, C, T, every = 1024, 3, 64, 8
-    cr = make_creature(n, C, seed=1024 + rank, temp=1.0, device=torch.device("cuda", local))
+    cr = make_creature(n, C, seed=1024, temp=1.0, device=dev)
     target = torch.tensor(np.roll(cr.seed, (8, 16), axis=(1, 2)), dtype=torch.float32,
-                          device="cuda")
+                          device=dev)
     m = DiffusionLeniaGPU(cr)
 
     def iteration():
@@ -589,15 +713,15 @@ def run_grad(args):
         xT = m(T, every)
         loss = torch.mean((xT - target) ** 2)
         loss.backward()
-        return loss
+        return loss, xT
 
-    for _ in range(max(args.warmup, 3)):
+    tb0 = time.perf_counter()
+    for _ in range(max(warmup, 3)):
         iteration()
     torch.cuda.synchronize()
-    barrier(dist, world)
-    iters = max(1, min(args.steps, 20))
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
     f_ms = b_ms = 0.0
+    tw0 = time.perf_counter()
     for _ in range(iters):
         m.zero_grad(set_to_none=True)
         ev[0].record()
@@ -609,15 +733,17 @@ def run_grad(args):
         ev[2].synchronize()
         f_ms += ev[0].elapsed_time(ev[1])
         b_ms += ev[1].elapsed_time(ev[2])
+    tw1 = time.perf_counter()
     f_ms, b_ms = f_ms / iters, b_ms / iters
-    tot = max_over_ranks(f_ms + b_ms, dist, world)
-    line = {
+    # mass of x_T against the seed's, FP64 on the GPU
+    mT = xT.detach().double().sum(dim=(1, 2))
+    m0 = m.seed.detach().double().sum(dim=(1, 2))
+    drift = float((mT / m0 - 1).abs().max())
+    out = {
         "metric": "cell-updates/s (fwd+bwd, differentiable unroll 1024^2, C=3, K=9, T=64, "
                   "checkpoints every 8)",
-        "value": world * n * n * T / (tot / 1e3), "unit": UNIT, "n_gpus": world,
-        "steps": iters, "warmup": max(args.warmup, 3), "ms_per_step": tot,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic",
+        "value": n * n * T / ((f_ms + b_ms) / 1e3), "unit": UNIT, "steps": iters,
+        "warmup": max(warmup, 3), "ms_per_step": f_ms + b_ms,
         "config": {"workload": "1 creature 1024^2, 3 channels, 9 kernels, T=64, checkpoint every "
                                "8 (backward recomputes each segment), loss MSE vs seed shifted "
                                "(+16,+8) px; grads: seed, mu, sigma, weights, ring weights",
@@ -629,8 +755,64 @@ def run_grad(args):
         # build 4 + parameter fold 1 in each direction; 2 final kernel-gradient
         # and 2 ring-gradient launches
         "gpu_launches": 13 * T - (T + every - 1) // every + 14,
-        "loss": float(loss.detach()),
+        "loss": float(loss.detach()), "mass_drift": {"max_rel": drift, "steps": T,
+                                                     "reduction": "FP64 on the GPU"},
+        "clocks": sampler.summary(tw0, tw1, (tb0, tw1, "warm-up and timed iterations")),
     }
+    del m
+    if check:
+        out["grad_check"] = grad_check_128(dev)
+    return out
+
+
+def grad_check_128(dev, T=64, every=8):
+    """The GPU gradients of the differentiable unroll on the 128^2 instance
+    (C=3, K=9, T=64, checkpoints every 8) against FP64 autograd of the step
+    (oracle/autograd_ref.py, itself pinned to the reference model's autograd
+    and to finite differences), relative to each gradient's largest
+    component."""
+    import torch
+    from cella_nova_gb300.autograd import DiffusionLeniaGPU
+    from cella_nova_gb300.creature import make_creature
+    from oracle import autograd_ref as AR
+    n = 128
+    cr = make_creature(n, 3, seed=128, radius=(n / 16, n / 6), seed_box=n // 2, temp=1.0)
+    target = AR.shifted_target(cr.seed)
+    t0 = time.perf_counter()
+    ref = AR.gradients(cr, T, target)
+    el = time.perf_counter() - t0
+    m = DiffusionLeniaGPU(cr)
+    xT = m(T, every)
+    loss = torch.mean((xT - torch.tensor(target, dtype=torch.float32, device=dev)) ** 2)
+    loss.backward()
+
+    def rel(a, b):
+        a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
+        return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-30))
+
+    err = {"seed": rel(m.seed.grad.cpu(), ref["seed"]), "mu": rel(m.mu.grad.cpu(), ref["mu"]),
+           "sigma": rel(m.sigma.grad.cpu(), ref["sigma"]),
+           "weights": rel(m.weights.grad.cpu(), ref["weights"]),
+           "ring_weights": rel(np.concatenate([b.grad.cpu().numpy() for b in m.ring_weights]),
+                               np.concatenate(ref["ring_weights"]))}
+    return {"instance": f"{n}^2, C=3, K=9, T={T}, checkpoints every {every}",
+            "max_rel_error": err, "loss_rel_error": abs(float(loss.detach()) / ref["loss"] - 1),
+            "oracle_s": el}
+
+
+def run_grad(args):
+    import torch
+    world, rank, local, dist = dist_setup(args.gpus)
+    torch.cuda.set_device(local)
+    sampler = ClockSampler(local)
+    sampler.start()
+    out = measure_grad(torch.device("cuda", local), sampler, iters=max(1, min(args.steps, 20)),
+                       warmup=args.warmup, check=not args.no_cpu_baseline and world == 1)
+    sampler.stop()
+    tot = max_over_ranks(out["ms_per_step"], dist, world)
+    line = dict(out, value=world * 1024 * 1024 * 64 / (tot / 1e3), n_gpus=world,
+                ms_per_step=tot, higher_is_better=True, scaling="weak", vs_baseline=None,
+                dtype="f32", data="synthetic")
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist is not None:
@@ -638,54 +820,44 @@ def run_grad(args):
     return 0
 
 
-def run_search(args):
-    """Batched gradient search: 32 candidates at 1024^2, C=3, K=9, T=128,
-    checkpoints every 16, MSE to the seed shifted by (+16, +8) px, Adam on
-    the seed, mu, sigma, weights and ring weights; every iteration of all
-    candidates is one CUDA graph (Adam included).  fwd+bwd cell-updates/s =
-    candidates * n^2 * T / iteration time, against the plain per-creature
-    loop (torch autograd over the same kernels + torch.optim.Adam, one
-    candidate at a time)."""
+def measure_search(dev, sampler, iters=3, warmup=3, ncand=32, check=True):
+    """Batched gradient search: `ncand` candidates at 1024^2, C=3, K=9,
+    T=128, checkpoints every 16, MSE to the seed shifted by (+16, +8) px,
+    Adam on the seed, mu, sigma, weights and ring weights; every iteration of
+    all candidates is one CUDA graph (Adam included).  fwd+bwd cell-updates/s
+    = candidates * n^2 * T / iteration time, against the plain per-creature
+    loop over every candidate (torch autograd over the same kernels +
+    torch.optim.Adam, one candidate at a time)."""
     import torch
-    world, rank, local, dist = dist_setup(args.gpus)
-    torch.cuda.set_device(local)
     from cella_nova_gb300 import _abi
     from cella_nova_gb300.autograd import DiffusionLeniaGPU
     from cella_nova_gb300.creature import make_creature
     from cella_nova_gb300.search import AdamConfig, GradientSearch
-    n, C, T, every, ncand = 1024, 3, 128, 16, args.candidates
+    n, C, T, every = 1024, 3, 128, 16
     t0 = time.perf_counter()
-    dev = torch.device("cuda", local)
-    crs = [make_creature(n, C, seed=5000 + 100 * rank + i, temp=1.0, device=dev)
-           for i in range(ncand)]
+    crs = [make_creature(n, C, seed=5000 + i, temp=1.0, device=dev) for i in range(ncand)]
     tgs = [np.roll(cr.seed, (8, 16), axis=(1, 2)) for cr in crs]
     gen_s = time.perf_counter() - t0
     adam = AdamConfig(lr_seed=1e-3, lr_params=1e-3, lr_rings=1e-2)
-    sampler = ClockSampler(local)
-    sampler.start()
     gs = GradientSearch(crs, tgs, T=T, every=every, adam=adam, n_streams=4)
-    warm = max(args.warmup, 3)
+    warm = max(warmup, 3)
     gs.run(1)                         # the first iteration eagerly (allocates scratch)
     loss_first = float(np.mean(gs.losses()))
     gs.run(warm - 1)                  # capture, then replays
     torch.cuda.synchronize()
-    barrier(dist, world)
-    iters = max(1, args.steps)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    t_wall0 = time.perf_counter()
+    tw0 = time.perf_counter()
     e0.record()
     gs.run(iters)
     e1.record()
     e1.synchronize()
-    t_wall1 = time.perf_counter()
-    barrier(dist, world)
-    ms = max_over_ranks(e0.elapsed_time(e1), dist, world) / iters
-    clocks = sampler.summary(t_wall0, t_wall1)
+    tw1 = time.perf_counter()
+    ms = e0.elapsed_time(e1) / iters
+    clocks = sampler.summary(tw0, tw1)
     losses = gs.losses()
-    # mass of x_T against the seed it started from, FP64 on the GPU
+    # mass of x_T of the last iteration against the x_0 it was unrolled from
+    # (the first checkpoint), FP64 on the GPU
     lib = _abi.load()
-    # (x_T of the last iteration against the x_0 it was unrolled from, the
-    # first checkpoint)
     drift = 0.0
     m0 = torch.zeros(C, dtype=torch.float64, device=dev)
     m1 = torch.zeros_like(m0)
@@ -699,45 +871,34 @@ def run_search(args):
         drift = max(drift, float((m1 / m0 - 1).abs().max()))
     gs.close()
 
-    # plain per-creature loop: torch autograd over the same adjoint kernels
-    # and torch.optim.Adam, one candidate at a time (no graphs)
-    plain_cands = min(ncand, 4)
+    # plain per-creature loop over every candidate: torch autograd over the
+    # same adjoint kernels and torch.optim.Adam, one candidate at a time (no
+    # graphs); each candidate's first iteration is its warm-up
+    tgt = [torch.tensor(tg, dtype=torch.float32, device=dev) for tg in tgs]
     plain_ms = 0.0
-    tgt = [torch.tensor(tg, dtype=torch.float32, device=dev) for tg in tgs[:plain_cands]]
-    models = [DiffusionLeniaGPU(cr) for cr in crs[:plain_cands]]
-    opts = [torch.optim.Adam([{"params": [m.seed], "lr": adam.lr_seed},
-                              {"params": [m.mu, m.sigma, m.weights], "lr": adam.lr_params},
-                              {"params": list(m.ring_weights), "lr": adam.lr_rings}])
-            for m in models]
+    for i in range(ncand):
+        mdl = DiffusionLeniaGPU(crs[i])
+        opt = torch.optim.Adam([{"params": [mdl.seed], "lr": adam.lr_seed},
+                                {"params": [mdl.mu, mdl.sigma, mdl.weights],
+                                 "lr": adam.lr_params},
+                                {"params": list(mdl.ring_weights), "lr": adam.lr_rings}])
 
-    def plain_iteration(i):
-        m, opt = models[i], opts[i]
-        opt.zero_grad(set_to_none=True)
-        loss = torch.mean((m(T, every) - tgt[i]) ** 2)
-        loss.backward()
-        opt.step()
+        def plain_iteration():
+            opt.zero_grad(set_to_none=True)
+            loss = torch.mean((mdl(T, every) - tgt[i]) ** 2)
+            loss.backward()
+            opt.step()
 
-    for i in range(plain_cands):
-        plain_iteration(i)
-    torch.cuda.synchronize()
-    p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    p0.record()
-    for i in range(plain_cands):
-        plain_iteration(i)
-    p1.record()
-    p1.synchronize()
-    plain_ms = p0.elapsed_time(p1) / plain_cands * ncand    # per iteration of all candidates
-    del models, opts
-    sampler.stop()
-
+        plain_iteration()
+        torch.cuda.synchronize()
+        plain_ms += timed(torch.cuda.current_stream(), plain_iteration)
+        del mdl, opt
     cells = ncand * n * n * T
-    value = world * cells / (ms / 1e3)
-    line = {
+    out = {
         "metric": "cell-updates/s (batched gradient search fwd+bwd: 32 x 1024^2, C=3, K=9, "
                   "T=128, checkpoints every 16, in-graph Adam)",
-        "value": value, "unit": UNIT, "n_gpus": world, "steps": iters, "warmup": warm,
-        "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32", "data": "synthetic",
+        "value": cells / (ms / 1e3), "unit": UNIT, "steps": iters, "warmup": warm,
+        "ms_per_step": ms,
         "config": {"workload": f"{ncand} candidates 1024^2, 3 channels, 9 kernels (all pairs), "
                                "ring kernels built on the GPU each iteration, T=128, checkpoint "
                                "every 16, loss MSE vs seed shifted (+16,+8) px, Adam on seed, "
@@ -745,15 +906,15 @@ def run_search(args):
                                "over 4 streams",
                    "step_unit": "one iteration (forward, backward, Adam) of every candidate",
                    "candidates": ncand},
-        "plain_loop": {"value": world * cells / (plain_ms / 1e3), "unit": UNIT,
-                       "ms_per_step": plain_ms,
-                       "how": f"torch autograd + torch.optim.Adam per candidate, "
-                              f"{plain_cands} candidates timed and scaled to {ncand}"},
+        "plain_loop": {"value": cells / (plain_ms / 1e3), "unit": UNIT, "ms_per_step": plain_ms,
+                       "how": f"torch autograd + torch.optim.Adam, one candidate at a time, "
+                              f"all {ncand} candidates timed (one iteration each after one "
+                              f"warm-up iteration)"},
         "batched_over_plain": plain_ms / ms,
         "loss_mean": float(np.mean(losses)),
         "loss_mean_first_iteration": loss_first,
         "iterations_total": warm + iters,
-        "mass_drift_max": drift,
+        "mass_drift": {"max_rel": drift, "steps": T, "reduction": "FP64 on the GPU"},
         # per candidate and iteration: builder 4, parameter fold 1, forward 4
         # per step, MSE 2, segment recompute 4 per step (3 for a segment's
         # last), backward 5 per step, kernel gradient 2, ring gradient 2, Adam
@@ -762,8 +923,26 @@ def run_search(args):
         "clocks": clocks,
         "setup_s": {"generate": gen_s},
     }
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        line["cpu_baseline"], line["grad_check"] = search_cpu_check(args)
+    if check:
+        out["cpu_baseline"], out["grad_check"] = search_cpu_check()
+    return out
+
+
+def run_search(args):
+    import torch
+    world, rank, local, dist = dist_setup(args.gpus)
+    torch.cuda.set_device(local)
+    sampler = ClockSampler(local)
+    sampler.start()
+    out = measure_search(torch.device("cuda", local), sampler, iters=max(1, args.steps),
+                         warmup=args.warmup, ncand=args.candidates,
+                         check=not args.no_cpu_baseline and world == 1)
+    sampler.stop()
+    ms = max_over_ranks(out["ms_per_step"], dist, world)
+    cells = out["config"]["candidates"] * 1024 * 1024 * 128
+    line = dict(out, value=world * cells / (ms / 1e3), n_gpus=world, ms_per_step=ms,
+                higher_is_better=True, scaling="weak", vs_baseline=None, dtype="f32",
+                data="synthetic")
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist is not None:
@@ -771,7 +950,7 @@ def run_search(args):
     return 0
 
 
-def search_cpu_check(args):
+def search_cpu_check():
     """CPU leg: the FP64 autograd oracle (torch, float64, all host threads)
     on a bounded sample -- one 128^2 candidate, C=3, K=9, T=16, checkpoints
     every 4 -- timed as fwd+bwd cell-updates/s, and used to check
@@ -823,6 +1002,8 @@ def main():
                     help="fixed CTA-shape variants r2c,col,c2r,diffusion (skips the autotuner)")
     ap.add_argument("--config", default="plain", choices=["plain", "batched", "grad", "search"])
     ap.add_argument("--candidates", type=int, default=32)
+    ap.add_argument("--no-configs", action="store_true",
+                    help="default run: skip the sub-objects of the other configurations")
     args = ap.parse_args()
     if args.steps is None:
         args.steps = {"plain": 4000, "batched": 500, "grad": 20, "search": 3}[args.config]

@@ -1,7 +1,7 @@
 """ctypes binding of include/cella_gpu.h (libcella_gpu.so, built in-tree).
 
-This is the same C ABI a Rust host binds; Python uses it for
-tests, the benchmark and the torch autograd wrapper.  There is no fallback:
+This is the same C ABI a Rust host binds with `extern "C"` declarations;
+Python uses it for tests, the benchmark and the torch autograd wrapper.  There is no fallback:
 if the library cannot be loaded, every call raises.
 """
 from __future__ import annotations
@@ -9,6 +9,8 @@ from __future__ import annotations
 import ctypes
 import os
 
+# variants per phase in the autotuner's tables (CG_MAX_VARIANTS)
+MAX_VARIANTS = 5
 _PKG = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_PKG, "libcella_gpu.so")
 
@@ -116,6 +118,7 @@ SIGNATURES = {
     "cg_batch_stream": ([_P, ctypes.POINTER(_P)], _I),
     "cg_batch_info": ([_P, ctypes.POINTER(_I), ctypes.POINTER(_I)], _I),
     "cg_batch_autotune": ([_P, _I, ctypes.POINTER(_I), _DP], _I),
+    "cg_batch_set_variants": ([_P, _I, ctypes.POINTER(_I)], _I),
     "cg_load_config_json": ([ctypes.c_char_p, ctypes.POINTER(cg_config)], _I),
     "cg_free_config": ([ctypes.POINTER(cg_config)], None),
     "cg_load_config_bin": ([ctypes.c_char_p, ctypes.POINTER(cg_config)], _I),

@@ -63,9 +63,9 @@ class LeniaWorld:
             self.h = None
 
     def autotune(self, reps: int = 5):
-        """Pick the fastest CTA shape of every phase (cg_autotune); the adjoint
-        kernels follow the forward phases' choice.  Returns the variants."""
-        ms = np.zeros(12, dtype=np.float64)
+        """Pick the fastest variant of every phase (cg_autotune); the adjoint
+        kernels follow the forward phases' CTA shapes.  Returns the variants."""
+        ms = np.zeros(4 * _abi.MAX_VARIANTS, dtype=np.float64)
         chosen = (ctypes.c_int * 4)()
         check(self.lib.cg_autotune(self.h, int(reps), ms.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
                                    chosen))

@@ -513,9 +513,14 @@ cudaError_t launch_backward(const BwdArgs& a, cudaStream_t st) {
         if (e != cudaSuccess) return e;
     }
     launch_diff_bwd<LOGN, kDiffBwdVariant>(a, st);
-    CG_VARIANT_SWITCH(a.var.c2r, launch_growth_bwd, a, st)
-    CG_VARIANT_SWITCH(a.var.col, launch_col_adj, a, st)
-    CG_VARIANT_SWITCH(a.var.c2r, launch_c2r_add, a, st)
+    // the adjoint kernels exist in the CTA shapes of variants 0-2: the plan
+    // variants take the shape they share (row passes: two rows per CTA as
+    // in variant 2; column pass: Geo::CVS)
+    const int vrow = a.var.c2r > 2 ? 2 : a.var.c2r;
+    const int vcol = a.var.col == 3 ? 1 : (a.var.col == 4 ? 0 : a.var.col);
+    CG_VARIANT_SWITCH(vrow, launch_growth_bwd, a, st)
+    CG_VARIANT_SWITCH(vcol, launch_col_adj, a, st)
+    CG_VARIANT_SWITCH(vrow, launch_c2r_add, a, st)
     return cudaGetLastError();
 }
 

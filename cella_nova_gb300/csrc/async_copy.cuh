@@ -118,11 +118,32 @@ __device__ __forceinline__ void cp_async_wait() {
     asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
 }
 
-// Reciprocal to ~1 ulp (MUFU); callers refine with an exact remainder.
+// Reciprocal estimate to ~1 ulp (MUFU); div_head_tail refines it.
 __device__ __forceinline__ float rcp_approx(float x) {
     float r;
     asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
     return r;
+}
+
+// q = x / (zh + zt) for a head zh and a tail zt with |zt| <= |zh|, close to
+// correctly rounded, from two published methods:
+//  * Fast2Sum (T. J. Dekker, "A floating-point technique for extending the
+//    available precision", Numer. Math. 18 (1971) 224-242): with
+//    z = fl(zh + zt), zl = zt - (z - zh) is exact and z + zl == zh + zt;
+//  * one quotient correction with the fused multiply-add remainder
+//    (P. Markstein, "Computation of elementary functions on the IBM RISC
+//    System/6000 processor", IBM J. Res. Dev. 34 (1990) 111-119): for
+//    q0 = fl(x r) with r close to 1/z, x - q0 z is exact in one fma, and
+//    q0 + (rem - q0 zl) r corrects q0 for its own rounding and for the
+//    tail zl of the divisor.
+// r is the hardware reciprocal estimate (rcp.approx.ftz.f32).
+__device__ __forceinline__ float div_head_tail(float x, float zh, float zt) {
+    const float z = zh + zt;
+    const float zl = zt - (z - zh);
+    const float r = rcp_approx(z);
+    const float q0 = x * r;
+    const float rem = fmaf(-q0, z, x);
+    return fmaf(rem - q0 * zl, r, q0);
 }
 
 // 2^x to a few ulp (MUFU); subnormal results flush to zero.

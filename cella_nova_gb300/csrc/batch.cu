@@ -27,10 +27,12 @@ namespace cg {
 constexpr int kBatchMinLogN = 6;   // 64^2 .. 2048^2 in one batch
 constexpr int kBatchMaxLogN = 11;
 
+constexpr int kVariants = 5;   // per phase; diffusion and sides below 512 have 3
+
 struct WorldDesc {
     // tensor maps of U for the inverse row pass's tile copies, one per
     // variant (rows per tile)
-    CUtensorMap umap[3];
+    CUtensorMap umap[kVariants];
     int logn, C, K;
     float temp;
     float* state[2];
@@ -43,10 +45,14 @@ struct WorldDesc {
     GrowthParams gp;
 };
 
-// Rows per inverse-row-pass tile of a size and variant (Geo<LOGN, V>::RB).
+// Rows per inverse-row-pass tile of a size and variant (C2RShape::RB).
 template <int LOGN>
 int row_tile_rows(int v) {
-    return v == 0 ? Geo<LOGN, 0>::RB : (v == 1 ? Geo<LOGN, 1>::RB : Geo<LOGN, 2>::RB);
+    if constexpr (LOGN >= kMinPairLogN) {
+        if (v == 3) return C2RShape<LOGN, 3>::RB;
+        if (v == 4) return C2RShape<LOGN, 4>::RB;
+    }
+    return v == 1 ? Geo<LOGN, 1>::RB : (v == 2 ? Geo<LOGN, 2>::RB : Geo<LOGN, 0>::RB);
 }
 int row_tile_rows(int logn, int v) {
     switch (logn) {
@@ -72,7 +78,7 @@ struct WorkItem {
 // ...  The variants are the single-world kernels' (Geo<LOGN, V>), with the same
 // bits.
 template <int LOGN, int V>
-__global__ void __launch_bounds__(Geo<LOGN, V>::RT, 512 / Geo<LOGN, V>::RT)
+__global__ void __launch_bounds__(R2CShape<LOGN, V>::RT, R2CShape<LOGN, V>::MINB)
     kb_row_r2c(const WorldDesc* __restrict__ worlds, const WorkItem* __restrict__ items, int count,
                int parity) {
     extern __shared__ __align__(128) float2 smb_r2c[];
@@ -80,7 +86,7 @@ __global__ void __launch_bounds__(Geo<LOGN, V>::RT, 512 / Geo<LOGN, V>::RT)
         __syncthreads();
         const WorkItem it = items[i];
         const WorldDesc& w = worlds[it.world];
-        row_r2c_body<LOGN, V>(w.state[parity], w.rowspec, w.tw, it.c, it.a, smb_r2c);
+        row_r2c_variant<LOGN, V>(w.state[parity], w.rowspec, w.tw, it.c, it.a, smb_r2c);
     }
 }
 
@@ -103,7 +109,7 @@ __global__ void __launch_bounds__(Geo<LOGN, V>::CT, 512 / Geo<LOGN, V>::CT)
 }
 
 template <int LOGN, int V>
-__global__ void __launch_bounds__(Geo<LOGN, V>::RT, 512 / Geo<LOGN, V>::RT)
+__global__ void __launch_bounds__(C2RShape<LOGN, V>::RT, C2RShape<LOGN, V>::MINB)
     kb_row_c2r_growth(const WorldDesc* __restrict__ worlds, const WorkItem* __restrict__ items,
                       int count, int* err) {
     extern __shared__ __align__(128) float2 smb_c2r[];
@@ -114,9 +120,9 @@ __global__ void __launch_bounds__(Geo<LOGN, V>::RT, 512 / Geo<LOGN, V>::RT)
         __syncthreads();
         const WorkItem it = items[i];
         const WorldDesc& w = worlds[it.world];
-        if (!row_c2r_growth_body<LOGN, V>(&w.umap[V], true, w.A, w.tw, w.groups, w.gp,
-                                          w.temp, nullptr, 0.f, it.c, it.a, smb_c2r, &bar, phase,
-                                          err))
+        if (!row_c2r_growth_variant<LOGN, V>(&w.umap[V], true, w.A, w.tw, w.groups, w.gp,
+                                             w.temp, nullptr, 0.f, it.c, it.a, smb_c2r, &bar,
+                                             phase, err))
             return;   // a bounded wait timed out (uniform across the block)
     }
 }
@@ -135,8 +141,6 @@ __global__ void __launch_bounds__(DiffTile<LOGN, V>::THREADS)
     }
 }
 
-constexpr int kVariants = 3;
-
 // Per size and variant: the four kernels, their block sizes, shared memory
 // and the unit each work item covers.
 struct PhaseVariant {
@@ -146,22 +150,31 @@ struct PhaseVariant {
     int unit_a, unit_b;   // rows per item (row phases), columns per item (column
                           // phase), tile width and height (diffusion)
 };
+// pv[p][v].fn == nullptr: phase p has no variant v at this size.
 template <int LOGN, int V>
 void fill_variant(PhaseVariant (&pv)[4][kVariants]) {
     using G = Geo<LOGN, V>;
-    using D = DiffTile<LOGN, V>;
-    pv[0][V] = {reinterpret_cast<const void*>(kb_row_r2c<LOGN, V>), G::RT, G::R2C_SMEM, G::RB, 0};
+    using R = R2CShape<LOGN, V>;
+    using Q = C2RShape<LOGN, V>;
+    pv[0][V] = {reinterpret_cast<const void*>(kb_row_r2c<LOGN, V>), R::RT, R::SMEM, R::RB, 0};
     pv[1][V] = {reinterpret_cast<const void*>(kb_col_conv<LOGN, V>), G::CT, G::COL_SMEM, G::TW, 0};
-    pv[2][V] = {reinterpret_cast<const void*>(kb_row_c2r_growth<LOGN, V>), G::RT, G::C2R_SMEM,
-                G::RB, 0};
-    pv[3][V] = {reinterpret_cast<const void*>(kb_diffusion<LOGN, V>), D::THREADS, D::SMEM, D::TX,
-                D::TY};
+    pv[2][V] = {reinterpret_cast<const void*>(kb_row_c2r_growth<LOGN, V>), Q::RT, Q::SMEM, Q::RB,
+                0};
+    if constexpr (V <= 2) {
+        using D = DiffTile<LOGN, V>;
+        pv[3][V] = {reinterpret_cast<const void*>(kb_diffusion<LOGN, V>), D::THREADS, D::SMEM,
+                    D::TX, D::TY};
+    }
 }
 template <int LOGN>
 void fill_size(PhaseVariant (&pv)[4][kVariants]) {
     fill_variant<LOGN, 0>(pv);
     fill_variant<LOGN, 1>(pv);
     fill_variant<LOGN, 2>(pv);
+    if constexpr (LOGN >= kMinPairLogN) {
+        fill_variant<LOGN, 3>(pv);
+        fill_variant<LOGN, 4>(pv);
+    }
 }
 static void phase_variants_for(int logn, PhaseVariant (&pv)[4][kVariants]) {
     switch (logn) {
@@ -440,8 +453,7 @@ int cg_batch_create(int n_worlds, const int* n, const int* C, const int* K, cons
         d.tw = b->tw_by_logn[W.logn];
         d.groups = W.groups;
         d.gp = W.gp;
-        static_assert(kVariants == 3, "one map per variant");
-        for (int m = 0; m < kVariants && rc == CG_OK; ++m)
+        for (int m = 0; m < phase_variant_count(W.logn, 2) && rc == CG_OK; ++m)
             chk(encode_u_map(&d.umap[m], W.U, W.n, W.K, row_tile_rows(W.logn, m)),
                 "encoding a tensor map of U");
     }
@@ -461,7 +473,7 @@ int cg_batch_create(int n_worlds, const int* n, const int* C, const int* K, cons
         sc.logn = logn;
         phase_variants_for(logn, sc.pv);
         for (int p = 0; p < 4 && rc == CG_OK; ++p)
-            for (int v = 0; v < kVariants && rc == CG_OK; ++v) {
+            for (int v = 0; v < phase_variant_count(logn, p) && rc == CG_OK; ++v) {
                 const PhaseVariant& pv = sc.pv[p][v];
                 std::vector<WorkItem> list;
                 for (int w = 0; w < n_worlds; ++w) {
@@ -648,6 +660,22 @@ int cg_batch_info(cg_batch* b, int* items4, int* grid4) {
     return CG_OK;
 }
 
+int cg_batch_set_variants(cg_batch* b, int n, const int v[4]) {
+    if (!b || !v) return fail(CG_ERR_ARG, "cg_batch_set_variants: NULL argument");
+    for (auto& sc : b->classes) {
+        if ((1 << sc.logn) != n) continue;
+        for (int p = 0; p < 4; ++p)
+            if (v[p] < 0 || v[p] >= phase_variant_count(sc.logn, p))
+                return fail(CG_ERR_ARG, "variant %d of phase %d outside [0, %d] at grid side %d",
+                            v[p], p, phase_variant_count(sc.logn, p) - 1, n);
+        BCHECK(cudaStreamSynchronize(b->stream), "cudaStreamSynchronize");
+        for (int p = 0; p < 4; ++p) sc.var[p] = v[p];
+        BCHECK(capture_batch_graphs(b), "re-capturing the batched step graph");
+        return CG_OK;
+    }
+    return fail(CG_ERR_ARG, "the batch has no world of grid side %d", n);
+}
+
 int cg_batch_autotune(cg_batch* b, int reps, int* chosen, double* ms_out) {
     if (!b) return fail(CG_ERR_ARG, "cg_batch_autotune: NULL handle");
     if (reps < 1 || reps > 1000)
@@ -657,7 +685,7 @@ int cg_batch_autotune(cg_batch* b, int reps, int* chosen, double* ms_out) {
     if (chosen)
         for (int i = 0; i < kSizes * 4; ++i) chosen[i] = -1;
     if (ms_out)
-        for (int i = 0; i < kSizes * 4 * kVariants; ++i) ms_out[i] = 0.0;
+        for (int i = 0; i < kSizes * 4 * kVariants; ++i) ms_out[i] = -1.0;
     // Each phase of a size class reads the state or the scratch the previous
     // phases wrote; run in order on the live batch, the state is untouched
     // (diffusion writes the spare ping-pong buffer only).
@@ -666,7 +694,7 @@ int cg_batch_autotune(cg_batch* b, int reps, int* chosen, double* ms_out) {
         for (int p = 0; p < 4; ++p) {
             double t[kVariants];
             int best = 0;
-            for (int v = 0; v < kVariants; ++v) {
+            for (int v = 0; v < phase_variant_count(sc.logn, p); ++v) {
                 for (int q = 0; q < p; ++q)
                     BCHECK(launch_class_phase(b, sc, q, sc.var[q], b->cur, b->stream),
                            "autotune prologue");

@@ -30,10 +30,18 @@ struct GrowthParams {
     float wsum[kMaxC];
 };
 
-// CTA-shape variant of each phase (0 = default); the autotuner picks them.
+// Variant of each phase (0 = default); the autotuner picks them.  Variants
+// 0-2 are CTA shapes with the same bits; 3 and 4 (row and column phases,
+// grid sides from 2^kMinPairLogN) change the FFT plans (step_kernels.cuh).
 struct Variants {
     int r2c = 0, col = 0, c2r = 0, diff = 0;
 };
+constexpr int kMinPairLogN = 9;
+constexpr int kMaxVariants = 5;
+// Variants phase p (0 r2c, 1 col, 2 c2r, 3 diffusion) has at side 2^logn.
+__host__ __device__ constexpr int phase_variant_count(int logn, int phase) {
+    return (phase == 3 || logn < kMinPairLogN) ? 3 : kMaxVariants;
+}
 
 // Everything one step's launches need.  Planar layouts, all device pointers:
 //   x_in, x_out : [C][n][n] f32 state (ping-pong)

@@ -153,6 +153,16 @@ __host__ __device__ constexpr int last_radix(int L, int MR = 16) {
     return r;
 }
 
+// Radix of the last pass of a greedy or remainder-first plan.
+__host__ __device__ constexpr int plan_last_radix(int L, bool remfirst, int MR = 16) {
+    int ns = 1, r = 1;
+    while (ns < L) {
+        r = plan_radix(L, ns, remfirst, MR);
+        ns *= r;
+    }
+    return r;
+}
+
 // One Stockham pass (radix R, sub-transform size NS) over S sequences of
 // length L, with T threads.  Work item `item` = (sequence s, butterfly j):
 // s = item / J, j = item % J, or with SFAST the sequence index runs fastest,
@@ -260,5 +270,24 @@ struct FftPasses {
         }
     }
 };
+
+// Run the first pass of a transform, then `hook()`, then the rest.
+// FIRSTBAR / LASTBAR as in FftPasses.
+template <int L, bool INV, int T, int S, bool REMFIRST, int MR = 16, bool SFAST = false,
+          bool FIRSTBAR = true, bool LASTBAR = true, class LD, class SMLD, class SMST, class STL,
+          class HOOK>
+__device__ __forceinline__ void fft_with_hook(LD& ld, SMLD& smld, SMST& smst, STL& stl,
+                                              const float2* __restrict__ tab, HOOK hook) {
+    constexpr int R = PassRadix<L, 1, REMFIRST, MR>::R;
+    if constexpr (R == L) {
+        stockham_pass<L, R, 1, INV, T, S, SFAST, FIRSTBAR || LASTBAR>(ld, stl, tab);
+        hook();
+    } else {
+        stockham_pass<L, R, 1, INV, T, S, SFAST, FIRSTBAR>(ld, smst, tab);
+        hook();
+        FftPasses<L, R, INV, T, S, REMFIRST, MR, SFAST, true, LASTBAR>::run(smld, smld, smst, stl,
+                                                                             tab);
+    }
+}
 
 }  // namespace cg

@@ -70,7 +70,8 @@ int cuda_fail(cudaError_t e, const char* what) {
 
 // W_n^m for m < n, then the Stockham pass tables (fft.cuh tw_offset layout)
 // of the column forward plan (greedy), the column inverse plan (remainder
-// first) and the row plan (greedy, length n/2).  Every entry is rounded once
+// first), the row plan (greedy, length n/2) and the radix-8 plan of length n
+// (greedy).  Every entry is rounded once
 // from double; the reference builds its table from an f32 angle
 // (convolution.rs:19-30).
 static void fill_plan(int L, bool remfirst, int MR, float2* out) {
@@ -100,6 +101,8 @@ void build_twiddle_tables(int n, float2* out) {
     fill_plan(n, true, 16, p);
     p += tw_size(n, true);
     fill_plan(n / 2, false, 16, p);
+    p += tw_size(n / 2, false);
+    fill_plan(n, false, 8, p);
 }
 
 static bool finite(float v) { return std::isfinite(v); }
@@ -1167,7 +1170,9 @@ int cg_unroll_backward(cg_sim* s, const float* ckpt, int T, int every, const flo
 int cg_set_variants(cg_sim* s, const int v[4]) {
     if (!s || !v) return fail(CG_ERR_ARG, "cg_set_variants: NULL argument");
     for (int p = 0; p < 4; ++p)
-        if (v[p] < 0 || v[p] > 2) return fail(CG_ERR_ARG, "variant %d of phase %d outside [0, 2]", v[p], p);
+        if (v[p] < 0 || v[p] >= phase_variant_count(s->logn, p))
+            return fail(CG_ERR_ARG, "variant %d of phase %d outside [0, %d] at grid side %d", v[p],
+                        p, phase_variant_count(s->logn, p) - 1, s->n);
     CG_CHECK(cudaStreamSynchronize(s->stream), "cudaStreamSynchronize");
     s->var.r2c = v[0];
     s->var.col = v[1];
@@ -1185,19 +1190,21 @@ int cg_get_variants(cg_sim* s, int v[4]) {
     return CG_OK;
 }
 
-int cg_autotune(cg_sim* s, int reps, double ms_out[12], int chosen[4]) {
+int cg_autotune(cg_sim* s, int reps, double ms_out[4 * CG_MAX_VARIANTS], int chosen[4]) {
+    static_assert(CG_MAX_VARIANTS == kMaxVariants, "variant count");
     if (!s) return fail(CG_ERR_ARG, "cg_autotune: NULL handle");
     if (reps < 1 || reps > 1000) return fail(CG_ERR_ARG, "cg_autotune: reps %d outside [1, 1000]", reps);
     CG_CHECK(cudaStreamSynchronize(s->stream), "cudaStreamSynchronize");
     const int phases[4] = {kPhaseRowFwd, kPhaseColConv, kPhaseGrowth, kPhaseDiffusion};
-    double ms[4][3];
+    double ms[4][kMaxVariants];
     int best[4];
     // Every phase reads the current state or the scratch the previous phase
     // wrote; running them in order on the live handle leaves the state
     // untouched (diffusion writes the spare ping-pong buffer only).
     for (int p = 0; p < 4; ++p) {
         best[p] = 0;
-        for (int v = 0; v < 3; ++v) {
+        for (int v = 0; v < kMaxVariants; ++v) ms[p][v] = -1.0;
+        for (int v = 0; v < phase_variant_count(s->logn, p); ++v) {
             Variants var = s->var;
             int* slot[4] = {&var.r2c, &var.col, &var.c2r, &var.diff};
             *slot[p] = v;
@@ -1221,7 +1228,7 @@ int cg_autotune(cg_sim* s, int reps, double ms_out[12], int chosen[4]) {
     if (rc != CG_OK) return rc;
     if (ms_out)
         for (int p = 0; p < 4; ++p)
-            for (int v = 0; v < 3; ++v) ms_out[p * 3 + v] = ms[p][v];
+            for (int v = 0; v < kMaxVariants; ++v) ms_out[p * kMaxVariants + v] = ms[p][v];
     if (chosen)
         for (int p = 0; p < 4; ++p) chosen[p] = best[p];
     return cg_set_variants(s, best);

@@ -502,29 +502,70 @@ namespace cg {
 // from cudaMalloc.  Every GPU that loads the library holds it (37,888 bytes)
 // until the process exits.  Host code cannot pass the array's name to a
 // kernel: on the host that name is only a stand-in, not a device address, so
-// the address is looked up once per device with cudaGetSymbolAddress while
-// that device is current, and cached.
+// the address is looked up with cudaGetSymbolAddress once per device and
+// context, while that device is current, and cached.  The cache key holds
+// the current context's unique ID (cuCtxGetId, never reused within a
+// process), so after cudaDeviceReset, or in another context on the same
+// device, the first call looks the address up again instead of using one
+// from a context that no longer exists.
 // ---------------------------------------------------------------------------
 constexpr int kNoAllocMaxC = kMaxC;
 static __device__ __align__(256) double g_mass_scratch[kNoAllocMaxC * kMassBlocks];
 
 int fail(int code, const char* fmt, ...);
 
+namespace {
+using CtxGetCurrentFn = CUresult (*)(CUcontext*);
+using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long*);
+
+// The unique ID of the calling thread's current context (0 if there is none
+// or the driver lacks cuCtxGetId).
+unsigned long long current_context_id() {
+    static CtxGetCurrentFn get_current = nullptr;
+    static CtxGetIdFn get_id = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault,
+                                             &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_current = reinterpret_cast<CtxGetCurrentFn>(p);
+        p = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_id = reinterpret_cast<CtxGetIdFn>(p);
+    });
+    CUcontext ctx = nullptr;
+    unsigned long long id = 0;
+    if (get_current && get_id && get_current(&ctx) == CUDA_SUCCESS && ctx &&
+        get_id(ctx, &id) == CUDA_SUCCESS)
+        return id;
+    return 0;
+}
+}  // namespace
+
 static cudaError_t mass_scratch_address(double** out) {
     static std::mutex mu;
-    static std::unordered_map<int, double*> by_device;
+    static std::unordered_map<int, std::pair<unsigned long long, double*>> by_device;
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
     std::lock_guard<std::mutex> lock(mu);
     auto it = by_device.find(dev);
-    if (it == by_device.end()) {
+    // a thread on which the runtime has not yet made the device's context
+    // current reads ID 0 and takes the lookup, which makes it current
+    const unsigned long long ctx = current_context_id();
+    if (it == by_device.end() || ctx == 0 || it->second.first != ctx) {
         void* p = nullptr;
         e = cudaGetSymbolAddress(&p, g_mass_scratch);
         if (e != cudaSuccess) return e;
-        it = by_device.emplace(dev, static_cast<double*>(p)).first;
+        // cudaGetSymbolAddress has initialised the context: read its ID now
+        by_device[dev] = {current_context_id(), static_cast<double*>(p)};
+        it = by_device.find(dev);
     }
-    *out = it->second;
+    *out = it->second.second;
     return cudaSuccess;
 }
 

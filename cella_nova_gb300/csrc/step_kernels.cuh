@@ -27,16 +27,25 @@
 
 namespace cg {
 
-// Geometry of one grid size.  V selects a variant of the CTA shapes (the
-// autotuner times them): row kernels V=1 / V=2 halve / quarter the rows per
-// CTA and the threads; the column kernel V=1 halves and V=2 doubles the
-// columns and the threads per CTA (work per thread is unchanged); diffusion
-// V=1 keeps its sums in registers (DiffGeoReg) and V=2 uses 64 tile rows
-// with two columns per thread instead of 32 rows (the diffusion adjoint
-// takes V=1 as 16 tile rows).  Layouts in memory do not depend on V, and
-// every variant computes the same bits.
+// Geometry of one grid size.  V selects a variant (the autotuner times
+// them): row kernels V=1 / V=2 halve / quarter the rows per CTA and the
+// threads; the column kernel V=1 halves and V=2 doubles the columns and the
+// threads per CTA (work per thread is unchanged); diffusion V=1 keeps its
+// sums in registers (DiffGeoReg) and V=2 uses 64 tile rows with two columns
+// per thread instead of 32 rows (the diffusion adjoint takes V=1 as 16 tile
+// rows).  Variants 0-2 compute the same bits.
+//
+// Variants 3 and 4 (grid sides of at least kMinPairLogN) change the FFT
+// plans instead of only the shapes, and agree with the others to rounding:
+// the row passes transform two real rows as one complex sequence of length
+// n (PairGeo, pair_rows.cuh) with radix-16 (V=3) or radix-8 (V=4) plans;
+// the column pass runs the remainder-first plan forward and the greedy plan
+// inverse (the order of variants 0-2 reversed) in the CTA shape of V=1
+// (V=3) or V=0 (V=4).  Layouts in memory do not depend on V.
 template <int LOGN, int V = 0>
 struct Geo {
+    static_assert(V >= 0 && V <= 4, "variant");
+    static_assert(V <= 2 || LOGN >= kMinPairLogN, "plan variants need n >= 512");
     static constexpr int N = 1 << LOGN;
     static constexpr int M = N / 2;
     // Row kernels: RB rows per CTA, RT threads, radix-16 plans (ROW_MR).  The
@@ -65,11 +74,15 @@ struct Geo {
     // Column kernel: TW columns per CTA, CT threads; a padded work buffer
     // and an unpadded staging tile that bulk copies fill.  TW = 4096/N keeps
     // 256 butterflies per radix-16 pass (one per thread) at every size.
+    // CVS: the CTA shape of the column pass (V=3 takes V=1's, V=4 V=0's);
+    // COL_SWAP: the remainder-first plan forward, the greedy plan inverse.
+    static constexpr int CVS = (V == 3) ? 1 : (V == 4 ? 0 : V);
+    static constexpr bool COL_SWAP = (V >= 3);
     static constexpr int TW0 = 4096 / N;
     static constexpr int TW1 = TW0 < 2 ? 2 : (TW0 > M ? M : TW0);
-    static constexpr int TW = (V == 1) ? (TW1 > 1 ? TW1 / 2 : 1)
-                                       : (V == 2 ? (2 * TW1 > M ? M : 2 * TW1) : TW1);
-    static constexpr int CT = (V == 1) ? 128 : (V == 2 ? 512 : 256);
+    static constexpr int TW = (CVS == 1) ? (TW1 > 1 ? TW1 / 2 : 1)
+                                         : (CVS == 2 ? (2 * TW1 > M ? M : 2 * TW1) : TW1);
+    static constexpr int CT = (CVS == 1) ? 128 : (CVS == 2 ? 512 : 256);
     // Resident CTAs per SM the compiler must allow for (the register cap) in
     // the single-world column pass: the small-CTA variant asks for five, which
     // ptxas meets without spills (96 registers at n = 2048; 66.0 against
@@ -77,23 +90,30 @@ struct Geo {
     // threads (80 registers) ran at 121 against 92 us, and five CTAs of the
     // 128-thread variant (96 registers) at 63.5 against 63.7 us, so that pass
     // keeps its default.
-    static constexpr int COL_MINB = (V == 1) ? 5 : 512 / CT;
+    static constexpr int COL_MINB = (CVS == 1) ? 5 : 512 / CT;
     static constexpr int CP = padded_len(N) + 1;
     // the staging tile is a bulk-copy (TMA) destination: 16-byte aligned
     static constexpr int KSOFF = (TW * CP + 1) & ~1;
     static_assert((KSOFF * sizeof(float2)) % 16 == 0, "bulk-copy destination alignment");
     static constexpr size_t COL_SMEM = (size_t(KSOFF) + size_t(TW) * N) * sizeof(float2);
     // Twiddle buffer: W_N^m (m < N), then the pass tables of the column
-    // forward plan, the column inverse plan and the row plan.
+    // forward plan (greedy radix 16, length N), the column inverse plan
+    // (remainder first), the row plan (greedy, length M) and the radix-8
+    // plan of length N (the paired row passes of V=4).
     static constexpr int TW_COL_FWD = N;
     static constexpr int TW_COL_INV = TW_COL_FWD + tw_size(N, false);
     static constexpr int TW_ROW = TW_COL_INV + tw_size(N, true);
-    static constexpr int TW_TOTAL = TW_ROW + tw_size(M, false);
+    static constexpr int TW_PAIR8 = TW_ROW + tw_size(M, false);
+    static constexpr int TW_TOTAL = TW_PAIR8 + tw_size(N, false, 8);
     // Diffusion tile.
     static constexpr int TX = N < 64 ? N : 64;
     static constexpr int TY0 = (V == 1) ? 16 : (V == 2 ? 64 : 32);
     static constexpr int TY = N < TY0 ? N : TY0;
 };
+
+}  // namespace cg
+#include "pair_rows.cuh"
+namespace cg {
 
 // ---------------------------------------------------------------------------
 // Forward row pass: state rows -> packed half spectra, kx-major.
@@ -171,33 +191,25 @@ __device__ __forceinline__ void r2c_finish(float2* sm, const float2* __restrict_
     }
 }
 
-template <int LOGN, int V = 0>
-__global__ void __launch_bounds__(Geo<LOGN, V>::RT, 512 / Geo<LOGN, V>::RT) k_row_r2c(const float* __restrict__ state,
-                                                               float2* __restrict__ rowspec,
-                                                               const float2* __restrict__ tw,
-                                                               int cbase) {
-    extern __shared__ __align__(128) float2 sm_r2c[];
-    row_r2c_body<LOGN, V>(state, rowspec, tw, blockIdx.y + cbase,
-                          blockIdx.x * Geo<LOGN, V>::RB, sm_r2c);
+// The forward row pass of variant V on the RB rows from y0 (R2CShape).
+template <int LOGN, int V>
+__device__ __forceinline__ void row_r2c_variant(const float* __restrict__ state,
+                                                float2* __restrict__ rowspec,
+                                                const float2* __restrict__ tw, int c, int y0,
+                                                float2* sm) {
+    if constexpr (R2CShape<LOGN, V>::PAIR)
+        pair_r2c_body<typename R2CShape<LOGN, V>::P>(state, rowspec, tw, c, y0, sm);
+    else
+        row_r2c_body<LOGN, V>(state, rowspec, tw, c, y0, sm);
 }
 
-// Run the first pass of a transform, then `hook()`, then the rest.
-// FIRSTBAR / LASTBAR as in FftPasses.
-template <int L, bool INV, int T, int S, bool REMFIRST, int MR = 16, bool SFAST = false,
-          bool FIRSTBAR = true, bool LASTBAR = true, class LD, class SMLD, class SMST, class STL,
-          class HOOK>
-__device__ __forceinline__ void fft_with_hook(LD& ld, SMLD& smld, SMST& smst, STL& stl,
-                                              const float2* __restrict__ tab, HOOK hook) {
-    constexpr int R = PassRadix<L, 1, REMFIRST, MR>::R;
-    if constexpr (R == L) {
-        stockham_pass<L, R, 1, INV, T, S, SFAST, FIRSTBAR || LASTBAR>(ld, stl, tab);
-        hook();
-    } else {
-        stockham_pass<L, R, 1, INV, T, S, SFAST, FIRSTBAR>(ld, smst, tab);
-        hook();
-        FftPasses<L, R, INV, T, S, REMFIRST, MR, SFAST, true, LASTBAR>::run(smld, smld, smst, stl,
-                                                                             tab);
-    }
+template <int LOGN, int V = 0>
+__global__ void __launch_bounds__(R2CShape<LOGN, V>::RT, R2CShape<LOGN, V>::MINB)
+    k_row_r2c(const float* __restrict__ state, float2* __restrict__ rowspec,
+              const float2* __restrict__ tw, int cbase) {
+    extern __shared__ __align__(128) float2 sm_r2c[];
+    row_r2c_variant<LOGN, V>(state, rowspec, tw, blockIdx.y + cbase,
+                             blockIdx.x * R2CShape<LOGN, V>::RB, sm_r2c);
 }
 
 // ---------------------------------------------------------------------------
@@ -268,8 +280,13 @@ __device__ __forceinline__ bool col_conv_body(const float2* __restrict__ rowspec
     issue(rowspec + (size_t(c) * M + kx0) * N);
     if (!wait_tile()) return false;
 
-    constexpr int RL = last_radix(N);
-    static_assert(PassRadix<N, 1, true>::R == RL,
+    // forward plan: greedy (variants 0-2) or remainder first (COL_SWAP);
+    // the inverse plan is the other one
+    constexpr bool FREM = G::COL_SWAP;
+    const float2* tw_fwd = tw + (FREM ? G::TW_COL_INV : G::TW_COL_FWD);
+    const float2* tw_inv = tw + (FREM ? G::TW_COL_FWD : G::TW_COL_INV);
+    constexpr int RL = plan_last_radix(N, FREM);
+    static_assert(PassRadix<N, 1, !FREM>::R == RL,
                   "the inverse must start with the radix the forward ends with");
     constexpr int JL = N / RL;
     constexpr int IPTL = (TW * JL + T - 1) / T;
@@ -279,8 +296,8 @@ __device__ __forceinline__ bool col_conv_body(const float2* __restrict__ rowspec
     auto keep = [&](int, int, float2 v, int it, int r) { F[it][r] = v; };
     // forward: the first pass reads the staging tile, the last one keeps its
     // values in registers (no load-store barriers)
-    fft_with_hook<N, false, T, TW, false, 16, false, false, false>(
-        ld_in, wrows, wrows, keep, tw + G::TW_COL_FWD, [&]() { issue(kernel_tile(0)); });
+    fft_with_hook<N, false, T, TW, FREM, 16, false, false, false>(
+        ld_in, wrows, wrows, keep, tw_fwd, [&]() { issue(kernel_tile(0)); });
 
     for (int gi = 0; gi < cnt; ++gi) {
         if (!wait_tile()) return false;
@@ -312,8 +329,8 @@ __device__ __forceinline__ bool col_conv_body(const float2* __restrict__ rowspec
         auto gst = [&](int s, int i, float2 v, int, int) { dst[size_t(s) * N + i] = v; };
         // inverse: the first pass reads W for column 0, so it keeps its
         // barrier; the last one writes global memory
-        fft_with_hook<N, true, T, TW, true, 16, false, true, false>(
-            ld_mul, wrows, wrows, gst, tw + G::TW_COL_INV, [&]() {
+        fft_with_hook<N, true, T, TW, !FREM, 16, false, true, false>(
+            ld_mul, wrows, wrows, gst, tw_inv, [&]() {
             if (gi + 1 < cnt) issue(kernel_tile(gi + 1));
         });
     }
@@ -482,21 +499,36 @@ __device__ __forceinline__ bool row_c2r_growth_body(const CUtensorMap* umap, boo
     return true;
 }
 
+// The inverse row pass + growth of variant V on the RB rows from y0
+// (C2RShape).
+template <int LOGN, int V>
+__device__ __forceinline__ bool row_c2r_growth_variant(
+    const CUtensorMap* umap, bool umap_global, float* __restrict__ A,
+    const float2* __restrict__ tw, const KernelGroups& groups, const GrowthParams& gp, float temp,
+    float* __restrict__ udbg, float udbg_scale, int c, int y0, float2* sm, uint64_t* barp,
+    uint32_t& phase, int* err) {
+    if constexpr (C2RShape<LOGN, V>::PAIR)
+        return pair_c2r_growth_body<typename C2RShape<LOGN, V>::P>(
+            umap, umap_global, A, tw, groups, gp, temp, udbg, udbg_scale, c, y0, sm, barp, phase,
+            err);
+    else
+        return row_c2r_growth_body<LOGN, V>(umap, umap_global, A, tw, groups, gp, temp, udbg,
+                                            udbg_scale, c, y0, sm, barp, phase, err);
+}
+
 template <int LOGN, int V = 0>
-__global__ void __launch_bounds__(Geo<LOGN, V>::RT, 512 / Geo<LOGN, V>::RT) k_row_c2r_growth(const __grid_constant__ CUtensorMap umap,
-                                                         float* __restrict__ A,
-                                                         const float2* __restrict__ tw,
-                                                         const __grid_constant__ KernelGroups groups,
-                                                         const GrowthParams* __restrict__ gp,
-                                                         float temp, float* __restrict__ udbg,
-                                                         float udbg_scale, int* err, int cbase) {
+__global__ void __launch_bounds__(C2RShape<LOGN, V>::RT, C2RShape<LOGN, V>::MINB)
+    k_row_c2r_growth(const __grid_constant__ CUtensorMap umap, float* __restrict__ A,
+                     const float2* __restrict__ tw, const __grid_constant__ KernelGroups groups,
+                     const GrowthParams* __restrict__ gp, float temp, float* __restrict__ udbg,
+                     float udbg_scale, int* err, int cbase) {
     extern __shared__ __align__(128) float2 sm_c2r[];
     __shared__ __align__(8) uint64_t bar;
     init_tile_barrier(&bar);
     uint32_t phase = 0;
-    row_c2r_growth_body<LOGN, V>(&umap, false, A, tw, groups, *gp, temp, udbg, udbg_scale,
-                                 blockIdx.y + cbase, blockIdx.x * Geo<LOGN, V>::RB, sm_c2r, &bar,
-                                 phase, err);
+    row_c2r_growth_variant<LOGN, V>(&umap, false, A, tw, groups, *gp, temp, udbg, udbg_scale,
+                                    blockIdx.y + cbase, blockIdx.x * C2RShape<LOGN, V>::RB,
+                                    sm_c2r, &bar, phase, err);
 }
 
 // ---------------------------------------------------------------------------
@@ -609,12 +641,7 @@ __device__ __forceinline__ void diffusion2_body(const float* __restrict__ A,
             const float l2 = pl[o] + pl[o + 1] + pl[o + 2];
             const float zh = h0 + h1 + h2;
             const float zt = l0 + l1 + l2;
-            const float z = zh + zt;
-            const float zl = zt - (z - zh);
-            const float rz = rcp_approx(z);
-            const float q0 = xv[i] * rz;
-            const float rem = fmaf(-q0, z, xv[i]);
-            pq[i * HW] = fmaf(rem - q0 * zl, rz, q0);
+            pq[i * HW] = div_head_tail(xv[i], zh, zt);
             h0 = h1;
             l0 = l1;
             h1 = h2;
@@ -753,12 +780,7 @@ __device__ __forceinline__ void diffusion_pair_body(const float* __restrict__ A,
             for (int m = 0; m < 2; ++m) {
                 const float zh = h0[m] + h1[m] + h2[m];
                 const float zt = l0[m] + l1[m] + l2[m];
-                const float z = zh + zt;
-                const float zl = zt - (z - zh);
-                const float rz = rcp_approx(z);
-                const float q0 = xv[i][m] * rz;
-                const float rem = fmaf(-q0, z, xv[i][m]);
-                q[m] = fmaf(rem - q0 * zl, rz, q0);
+                q[m] = div_head_tail(xv[i][m], zh, zt);
                 h0[m] = h1[m];
                 l0[m] = l1[m];
                 h1[m] = h2[m];
@@ -884,12 +906,7 @@ __device__ __forceinline__ void diffusion_reg_body(const float* __restrict__ A,
             for (int j = 0; j < 6; ++j) {
                 const float zh = hs[t0][j] + hs[t1][j] + hs[b][j];
                 const float zt = ls[t0][j] + ls[t1][j] + ls[b][j];
-                const float z = zh + zt;
-                const float zl = zt - (z - zh);
-                const float rz = rcp_approx(z);
-                const float q0 = xv[j] * rz;
-                const float rem = fmaf(-q0, z, xv[j]);
-                q[j] = fmaf(rem - q0 * zl, rz, q0);
+                q[j] = div_head_tail(xv[j], zh, zt);
             }
 #pragma unroll
             for (int o = 0; o < 4; ++o) qs[b][o] = q[o] + q[o + 1] + q[o + 2];
@@ -984,16 +1001,18 @@ cudaError_t prepare_variant() {
     using G = Geo<LOGN, V>;
     cudaError_t e;
     if ((e = cudaFuncSetAttribute(k_row_r2c<LOGN, V>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  int(G::R2C_SMEM))) != cudaSuccess)
+                                  int(R2CShape<LOGN, V>::SMEM))) != cudaSuccess)
         return e;
     if ((e = cudaFuncSetAttribute(k_row_c2r_growth<LOGN, V>,
                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  int(G::C2R_SMEM))) != cudaSuccess)
+                                  int(C2RShape<LOGN, V>::SMEM))) != cudaSuccess)
         return e;
-    if ((e = cudaFuncSetAttribute(k_diffusion<LOGN, V>,
-                                  cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  int(DiffTile<LOGN, V>::SMEM))) != cudaSuccess)
-        return e;
+    if constexpr (V <= 2) {
+        if ((e = cudaFuncSetAttribute(k_diffusion<LOGN, V>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      int(DiffTile<LOGN, V>::SMEM))) != cudaSuccess)
+            return e;
+    }
     return cudaFuncSetAttribute(k_col_conv<LOGN, V>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 int(G::COL_SMEM));
 }
@@ -1003,6 +1022,10 @@ cudaError_t prepare_size() {
     cudaError_t e = prepare_variant<LOGN, 0>();
     if (e == cudaSuccess) e = prepare_variant<LOGN, 1>();
     if (e == cudaSuccess) e = prepare_variant<LOGN, 2>();
+    if constexpr (LOGN >= kMinPairLogN) {
+        if (e == cudaSuccess) e = prepare_variant<LOGN, 3>();
+        if (e == cudaSuccess) e = prepare_variant<LOGN, 4>();
+    }
     return e;
 }
 
@@ -1010,9 +1033,9 @@ cudaError_t prepare_size() {
 // c2r/diffusion: the channels written) in variant V.
 template <int LOGN, int V>
 void launch_r2c(const StepArgs& a, int c_lo, int nc, cudaStream_t st) {
-    using G = Geo<LOGN, V>;
-    k_row_r2c<LOGN, V><<<dim3(G::N / G::RB, nc), G::RT, G::R2C_SMEM, st>>>(a.x_in, a.rowspec,
-                                                                          a.tw, c_lo);
+    using R = R2CShape<LOGN, V>;
+    k_row_r2c<LOGN, V><<<dim3((1 << LOGN) / R::RB, nc), R::RT, R::SMEM, st>>>(a.x_in, a.rowspec,
+                                                                             a.tw, c_lo);
 }
 template <int LOGN, int V>
 void launch_col(const StepArgs& a, int c_lo, int nc, cudaStream_t st) {
@@ -1022,12 +1045,13 @@ void launch_col(const StepArgs& a, int c_lo, int nc, cudaStream_t st) {
 }
 template <int LOGN, int V>
 cudaError_t launch_c2r(const StepArgs& a, int c_lo, int nc, cudaStream_t st) {
-    using G = Geo<LOGN, V>;
+    using R = C2RShape<LOGN, V>;
+    constexpr int N = 1 << LOGN;
     CUtensorMap umap;   // passed by value: a graph capture keeps its own copy
-    const cudaError_t e = encode_u_map(&umap, a.U, G::N, a.K, G::RB);
+    const cudaError_t e = encode_u_map(&umap, a.U, N, a.K, R::RB);
     if (e != cudaSuccess) return e;
-    k_row_c2r_growth<LOGN, V><<<dim3(G::N / G::RB, nc), G::RT, G::C2R_SMEM, st>>>(
-        umap, a.A, a.tw, a.groups, a.gp, a.temp, a.udbg, float(G::N) * float(G::N), a.err, c_lo);
+    k_row_c2r_growth<LOGN, V><<<dim3(N / R::RB, nc), R::RT, R::SMEM, st>>>(
+        umap, a.A, a.tw, a.groups, a.gp, a.temp, a.udbg, float(N) * float(N), a.err, c_lo);
     return cudaSuccess;
 }
 template <int LOGN, int V>
@@ -1045,6 +1069,22 @@ void launch_diff(const StepArgs& a, int c_lo, int nc, cudaStream_t st) {
         default: FN<LOGN, 0>(__VA_ARGS__); break; \
     }
 
+// The same over all five variants of the row and column phases (3 and 4
+// exist from kMinPairLogN on; below it they fall back to variant 0, which
+// the host never selects there).
+#define CG_VARIANT_SWITCH5(v, FN, ...)                                      \
+    if constexpr (LOGN >= kMinPairLogN) {                                   \
+        switch (v) {                                                        \
+            case 1: FN<LOGN, 1>(__VA_ARGS__); break;                        \
+            case 2: FN<LOGN, 2>(__VA_ARGS__); break;                        \
+            case 3: FN<LOGN, kMinPairLogN <= LOGN ? 3 : 0>(__VA_ARGS__); break; \
+            case 4: FN<LOGN, kMinPairLogN <= LOGN ? 4 : 0>(__VA_ARGS__); break; \
+            default: FN<LOGN, 0>(__VA_ARGS__); break;                       \
+        }                                                                   \
+    } else {                                                                \
+        CG_VARIANT_SWITCH(v, FN, __VA_ARGS__)                               \
+    }
+
 // The given phases for channels [c_lo, c_hi), each in the variant a.var
 // names.
 template <int LOGN>
@@ -1052,15 +1092,11 @@ cudaError_t launch_step_range(const StepArgs& a, int phases, int c_lo, int c_hi,
                               cudaStream_t st) {
     const int nc = c_hi - c_lo;
     if (nc <= 0) return cudaSuccess;
-    if (phases & kPhaseRowFwd) { CG_VARIANT_SWITCH(a.var.r2c, launch_r2c, a, c_lo, nc, st) }
-    if (phases & kPhaseColConv) { CG_VARIANT_SWITCH(a.var.col, launch_col, a, c_lo, nc, st) }
+    if (phases & kPhaseRowFwd) { CG_VARIANT_SWITCH5(a.var.r2c, launch_r2c, a, c_lo, nc, st) }
+    if (phases & kPhaseColConv) { CG_VARIANT_SWITCH5(a.var.col, launch_col, a, c_lo, nc, st) }
     if (phases & kPhaseGrowth) {
-        cudaError_t e;
-        switch (a.var.c2r) {
-            case 1: e = launch_c2r<LOGN, 1>(a, c_lo, nc, st); break;
-            case 2: e = launch_c2r<LOGN, 2>(a, c_lo, nc, st); break;
-            default: e = launch_c2r<LOGN, 0>(a, c_lo, nc, st); break;
-        }
+        cudaError_t e = cudaSuccess;
+        CG_VARIANT_SWITCH5(a.var.c2r, e = launch_c2r, a, c_lo, nc, st)
         if (e != cudaSuccess) return e;
     }
     if (phases & kPhaseDiffusion) { CG_VARIANT_SWITCH(a.var.diff, launch_diff, a, c_lo, nc, st) }

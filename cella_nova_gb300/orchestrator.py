@@ -218,12 +218,13 @@ class GpuMaceLenia:
         return ms
 
     def autotune(self, reps=10):
-        """Time every CTA-shape variant of every phase, keep the fastest.
-        Returns (chosen[4], ms[4][3])."""
-        ms = np.zeros(12, dtype=np.float64)
+        """Time every variant of every phase (CTA shapes and FFT plans), keep
+        the fastest.  Returns (chosen[4], ms[4][5]); ms is -1 where a phase
+        lacks a variant at this grid side."""
+        ms = np.zeros(4 * _abi.MAX_VARIANTS, dtype=np.float64)
         ch = (ctypes.c_int * 4)()
         check(self._lib.cg_autotune(self._h, int(reps), dptr(ms), ch))
-        return list(ch), ms.reshape(4, 3)
+        return list(ch), ms.reshape(4, _abi.MAX_VARIANTS)
 
     def set_variants(self, v):
         arr = (ctypes.c_int * 4)(*[int(x) for x in v])
@@ -480,14 +481,23 @@ class GpuMaceLeniaBatch:
         check(self._lib.cg_batch_info(self._h, items, grid))
         return list(items), list(grid)
 
+    def set_variants(self, n, v):
+        """Variants [row FFT, column, inverse row + growth, diffusion] of the
+        worlds of grid side n."""
+        arr = (ctypes.c_int * 4)(*[int(x) for x in v])
+        check(self._lib.cg_batch_set_variants(self._h, int(n), arr))
+
     def autotune(self, reps=5):
-        """Per grid side present: time every CTA-shape variant of every phase
-        and keep the fastest.  Returns {side: (chosen[4], ms[4][3])}."""
+        """Per grid side present: time every variant of every phase and keep
+        the fastest.  Returns {side: (chosen[4], ms[4][5])}, ms -1 where a
+        phase lacks a variant at that side."""
+        V = _abi.MAX_VARIANTS
         chosen = (ctypes.c_int * 24)()
-        ms = np.zeros(72, dtype=np.float64)
+        ms = np.zeros(24 * V, dtype=np.float64)
         check(self._lib.cg_batch_autotune(self._h, int(reps), chosen, dptr(ms)))
         out = {}
         for i in range(6):
             if chosen[4 * i] >= 0:
-                out[64 << i] = (list(chosen[4 * i:4 * i + 4]), ms[12 * i:12 * i + 12].reshape(4, 3))
+                out[64 << i] = (list(chosen[4 * i:4 * i + 4]),
+                                ms[4 * V * i:4 * V * (i + 1)].reshape(4, V))
         return out

@@ -99,7 +99,7 @@ class _Candidate:
             self.h = None
 
     def autotune(self, lib, reps: int = 5):
-        ms = np.zeros(12, dtype=np.float64)
+        ms = np.zeros(4 * _abi.MAX_VARIANTS, dtype=np.float64)
         chosen = (ctypes.c_int * 4)()
         check(lib.cg_autotune(self.h, int(reps), ms.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
                               chosen))

@@ -4,8 +4,8 @@
  * Drop-in for the `GpuMaceLenia` orchestrator of anima-zetta/cella-nova
  * (ml-rs/orchestrator/mod.rs:45-541) and its file loaders (ml-rs/config.rs).
  * Every entry point takes plain pointers and sizes; none takes a torch or
- * wgpu type.  The Rust binding a maintainer adds in place of the wgpu path is
- * shown in INTEGRATION.md.
+ * wgpu type, so a Rust host binds it with plain `extern "C"` declarations in
+ * place of the wgpu path.
  *
  * Conventions
  *   - Every function returns CG_OK (0) or a negative cg_status.  The reason
@@ -20,7 +20,7 @@
  *   - Work is enqueued on the handle's CUDA stream (its own, or the one given
  *     to cg_create) and is asynchronous, like wgpu's queue.submit (mod.rs:385);
  *     downloads block, like map_async + poll(Wait) (mod.rs:255-257).
- *   - Grid sides are powers of two from 64 to 2048 (the reference accepts
+ *   - Grid sides are powers of two from 16 to 2048 (the reference accepts
  *     only 1024 and 2048, mod.rs:30-39); C <= 16 (compute_1024.wgsl:307);
  *     K <= 64.
  */
@@ -173,18 +173,30 @@ int cg_download_affinity(cg_sim* sim, float* out);
  * copy (always 0: the state is ping-ponged, no copy exists). */
 int cg_timed_iterate(cg_sim* sim, double ms[4]);
 
-/* Autotuner (no reference counterpart).  Each phase has three variants:
- * CTA shapes (rows per CTA and threads for the row FFTs, columns per CTA and
- * threads for the column pass, tile rows and columns per thread for
- * diffusion).  All variants give bit-identical results.
- * cg_autotune times every variant of every phase
- * `reps` times on the live handle (the state is not advanced), keeps the
- * fastest per phase and re-captures the step graphs.  ms_out[12]
- * (phase-major: [row FFT v0..v2, column v0..v2, inverse row + growth
- * v0..v2, diffusion v0..v2]) and chosen[4] may be NULL. */
-int cg_autotune(cg_sim* sim, int reps, double ms_out[12], int chosen[4]);
+/* Autotuner (no reference counterpart; the reference fixes one register
+ * stage split per grid size, ml-rs/shaders/compute_1024.wgsl:55-78 against
+ * compute_2048.wgsl:57-84).  Each phase has up to CG_MAX_VARIANTS variants:
+ *   0-2  CTA shapes (rows per CTA and threads for the row FFTs, columns per
+ *        CTA and threads for the column pass, tile rows and columns per
+ *        thread for diffusion), radix-16 plans; bit-identical results.
+ *   3, 4 FFT plans, for the row and column phases at grid sides >= 512:
+ *        row FFTs over two real rows as one complex sequence of length n
+ *        with radix-16 (3) or radix-8 (4) passes; the column pass with its
+ *        forward and inverse plan orders swapped (remainder-first radix
+ *        first forward) in the CTA shape of variant 1 (3) or 0 (4).  These
+ *        agree with variants 0-2 to rounding (the same step error bar
+ *        against FP64), not bit for bit.
+ * Diffusion, and every phase below side 512, has variants 0-2 only.
+ * cg_autotune times every variant of every phase `reps` times on the live
+ * handle (the state is not advanced), keeps the fastest per phase and
+ * re-captures the step graphs.  ms_out[4 * CG_MAX_VARIANTS] (phase-major:
+ * [row FFT v0..v4, column v0..v4, inverse row + growth v0..v4, diffusion
+ * v0..v4], -1 where a variant does not exist) and chosen[4] may be NULL. */
+#define CG_MAX_VARIANTS 5
+int cg_autotune(cg_sim* sim, int reps, double ms_out[4 * CG_MAX_VARIANTS], int chosen[4]);
 /* Set / read the variant of each phase ([row FFT, column, inverse row +
- * growth, diffusion], each 0..2); setting re-captures the graphs. */
+ * growth, diffusion]); a variant the phase lacks at this grid side is
+ * CG_ERR_ARG.  Setting re-captures the graphs. */
 int cg_set_variants(cg_sim* sim, const int v[4]);
 int cg_get_variants(cg_sim* sim, int v[4]);
 
@@ -212,7 +224,9 @@ int cg_mass_f64(cg_sim* sim, double* out);
  *     until the process exits.
  *   - The first call on a device looks up that array's device address with
  *     cudaGetSymbolAddress (the device must be current); make that first
- *     call before any stream capture.
+ *     call before any stream capture.  The address is cached per device and
+ *     per CUDA context: after cudaDeviceReset (or from another context) the
+ *     next call looks it up again, so that call is again a first call.
  *   - Work is enqueued on `stream` (NULL = the legacy default stream) and
  *     dev_out is valid once that stream is synchronised.
  *   - All calls share the one array: calls that overlap on the GPU (other
@@ -351,12 +365,15 @@ int cg_batch_stream(cg_batch* b, cg_stream_t* out);
 int cg_batch_info(cg_batch* b, int* items4, int* grid4);
 
 /* Autotuner of the batch: per grid side present and per phase, times the
- * three variants (those of cg_autotune) on
- * the live batch without stepping it, keeps the fastest and re-captures the
- * step graphs.  chosen[6*4] and ms[6*4*3] (either may be NULL) are indexed
- * by grid side 64, 128, ..., 2048, then phase, then variant; sides the batch
- * lacks give -1 and 0. */
+ * variants that phase has at that side (those of cg_autotune) on the live
+ * batch without stepping it, keeps the fastest and re-captures the step
+ * graphs.  chosen[6*4] and ms[6*4*CG_MAX_VARIANTS] (either may be NULL) are
+ * indexed by grid side 64, 128, ..., 2048, then phase, then variant; sides
+ * the batch lacks give -1, variants a phase lacks give ms -1. */
 int cg_batch_autotune(cg_batch* b, int reps, int* chosen, double* ms);
+/* Set the variants of the batch's worlds of grid side n (as cg_set_variants
+ * does for one world); re-captures the step graphs. */
+int cg_batch_set_variants(cg_batch* b, int n, const int v[4]);
 
 /* ---------------------------------------------------------------------------
  * Gradient-search helpers (the optimisation loop of train/, on the device).

@@ -191,4 +191,6 @@ def main(ref_root, only=None):
 if __name__ == "__main__":
     args = [a for a in sys.argv[1:] if not a.startswith("--only=")]
     only = next((a.split("=", 1)[1] for a in sys.argv[1:] if a.startswith("--only=")), None)
-    main(args[0] if args else "/root/reference", only)
+    if len(args) != 1:
+        sys.exit("usage: make_golden.py /path/to/cella-nova [--only=NAME]")
+    main(args[0], only)

@@ -180,8 +180,9 @@ def test_kernel_reupload_and_zero_kernel():
 
 @pytest.mark.parametrize("n", [16, 32, 64, 256, 1024, 2048])
 def test_variants_agree_and_autotune(n):
-    """Every CTA-shape variant computes the same bits, so the autotuner never
-    changes results."""
+    """Every CTA-shape variant (0-2) computes the same bits; the autotuner
+    keeps a variant of each phase that exists at this size and does not
+    step the world."""
     cr = make_creature(n, 3, seed=70 + n, radius=(max(2.0, n / 16), max(4.0, n / 6)),
                        seed_box=n // 2)
     with GpuMaceLenia.from_creature(cr) as sim:
@@ -196,14 +197,54 @@ def test_variants_agree_and_autotune(n):
                 sim.set_variants(var)
                 sim.run_steps(3)
                 np.testing.assert_array_equal(sim.state(), ref, err_msg=str(var))
+    counts = [5 if n >= 512 and p < 3 else 3 for p in range(4)]
     with GpuMaceLenia.from_creature(cr) as sim:
         x0 = sim.state()
         chosen, ms = sim.autotune(reps=3)
         np.testing.assert_array_equal(sim.state(), x0)    # tuning does not step
-        assert all(0 <= c <= 2 for c in chosen) and ms.shape == (4, 3) and (ms > 0).all()
+        assert ms.shape == (4, 5)
+        for p in range(4):
+            assert 0 <= chosen[p] < counts[p]
+            assert (ms[p, :counts[p]] > 0).all() and (ms[p, counts[p]:] == -1).all()
         assert sim.variants() == chosen
         sim.run_steps(3)
-        np.testing.assert_array_equal(sim.state(), ref)
+        if max(chosen[:3]) <= 2:
+            np.testing.assert_array_equal(sim.state(), ref)
+        else:   # an FFT-plan variant: the same step to rounding
+            assert np.abs(sim.state() - ref).max() <= 3 * STEP_TOL
+
+
+@pytest.mark.parametrize("n", [512, 1024, 2048])
+def test_plan_variants_match_oracle(n):
+    """The FFT-plan variants (3: paired rows, radix 16 / swapped column
+    plans; 4: paired rows, radix 8 / swapped plans in another CTA shape),
+    alone and together, step by step against the FP64 oracle."""
+    cr = make_creature(n, 3, seed=90 + n, temp=1.0)
+    a = (cr.kspec.astype(np.complex128), cr.c0, cr.c1, cr.mu.astype(np.float64),
+         cr.sigma.astype(np.float64), cr.weights.astype(np.float64), cr.temp)
+    combos = [[3, 0, 0, 0], [4, 0, 0, 0], [0, 3, 0, 0], [0, 4, 0, 0], [0, 0, 3, 0],
+              [0, 0, 4, 0], [3, 3, 3, 1], [4, 4, 4, 1]]
+    worst = {}
+    for var in combos:
+        with GpuMaceLenia.from_creature(cr) as sim:
+            sim.set_variants(var)
+            assert sim.variants() == var
+            sim.run_steps(2)
+            errs = []
+            for _ in range(2):
+                x = sim.state()
+                sim.iterate()
+                ref, _, _ = O.step_c(x.astype(np.float64), *a, nthreads=os.cpu_count() or 1)
+                errs.append(float(np.abs(sim.state() - ref).max()))
+            worst[str(var)] = max(errs)
+            if n == 512 and var[2] >= 3:
+                # the debug buffer of the paired inverse row pass
+                x = sim.state()
+                conv = sim.download_conv_buffer().reshape(cr.K, n, n)
+                _, u, _ = oracle_step(x, cr, want_u=True)
+                worst[f"{var} u"] = float(np.abs(conv / (n * n) - u).max())
+    print(n, worst)
+    assert max(worst.values()) <= STEP_TOL, worst
 
 
 def test_maximum_channels_and_kernels():
