@@ -49,17 +49,20 @@ def bytes_per_px(C, K):
     return 36 * C + 12 * K
 
 
-def bytes_per_px_as_built(C, K):
+def bytes_per_px_as_built(C, K, real=False):
     """The same for the passes this library runs: the forward column FFT is
     fused into the column convolution, so its 8C never reach HBM (row pass 8C,
-    column pass 4C + 8K, inverse row pass 4K + 4C, diffusion 12C)."""
-    return 28 * C + 12 * K
+    column pass 4C + 8K, inverse row pass 4K + 4C, diffusion 12C).  With real
+    kernel spectra (point-symmetric kernels) the column pass reads 2 instead
+    of 4 bytes per grid point and kernel: 28C + 10K."""
+    return 28 * C + (10 if real else 12) * K
 
 
-def col_conv_bytes_per_px(C, K):
+def col_conv_bytes_per_px(C, K, real=False):
     """k_col_conv: read the row spectra once (4C), read each kernel's half
-    spectrum and write its column-inverted product (8K)."""
-    return 4 * C + 8 * K
+    spectrum (4K complex, 2K real) and write its column-inverted product
+    (4K)."""
+    return 4 * C + (6 if real else 8) * K
 
 
 # Algorithmic bytes per grid point of each step kernel, in the order of
@@ -67,23 +70,24 @@ def col_conv_bytes_per_px(C, K):
 KERNEL_NAMES = ("k_row_r2c", "k_col_conv", "k_row_c2r_growth", "k_diffusion")
 
 
-def kernel_bytes_per_px(C, K):
+def kernel_bytes_per_px(C, K, real=False):
     return (8 * C,                       # read the state, write the row spectra
-            col_conv_bytes_per_px(C, K),
+            col_conv_bytes_per_px(C, K, real),
             4 * K + 4 * C,               # read each U, write A
             12 * C)                      # read A and the state, write the new state
 
 
-def roofline_object(kms, n, C, K, peak, peak_kind, traffic=None):
+def roofline_object(kms, n, C, K, peak, peak_kind, traffic=None, real=False):
     """The `roofline` object of the bench line: every step kernel's
     algorithmic bytes per launch (kernel_bytes_per_px x n^2) over its
     measured duration (kms, ms per step, in KERNEL_NAMES order) against the
     peak, and the kernel with the largest device time reported on top.
-    `traffic` maps "<kernel>_<n>" to an ncu capture's DRAM bytes per launch."""
+    `traffic` maps "<kernel>_<n>" to an ncu capture's DRAM bytes per launch;
+    `real`: the column pass reads real kernel spectra."""
     traffic = traffic or {}
     px = n * n
     per_kernel = []
-    for name, b, t in zip(KERNEL_NAMES, kernel_bytes_per_px(C, K), kms):
+    for name, b, t in zip(KERNEL_NAMES, kernel_bytes_per_px(C, K, real), kms):
         ach = b * px / (t / 1e3) / 1e9
         per_kernel.append({"kernel": name, "algorithmic_bytes": b * px, "kernel_ms": t,
                            "achieved": ach, "frac": ach / peak,
@@ -362,6 +366,7 @@ def run_ours(args):
     t_busy0 = time.perf_counter()
     cr = make_creature(N_GRID, C_CH, seed=2048 + rank, temp=1.0)
     sim = GpuMaceLenia.from_creature(cr)
+    real = sim.kernels_real()
     px = N_GRID * N_GRID
     checks = {}
     mass0 = sim.mass_f64()
@@ -426,7 +431,7 @@ def run_ours(args):
     bpp = bytes_per_px(C_CH, K_KER)
     step_s = ms / 1e3 / args.steps
     value = world * px * args.steps / (ms / 1e3)
-    built = bytes_per_px_as_built(C_CH, K_KER) * px
+    built = bytes_per_px_as_built(C_CH, K_KER, real) * px
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": warm, "ms_per_step": ms / args.steps,
@@ -435,11 +440,13 @@ def run_ours(args):
         "config": workload_config(world),
         # every step kernel against the roofline; the kernel with the
         # largest share of the step's device time on top
-        "roofline": roofline_object(kms, N_GRID, C_CH, K_KER, peak, peak_kind, load_traffic()),
+        "roofline": roofline_object(kms, N_GRID, C_CH, K_KER, peak, peak_kind, load_traffic(),
+                                    real),
         # the step against HBM: first on the bytes the built passes move,
         # then on the survey's pass structure (which adds a forward column
         # pass of 8C B/px that this build fuses away)
-        "step_hbm": {"bytes_per_step_as_built": built,
+        "step_hbm": {"kernel_spectra": "real (point-symmetric kernels)" if real else "complex",
+                     "bytes_per_step_as_built": built,
                      "achieved_gbs_as_built": built / step_s / 1e9,
                      "frac_as_built": built / step_s / 1e9 / peak,
                      "bytes_per_step_algorithmic": bpp * px,
@@ -559,6 +566,7 @@ def measure_plain_1024(dev, sampler, steps=200, check=True):
     cr = make_creature(n, 3, seed=1024, temp=1.0, device=dev)
     tb0 = time.perf_counter()
     sim = GpuMaceLenia.from_creature(cr)
+    real = sim.kernels_real()
     m0 = sim.mass_f64()
     checks = {"step 1": sample_step(sim)}
     sim.autotune(reps=10)
@@ -579,7 +587,8 @@ def measure_plain_1024(dev, sampler, steps=200, check=True):
     out = {"metric": "cell-updates/s (DiffusionLenia fwd step, 1024^2, C=3, K=9)",
            "value": px * steps / (ms / 1e3), "unit": UNIT, "steps": steps,
            "ms_per_step": ms / steps, "variants": variants,
-           "hbm_frac_as_built": bytes_per_px_as_built(3, 9) * px / (ms / 1e3 / steps) / 1e9
+           "kernel_spectra": "real (point-symmetric kernels)" if real else "complex",
+           "hbm_frac_as_built": bytes_per_px_as_built(3, 9, real) * px / (ms / 1e3 / steps) / 1e9
            / peaks()[0],
            "mass_drift": {"steps": 2 * steps + 6, "max_rel": float(np.abs(m1 / m0 - 1).max()),
                           "reduction": "FP64 on the GPU"},

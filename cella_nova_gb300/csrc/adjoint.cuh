@@ -500,6 +500,7 @@ cudaError_t launch_backward(const BwdArgs& a, cudaStream_t st) {
     f.x_out = nullptr;
     f.rowspec = a.rowspec;
     f.kspec = a.kspec;
+    f.kre = a.kre;
     f.U = a.U;
     f.A = a.A;
     f.tw = a.tw;

@@ -118,6 +118,19 @@ __device__ __forceinline__ void cp_async_wait() {
     asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
 }
 
+// Programmatic dependent launch.  A kernel launched with the programmatic
+// stream serialization attribute may start while the kernel before it in the
+// stream is still running; pdl_wait blocks until that kernel has completed
+// and its memory operations are visible (a no-op for a kernel launched
+// without the attribute), and pdl_launch_dependents lets the next such
+// kernel start launching its CTAs, which then wait in their own pdl_wait.
+// The step kernels call both before touching global memory, so the overlap
+// covers only launch latency and the last wave's tail.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_launch_dependents() {
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 // Reciprocal estimate to ~1 ulp (MUFU); div_head_tail refines it.
 __device__ __forceinline__ float rcp_approx(float x) {
     float r;

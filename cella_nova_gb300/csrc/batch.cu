@@ -38,6 +38,7 @@ struct WorldDesc {
     float* state[2];
     float2* rowspec;
     const float2* kspec;
+    const float* kre;   // real parts of kspec (read when every world's kernels are real)
     float2* U;
     float* A;
     const float2* tw;
@@ -90,7 +91,7 @@ __global__ void __launch_bounds__(R2CShape<LOGN, V>::RT, R2CShape<LOGN, V>::MINB
     }
 }
 
-template <int LOGN, int V>
+template <int LOGN, int V, bool KRE = false>
 __global__ void __launch_bounds__(Geo<LOGN, V>::CT, 512 / Geo<LOGN, V>::CT)
     kb_col_conv(const WorldDesc* __restrict__ worlds, const WorkItem* __restrict__ items, int count,
                 int* err) {
@@ -102,8 +103,8 @@ __global__ void __launch_bounds__(Geo<LOGN, V>::CT, 512 / Geo<LOGN, V>::CT)
         __syncthreads();
         const WorkItem it = items[i];
         const WorldDesc& w = worlds[it.world];
-        if (!col_conv_body<LOGN, V>(w.rowspec, w.kspec, w.U, w.tw, w.groups, it.c, it.a, smb_col,
-                                    &bar, phase, err))
+        if (!col_conv_body<LOGN, V, KRE>(w.rowspec, w.kspec, w.kre, w.U, w.tw, w.groups, it.c,
+                                         it.a, smb_col, &bar, phase, err))
             return;   // a bounded wait timed out (uniform across the block)
     }
 }
@@ -145,6 +146,7 @@ __global__ void __launch_bounds__(DiffTile<LOGN, V>::THREADS)
 // and the unit each work item covers.
 struct PhaseVariant {
     const void* fn;
+    const void* fn_real;   // column phase: the real-spectrum form (else nullptr)
     int threads;
     size_t smem;
     int unit_a, unit_b;   // rows per item (row phases), columns per item (column
@@ -156,14 +158,17 @@ void fill_variant(PhaseVariant (&pv)[4][kVariants]) {
     using G = Geo<LOGN, V>;
     using R = R2CShape<LOGN, V>;
     using Q = C2RShape<LOGN, V>;
-    pv[0][V] = {reinterpret_cast<const void*>(kb_row_r2c<LOGN, V>), R::RT, R::SMEM, R::RB, 0};
-    pv[1][V] = {reinterpret_cast<const void*>(kb_col_conv<LOGN, V>), G::CT, G::COL_SMEM, G::TW, 0};
-    pv[2][V] = {reinterpret_cast<const void*>(kb_row_c2r_growth<LOGN, V>), Q::RT, Q::SMEM, Q::RB,
+    pv[0][V] = {reinterpret_cast<const void*>(kb_row_r2c<LOGN, V>), nullptr, R::RT, R::SMEM, R::RB,
                 0};
+    pv[1][V] = {reinterpret_cast<const void*>(kb_col_conv<LOGN, V>),
+                reinterpret_cast<const void*>(kb_col_conv<LOGN, V, true>), G::CT, G::COL_SMEM, G::TW,
+                0};
+    pv[2][V] = {reinterpret_cast<const void*>(kb_row_c2r_growth<LOGN, V>), nullptr, Q::RT, Q::SMEM,
+                Q::RB, 0};
     if constexpr (V <= 2) {
         using D = DiffTile<LOGN, V>;
-        pv[3][V] = {reinterpret_cast<const void*>(kb_diffusion<LOGN, V>), D::THREADS, D::SMEM,
-                    D::TX, D::TY};
+        pv[3][V] = {reinterpret_cast<const void*>(kb_diffusion<LOGN, V>), nullptr, D::THREADS,
+                    D::SMEM, D::TX, D::TY};
     }
 }
 template <int LOGN>
@@ -198,6 +203,8 @@ struct cg_batch {
         float* state[2] = {nullptr, nullptr};
         float2* rowspec = nullptr;
         float2* kspec = nullptr;
+        float* kspec_re = nullptr;
+        std::vector<uint8_t> kreal;   // per kernel: point-symmetric (cg_batch_set_kernel)
         float2* U = nullptr;
         float* A = nullptr;
         KernelGroups groups{};
@@ -223,6 +230,7 @@ struct cg_batch {
     double* mass_out = nullptr;
     cudaStream_t stream = nullptr;
     bool own_stream = false;
+    bool kreal_all = false;   // every world's kernels point-symmetric: real column pass
     int cur = 0;
     int device = 0;
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
@@ -244,6 +252,7 @@ void batch_release(cg_batch* b) {
         cudaFree(w.state[1]);
         cudaFree(w.rowspec);
         cudaFree(w.kspec);
+        cudaFree(w.kspec_re);
         cudaFree(w.U);
         cudaFree(w.A);
     }
@@ -274,7 +283,8 @@ cudaError_t launch_class_phase(cg_batch* b, const cg_batch::SizeClass& sc, int p
     args[2] = &count;
     if (phase == 1 || phase == 2) args[3] = &b->err;   // the bulk-copy phases
     else args[3] = &parity;
-    return cudaLaunchKernel(pv.fn, dim3(sc.grid[phase][v]), dim3(pv.threads), args, pv.smem, st);
+    const void* fn = (b->kreal_all && pv.fn_real) ? pv.fn_real : pv.fn;
+    return cudaLaunchKernel(fn, dim3(sc.grid[phase][v]), dim3(pv.threads), args, pv.smem, st);
 }
 
 // One phase: a persistent launch per size class (largest first).
@@ -415,6 +425,8 @@ int cg_batch_create(int n_worlds, const int* n, const int* C, const int* K, cons
         chk(cudaMalloc(&W.state[1], sizeof(float) * W.C * px), "cudaMalloc(state)");
         chk(cudaMalloc(&W.rowspec, sizeof(float2) * W.C * half), "cudaMalloc(rowspec)");
         chk(cudaMalloc(&W.kspec, sizeof(float2) * W.K * (half + W.n)), "cudaMalloc(kspec)");
+        chk(cudaMalloc(&W.kspec_re, sizeof(float) * W.K * (half + W.n)), "cudaMalloc(kspec_re)");
+        W.kreal.assign(size_t(W.K), 0);
         chk(cudaMalloc(&W.U, sizeof(float2) * W.K * half), "cudaMalloc(U)");
         chk(cudaMalloc(&W.A, sizeof(float) * W.C * px), "cudaMalloc(A)");
         if (rc == CG_OK) {
@@ -448,6 +460,7 @@ int cg_batch_create(int n_worlds, const int* n, const int* C, const int* K, cons
         d.state[1] = W.state[1];
         d.rowspec = W.rowspec;
         d.kspec = W.kspec;
+        d.kre = W.kspec_re;
         d.U = W.U;
         d.A = W.A;
         d.tw = b->tw_by_logn[W.logn];
@@ -503,6 +516,11 @@ int cg_batch_create(int n_worlds, const int* n, const int* C, const int* K, cons
                 chk(cudaFuncSetAttribute(pv.fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          int(pv.smem)),
                     "cudaFuncSetAttribute");
+                if (pv.fn_real)
+                    chk(cudaFuncSetAttribute(pv.fn_real,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             int(pv.smem)),
+                        "cudaFuncSetAttribute");
                 int per_sm = 0;
                 chk(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pv.fn, pv.threads,
                                                                   pv.smem),
@@ -553,9 +571,24 @@ int cg_batch_set_kernel(cg_batch* b, int world, int k, const float* spec) {
     BCHECK(cudaMemcpyAsync(b->staging, spec, sizeof(float2) * px, cudaMemcpyHostToDevice,
                            b->stream),
            "uploading kernel spectrum");
-    BCHECK(size_ops(W.logn)->pack(static_cast<const float2*>(b->staging),
-                                  W.kspec + size_t(k) * (half + W.n), b->stream),
+    float2* packed = W.kspec + size_t(k) * (half + W.n);
+    BCHECK(size_ops(W.logn)->pack(static_cast<const float2*>(b->staging), packed, b->stream),
            "packing kernel spectrum");
+    // point-symmetric kernels: keep the real parts (see cg_set_kernel)
+    const bool real = hermitian_part_is_real(spec, W.n);
+    if (real)
+        BCHECK(launch_real_parts(packed, W.kspec_re + size_t(k) * (half + W.n), half + W.n,
+                                 b->stream),
+               "keeping the real parts");
+    W.kreal[size_t(k)] = real ? 1 : 0;
+    bool all = true;
+    for (const auto& w : b->worlds)
+        for (uint8_t r : w.kreal) all = all && r != 0;
+    if (all != b->kreal_all) {
+        BCHECK(cudaStreamSynchronize(b->stream), "cudaStreamSynchronize");
+        b->kreal_all = all;
+        BCHECK(capture_batch_graphs(b), "re-capturing the batched step graph");
+    }
     return CG_OK;
 }
 

@@ -59,6 +59,10 @@ struct StepArgs {
     float* x_out;
     float2* rowspec;
     const float2* kspec;
+    // optional [K][n/2+1][n] f32: the real parts of kspec, set when every
+    // kernel's Hermitian part is real (point-symmetric kernels); the column
+    // pass then reads 4 instead of 8 bytes per spectrum value
+    const float* kre;
     float2* U;
     float* A;
     const float2* tw;
@@ -98,6 +102,7 @@ struct BwdArgs {
     double* pgrad;
     float2* kgrad;
     int* err;
+    const float* kre;         // as StepArgs::kre (the forward recompute's column pass)
     KernelGroups groups;
     const GrowthParams* gp;   // device-resident
     const AdjointParams* ap;  // device-resident
@@ -177,6 +182,11 @@ const SizeOps* size_ops(int logn);
 
 // Size-independent kernels (kernels_common.cu).
 cudaError_t launch_f64_to_f32(const double* in, float* out, size_t count, cudaStream_t s);
+// out[i] = in[i].x (the real parts of packed kernel spectra)
+cudaError_t launch_real_parts(const float2* in, float* out, size_t count, cudaStream_t s);
+// Whether the Hermitian part of a full n x n spectrum (interleaved re, im)
+// is real to rounding, i.e. the kernel is point-symmetric (host.cu).
+bool hermitian_part_is_real(const float* spec, int n);
 cudaError_t launch_mass_f64(const float* x, int C, size_t px, double* partial, int nblocks,
                             double* out, cudaStream_t s);
 cudaError_t launch_render(const float* x, int C, size_t px, unsigned* out, cudaStream_t s);

@@ -107,6 +107,27 @@ void build_twiddle_tables(int n, float2* out) {
 
 static bool finite(float v) { return std::isfinite(v); }
 
+// The packed kernel spectrum is the Hermitian part (K(f) + conj K(-f)) / 2;
+// it is real when Im K(f) = Im K(-f), i.e. the spatial kernel is
+// point-symmetric (h(x) = h(-x)), as every radially symmetric Lenia ring
+// is.  Real to rounding: max |Im K(f) - Im K(-f)| <= 1e-9 max |Re K(f) +
+// Re K(-f)|; a spectrum computed in double from a symmetric kernel leaves
+// ~1e-17 there, any genuinely complex one orders of magnitude more.
+bool hermitian_part_is_real(const float* spec, int n) {
+    double re = 0.0, im = 0.0;
+    for (int fy = 0; fy < n; ++fy) {
+        const int my = (n - fy) & (n - 1);
+        for (int fx = 0; fx < n; ++fx) {
+            const int mx = (n - fx) & (n - 1);
+            const float* a = spec + 2 * (size_t(fy) * n + fx);
+            const float* b = spec + 2 * (size_t(my) * n + mx);
+            re = std::max(re, std::fabs(double(a[0]) + double(b[0])));
+            im = std::max(im, std::fabs(double(a[1]) - double(b[1])));
+        }
+    }
+    return im <= 1e-9 * re;
+}
+
 int validate_world(int n, int C, int K, const uint32_t* c0, const uint32_t* c1, const float* mu,
                    const float* sigma, const float* weights, float temp, int* logn_out) {
     int logn = 0;
@@ -193,6 +214,11 @@ struct cg_sim {
     int cur = 0;
     float2* rowspec = nullptr;
     float2* kspec = nullptr;
+    // real parts of kspec, and which kernels cg_set_kernel found
+    // point-symmetric: when all are, the column pass reads kspec_re
+    float* kspec_re = nullptr;
+    std::vector<uint8_t> kreal;
+    bool kreal_all = false;
     float2* U = nullptr;       // two [K][n/2][n] buffers, one per ping-pong parity
     float* A = nullptr;
     float2* tw = nullptr;
@@ -235,6 +261,7 @@ struct cg_sim {
         a.x_out = state[from ^ 1];
         a.rowspec = rowspec;
         a.kspec = kspec;
+        a.kre = kreal_all ? kspec_re : nullptr;
         a.U = U + size_t(from) * K * (size_t(n / 2) * n);
         a.A = A;
         a.tw = tw;
@@ -264,6 +291,7 @@ void release(cg_sim* s) {
     cudaFree(s->state[1]);
     cudaFree(s->rowspec);
     cudaFree(s->kspec);
+    cudaFree(s->kspec_re);
     cudaFree(s->U);
     cudaFree(s->A);
     cudaFree(s->tw);
@@ -456,6 +484,7 @@ BwdArgs bwd_args(cg_sim* s, const float* x, const float* ybar, float* xbar, doub
     a.abar = s->abar;
     a.rowspec = s->rowspec;
     a.kspec = s->kspec;
+    a.kre = s->kreal_all ? s->kspec_re : nullptr;
     a.U = s->U;
     a.A = s->A;
     a.tw = s->tw;
@@ -547,6 +576,8 @@ int cg_create(int n, int C, int K, const uint32_t* c0, const uint32_t* c1, const
     if (rc == CG_OK) chk(cudaMalloc(&s->rowspec, sizeof(float2) * C * half), "cudaMalloc(rowspec)");
     if (rc == CG_OK)
         chk(cudaMalloc(&s->kspec, sizeof(float2) * K * (half + n)), "cudaMalloc(kspec)");
+        chk(cudaMalloc(&s->kspec_re, sizeof(float) * K * (half + n)), "cudaMalloc(kspec_re)");
+        s->kreal.assign(size_t(K), 0);
     if (rc == CG_OK) chk(cudaMalloc(&s->U, 2 * sizeof(float2) * K * half), "cudaMalloc(U)");
     if (rc == CG_OK) chk(cudaMalloc(&s->A, sizeof(float) * C * px), "cudaMalloc(A)");
     if (rc == CG_OK)
@@ -591,16 +622,47 @@ int cg_destroy(cg_sim* s) {
     return CG_OK;
 }
 
+}  // extern "C"
+
+namespace {
+// Record whether kernel k's spectrum is real (k < 0: every kernel not real);
+// when the world's column pass changes between the real and the complex
+// form, re-capture the step graphs.
+int set_kernel_realness(cg_sim* s, int k, bool real) {
+    if (k >= 0) s->kreal[size_t(k)] = real ? 1 : 0;
+    else std::fill(s->kreal.begin(), s->kreal.end(), uint8_t(0));
+    bool all = true;
+    for (uint8_t r : s->kreal) all = all && r != 0;
+    if (all == s->kreal_all) return CG_OK;
+    CG_CHECK(cudaStreamSynchronize(s->stream), "cudaStreamSynchronize");
+    s->kreal_all = all;
+    return recapture(s);
+}
+}  // namespace
+
+extern "C" {
+
 int cg_set_kernel(cg_sim* s, int k, const float* spec) {
     if (!s || !spec) return fail(CG_ERR_ARG, "cg_set_kernel: NULL argument");
     if (k < 0 || k >= s->K) return fail(CG_ERR_ARG, "kernel index %d outside [0, %d)", k, s->K);
     const size_t half = size_t(s->n / 2) * s->n;
+    const bool real = hermitian_part_is_real(spec, s->n);
     CG_CHECK(cudaMemcpyAsync(s->staging, spec, sizeof(float2) * s->px(), cudaMemcpyHostToDevice,
                              s->stream),
              "uploading kernel spectrum");
-    CG_CHECK(s->ops->pack(static_cast<const float2*>(s->staging), s->kspec + size_t(k) * (half + s->n),
-                          s->stream),
+    float2* packed = s->kspec + size_t(k) * (half + s->n);
+    CG_CHECK(s->ops->pack(static_cast<const float2*>(s->staging), packed, s->stream),
              "packing kernel spectrum");
+    if (real)
+        CG_CHECK(launch_real_parts(packed, s->kspec_re + size_t(k) * (half + s->n), half + s->n,
+                                   s->stream),
+                 "keeping the real parts");
+    return set_kernel_realness(s, k, real);
+}
+
+int cg_kernels_real(cg_sim* s, int* real) {
+    if (!s || !real) return fail(CG_ERR_ARG, "cg_kernels_real: NULL argument");
+    *real = s->kreal_all ? 1 : 0;
     return CG_OK;
 }
 
@@ -611,7 +673,8 @@ int cg_set_kernel_device(cg_sim* s, int k, const float* dev_spec) {
     CG_CHECK(s->ops->pack(reinterpret_cast<const float2*>(dev_spec),
                           s->kspec + size_t(k) * (half + s->n), s->stream),
              "packing kernel spectrum");
-    return CG_OK;
+    // device spectra are not inspected: the column pass keeps the complex form
+    return set_kernel_realness(s, k, false);
 }
 
 int cg_upload_channel(cg_sim* s, int c, const double* data) {
@@ -1004,7 +1067,8 @@ int cg_build_ring_kernels(cg_sim* s, const cg_ring_spec* specs, const float* dev
     CG_CHECK(s->ops->step(a, kPhaseRowFwd, s->stream), "launching the builder's row transform");
     CG_CHECK(s->ops->kspec_cols(rows, s->kspec, s->tw, s->zsum, s->K, s->stream),
              "launching the builder's column transform");
-    return CG_OK;
+    // spectra built on the device keep the complex column pass
+    return set_kernel_realness(s, -1, false);
 }
 
 int cg_ring_weight_grad(cg_sim* s, const cg_ring_spec* specs, const float* dev_ring_weights,

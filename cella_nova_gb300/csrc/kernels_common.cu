@@ -17,6 +17,18 @@ __global__ void k_f64_to_f32(const double* __restrict__ in, float* __restrict__ 
         out[i] = __double2float_rn(in[i]);
 }
 
+__global__ void k_real_parts(const float2* __restrict__ in, float* __restrict__ out, size_t n) {
+    for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n;
+         i += size_t(gridDim.x) * blockDim.x)
+        out[i] = in[i].x;
+}
+
+cudaError_t launch_real_parts(const float2* in, float* out, size_t count, cudaStream_t s) {
+    const int blocks = int((count + 255) / 256 < 4096 ? (count + 255) / 256 : 4096);
+    k_real_parts<<<blocks, 256, 0, s>>>(in, out, count);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_f64_to_f32(const double* in, float* out, size_t count, cudaStream_t s) {
     const int blocks = int((count + 255) / 256 < 4096 ? (count + 255) / 256 : 4096);
     k_f64_to_f32<<<blocks, 256, 0, s>>>(in, out, count);

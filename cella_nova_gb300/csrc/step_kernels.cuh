@@ -208,6 +208,8 @@ __global__ void __launch_bounds__(R2CShape<LOGN, V>::RT, R2CShape<LOGN, V>::MINB
     k_row_r2c(const float* __restrict__ state, float2* __restrict__ rowspec,
               const float2* __restrict__ tw, int cbase) {
     extern __shared__ __align__(128) float2 sm_r2c[];
+    pdl_wait();
+    pdl_launch_dependents();
     row_r2c_variant<LOGN, V>(state, rowspec, tw, blockIdx.y + cbase,
                              blockIdx.x * R2CShape<LOGN, V>::RB, sm_r2c);
 }
@@ -236,9 +238,13 @@ __global__ void __launch_bounds__(R2CShape<LOGN, V>::RT, R2CShape<LOGN, V>::MINB
 // Returns false if a bounded wait timed out (the error word is set).  `bar`
 // is an initialised mbarrier owned by the caller and `phase` counts its
 // completed phases, so one CTA can run many tiles back to back.
-template <int LOGN, int V = 0>
+// KRE: the kernel spectra are real (point-symmetric kernels) and come from
+// kre, the real parts of kspec: half the bytes per kernel tile, and each
+// product is two multiplications instead of a complex one.
+template <int LOGN, int V = 0, bool KRE = false>
 __device__ __forceinline__ bool col_conv_body(const float2* __restrict__ rowspec,
                                               const float2* __restrict__ kspec,
+                                              const float* __restrict__ kre,
                                               float2* __restrict__ U,
                                               const float2* __restrict__ tw,
                                               const KernelGroups& groups, int c, int kx0,
@@ -250,17 +256,20 @@ __device__ __forceinline__ bool col_conv_body(const float2* __restrict__ rowspec
     if (cnt == 0) return true;
     float2* W = sm;
     float2* KS = sm + G::KSOFF;
+    const float* KR = reinterpret_cast<const float*>(KS);   // the real kernel tile (KRE)
     uint64_t& bar = *barp;
     const int base = groups.in_start[c];
     constexpr uint32_t kTileBytes = uint32_t(TW) * N * sizeof(float2);
-    auto issue = [&](const float2* src) {   // all threads call; thread 0 copies
+    constexpr uint32_t kKernelBytes = KRE ? uint32_t(TW) * N * sizeof(float) : kTileBytes;
+    auto issue_bytes = [&](const void* src, uint32_t bytes) {   // all threads call; thread 0 copies
         fence_proxy_async_smem();
         __syncthreads();
         if (threadIdx.x == 0) {
-            mbar_arrive_expect_tx(&bar, kTileBytes);
-            bulk_g2s(KS, src, kTileBytes, &bar);
+            mbar_arrive_expect_tx(&bar, bytes);
+            bulk_g2s(KS, src, bytes, &bar);
         }
     };
+    auto issue = [&](const float2* src) { issue_bytes(src, kTileBytes); };
     auto wait_tile = [&]() -> bool {
         const bool ok = mbar_wait(&bar, phase & 1, err);
         if (__syncthreads_or(!ok)) {
@@ -272,9 +281,11 @@ __device__ __forceinline__ bool col_conv_body(const float2* __restrict__ rowspec
         ++phase;
         return true;
     };
-    auto kernel_tile = [&](int gi) {
+    auto issue_kernel = [&](int gi) {
         const int k = groups.in_idx[base + gi];
-        return kspec + (size_t(k) * (M + 1) + kx0) * N;
+        const size_t off = (size_t(k) * (M + 1) + kx0) * N;
+        if constexpr (KRE) issue_bytes(kre + off, kKernelBytes);
+        else issue_bytes(kspec + off, kKernelBytes);
     };
 
     issue(rowspec + (size_t(c) * M + kx0) * N);
@@ -297,7 +308,7 @@ __device__ __forceinline__ bool col_conv_body(const float2* __restrict__ rowspec
     // forward: the first pass reads the staging tile, the last one keeps its
     // values in registers (no load-store barriers)
     fft_with_hook<N, false, T, TW, FREM, 16, false, false, false>(
-        ld_in, wrows, wrows, keep, tw_fwd, [&]() { issue(kernel_tile(0)); });
+        ld_in, wrows, wrows, keep, tw_fwd, [&]() { issue_kernel(0); });
 
     for (int gi = 0; gi < cnt; ++gi) {
         if (!wait_tile()) return false;
@@ -316,14 +327,28 @@ __device__ __forceinline__ bool col_conv_body(const float2* __restrict__ rowspec
         }
         const int k = groups.in_idx[base + gi];
         const float2* kb = kspec + (size_t(k) * (M + 1) + M) * N;
+        const float* kbr = KRE ? kre + (size_t(k) * (M + 1) + M) * N : nullptr;
         auto ld_mul = [&](int s, int i, int it, int r) {
             const float2 p = F[it][r];
-            const float2 kv = KS[s * N + i];
-            if (kx0 + s == 0) {
-                const float2 pm = cconj(W[pidx((N - i) & (N - 1))]);
-                return cadd(cmul(p, kv), cmul(pm, __ldg(&kb[i])));
+            if constexpr (KRE) {
+                // the roundings are pinned (no contraction left to the
+                // compiler), so that every CTA shape gives the same bits
+                const float kv = KR[s * N + i];
+                if (kx0 + s == 0) {   // p alpha + conj P(-ky) beta
+                    const float2 pm = cconj(W[pidx((N - i) & (N - 1))]);
+                    const float b = __ldg(&kbr[i]);
+                    return make_float2(__fmaf_rn(p.x, kv, __fmul_rn(pm.x, b)),
+                                       __fmaf_rn(p.y, kv, __fmul_rn(pm.y, b)));
+                }
+                return make_float2(__fmul_rn(p.x, kv), __fmul_rn(p.y, kv));
+            } else {
+                const float2 kv = KS[s * N + i];
+                if (kx0 + s == 0) {
+                    const float2 pm = cconj(W[pidx((N - i) & (N - 1))]);
+                    return cadd(cmul(p, kv), cmul(pm, __ldg(&kb[i])));
+                }
+                return cmul(p, kv);
             }
-            return cmul(p, kv);
         };
         float2* dst = U + (size_t(k) * M + kx0) * N;
         auto gst = [&](int s, int i, float2 v, int, int) { dst[size_t(s) * N + i] = v; };
@@ -331,7 +356,7 @@ __device__ __forceinline__ bool col_conv_body(const float2* __restrict__ rowspec
         // barrier; the last one writes global memory
         fft_with_hook<N, true, T, TW, !FREM, 16, false, true, false>(
             ld_mul, wrows, wrows, gst, tw_inv, [&]() {
-            if (gi + 1 < cnt) issue(kernel_tile(gi + 1));
+            if (gi + 1 < cnt) issue_kernel(gi + 1);
         });
     }
     return true;
@@ -345,19 +370,22 @@ __device__ __forceinline__ void init_tile_barrier(uint64_t* bar) {
     __syncthreads();
 }
 
-template <int LOGN, int V = 0>
+template <int LOGN, int V = 0, bool KRE = false>
 __global__ void __launch_bounds__(Geo<LOGN, V>::CT, Geo<LOGN, V>::COL_MINB)
     k_col_conv(const float2* __restrict__ rowspec, const float2* __restrict__ kspec,
-               float2* __restrict__ U, const float2* __restrict__ tw,
-               const __grid_constant__ KernelGroups groups, int* err, int cbase) {
+               const float* __restrict__ kre, float2* __restrict__ U,
+               const float2* __restrict__ tw, const __grid_constant__ KernelGroups groups,
+               int* err, int cbase) {
     extern __shared__ __align__(128) float2 sm_col[];
     __shared__ __align__(8) uint64_t bar;
+    pdl_wait();
+    pdl_launch_dependents();
     const int c = blockIdx.y + cbase;
     if (groups.in_count[c] == 0) return;
     init_tile_barrier(&bar);
     uint32_t phase = 0;
-    col_conv_body<LOGN, V>(rowspec, kspec, U, tw, groups, c, blockIdx.x * Geo<LOGN, V>::TW,
-                           sm_col, &bar, phase, err);
+    col_conv_body<LOGN, V, KRE>(rowspec, kspec, kre, U, tw, groups, c,
+                                blockIdx.x * Geo<LOGN, V>::TW, sm_col, &bar, phase, err);
 }
 
 // ---------------------------------------------------------------------------
@@ -524,6 +552,8 @@ __global__ void __launch_bounds__(C2RShape<LOGN, V>::RT, C2RShape<LOGN, V>::MINB
                      float udbg_scale, int* err, int cbase) {
     extern __shared__ __align__(128) float2 sm_c2r[];
     __shared__ __align__(8) uint64_t bar;
+    pdl_wait();
+    pdl_launch_dependents();
     init_tile_barrier(&bar);
     uint32_t phase = 0;
     row_c2r_growth_variant<LOGN, V>(&umap, false, A, tw, groups, *gp, temp, udbg, udbg_scale,
@@ -962,6 +992,8 @@ __global__ void __launch_bounds__(DiffTile<LOGN, V>::THREADS)
     k_diffusion(const float* __restrict__ A, const float* __restrict__ x, float* __restrict__ out,
                 int cbase, unsigned char* __restrict__ render, int nch) {
     extern __shared__ __align__(128) float sm_diff[];
+    pdl_wait();
+    pdl_launch_dependents();
     diffusion_tile<LOGN, V>(A, x, out, blockIdx.z + cbase, blockIdx.x * DiffTile<LOGN, V>::TX,
                             blockIdx.y * DiffTile<LOGN, V>::TY, sm_diff, render, nch);
 }
@@ -1013,6 +1045,10 @@ cudaError_t prepare_variant() {
                                       int(DiffTile<LOGN, V>::SMEM))) != cudaSuccess)
             return e;
     }
+    if ((e = cudaFuncSetAttribute(k_col_conv<LOGN, V, true>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  int(G::COL_SMEM))) != cudaSuccess)
+        return e;
     return cudaFuncSetAttribute(k_col_conv<LOGN, V>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 int(G::COL_SMEM));
 }
@@ -1030,18 +1066,41 @@ cudaError_t prepare_size() {
 }
 
 // One phase for channels [c_lo, c_lo + nc) (r2c/col: the channels read;
-// c2r/diffusion: the channels written) in variant V.
+// c2r/diffusion: the channels written) in variant V.  Every step kernel is
+// launched with programmatic stream serialization (pdl_wait): within a
+// stream, and within the step graphs captured from it, a kernel's CTAs are
+// dispatched while the kernel before it drains.
+template <class... KArgs, class... Args>
+cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, int threads, size_t smem,
+                       cudaStream_t st, Args... args) {
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = grid;
+    cfg.blockDim = dim3(threads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
 template <int LOGN, int V>
-void launch_r2c(const StepArgs& a, int c_lo, int nc, cudaStream_t st) {
+cudaError_t launch_r2c(const StepArgs& a, int c_lo, int nc, cudaStream_t st) {
     using R = R2CShape<LOGN, V>;
-    k_row_r2c<LOGN, V><<<dim3((1 << LOGN) / R::RB, nc), R::RT, R::SMEM, st>>>(a.x_in, a.rowspec,
-                                                                             a.tw, c_lo);
+    return launch_pdl(k_row_r2c<LOGN, V>, dim3((1 << LOGN) / R::RB, nc), R::RT, R::SMEM, st,
+                      a.x_in, a.rowspec, a.tw, c_lo);
 }
 template <int LOGN, int V>
-void launch_col(const StepArgs& a, int c_lo, int nc, cudaStream_t st) {
+cudaError_t launch_col(const StepArgs& a, int c_lo, int nc, cudaStream_t st) {
     using G = Geo<LOGN, V>;
-    k_col_conv<LOGN, V><<<dim3(G::M / G::TW, nc), G::CT, G::COL_SMEM, st>>>(
-        a.rowspec, a.kspec, a.U, a.tw, a.groups, a.err, c_lo);
+    const dim3 grid(G::M / G::TW, nc);
+    if (a.kre)
+        return launch_pdl(k_col_conv<LOGN, V, true>, grid, G::CT, G::COL_SMEM, st, a.rowspec,
+                          a.kspec, a.kre, a.U, a.tw, a.groups, a.err, c_lo);
+    return launch_pdl(k_col_conv<LOGN, V>, grid, G::CT, G::COL_SMEM, st, a.rowspec, a.kspec,
+                      static_cast<const float*>(nullptr), a.U, a.tw, a.groups, a.err, c_lo);
 }
 template <int LOGN, int V>
 cudaError_t launch_c2r(const StepArgs& a, int c_lo, int nc, cudaStream_t st) {
@@ -1050,16 +1109,16 @@ cudaError_t launch_c2r(const StepArgs& a, int c_lo, int nc, cudaStream_t st) {
     CUtensorMap umap;   // passed by value: a graph capture keeps its own copy
     const cudaError_t e = encode_u_map(&umap, a.U, N, a.K, R::RB);
     if (e != cudaSuccess) return e;
-    k_row_c2r_growth<LOGN, V><<<dim3(N / R::RB, nc), R::RT, R::SMEM, st>>>(
-        umap, a.A, a.tw, a.groups, a.gp, a.temp, a.udbg, float(N) * float(N), a.err, c_lo);
-    return cudaSuccess;
+    return launch_pdl(k_row_c2r_growth<LOGN, V>, dim3(N / R::RB, nc), R::RT, R::SMEM, st, umap,
+                      a.A, a.tw, a.groups, a.gp, a.temp, a.udbg, float(N) * float(N), a.err,
+                      c_lo);
 }
 template <int LOGN, int V>
-void launch_diff(const StepArgs& a, int c_lo, int nc, cudaStream_t st) {
+cudaError_t launch_diff(const StepArgs& a, int c_lo, int nc, cudaStream_t st) {
     using G = Geo<LOGN, V>;
     using D = DiffTile<LOGN, V>;
-    k_diffusion<LOGN, V><<<dim3(G::N / D::TX, G::N / D::TY, nc), D::THREADS, D::SMEM, st>>>(
-        a.A, a.x_in, a.x_out, c_lo, a.render, a.C);
+    return launch_pdl(k_diffusion<LOGN, V>, dim3(G::N / D::TX, G::N / D::TY, nc), D::THREADS,
+                      D::SMEM, st, a.A, a.x_in, a.x_out, c_lo, a.render, a.C);
 }
 
 #define CG_VARIANT_SWITCH(v, FN, ...)            \
@@ -1092,14 +1151,17 @@ cudaError_t launch_step_range(const StepArgs& a, int phases, int c_lo, int c_hi,
                               cudaStream_t st) {
     const int nc = c_hi - c_lo;
     if (nc <= 0) return cudaSuccess;
-    if (phases & kPhaseRowFwd) { CG_VARIANT_SWITCH5(a.var.r2c, launch_r2c, a, c_lo, nc, st) }
-    if (phases & kPhaseColConv) { CG_VARIANT_SWITCH5(a.var.col, launch_col, a, c_lo, nc, st) }
-    if (phases & kPhaseGrowth) {
-        cudaError_t e = cudaSuccess;
-        CG_VARIANT_SWITCH5(a.var.c2r, e = launch_c2r, a, c_lo, nc, st)
-        if (e != cudaSuccess) return e;
+    cudaError_t e = cudaSuccess;
+    if (phases & kPhaseRowFwd) { CG_VARIANT_SWITCH5(a.var.r2c, e = launch_r2c, a, c_lo, nc, st) }
+    if (e != cudaSuccess) return e;
+    if (phases & kPhaseColConv) { CG_VARIANT_SWITCH5(a.var.col, e = launch_col, a, c_lo, nc, st) }
+    if (e != cudaSuccess) return e;
+    if (phases & kPhaseGrowth) { CG_VARIANT_SWITCH5(a.var.c2r, e = launch_c2r, a, c_lo, nc, st) }
+    if (e != cudaSuccess) return e;
+    if (phases & kPhaseDiffusion) {
+        CG_VARIANT_SWITCH(a.var.diff, e = launch_diff, a, c_lo, nc, st)
     }
-    if (phases & kPhaseDiffusion) { CG_VARIANT_SWITCH(a.var.diff, launch_diff, a, c_lo, nc, st) }
+    if (e != cudaSuccess) return e;
     return cudaGetLastError();
 }
 

@@ -90,6 +90,11 @@ class GpuMaceLenia:
             inter[:] = flat.reshape(-1, 2) if flat.size == 2 * self.total_elements else 0
         check(self._lib.cg_set_kernel(self._h, int(kernel_idx), fptr(inter)))
 
+    def set_kernel_device(self, dev_ptr: int, kernel_idx):
+        """Kernel ``kernel_idx``'s full spectrum from device memory (n*n
+        interleaved f32 pairs), enqueued on the handle's stream."""
+        check(self._lib.cg_set_kernel_device(self._h, int(kernel_idx), ctypes.c_void_p(dev_ptr)))
+
     def upload_channel(self, data, channel):
         """Channel ``channel`` from n*n f64 values (mod.rs:217-226)."""
         a = np.ascontiguousarray(data, dtype=np.float64).reshape(-1)
@@ -229,6 +234,13 @@ class GpuMaceLenia:
     def set_variants(self, v):
         arr = (ctypes.c_int * 4)(*[int(x) for x in v])
         check(self._lib.cg_set_variants(self._h, arr))
+
+    def kernels_real(self) -> bool:
+        """Whether the column pass uses the real form of the kernel spectra
+        (every kernel point-symmetric; see cg_set_kernel)."""
+        v = ctypes.c_int()
+        check(self._lib.cg_kernels_real(self._h, ctypes.byref(v)))
+        return bool(v.value)
 
     def variants(self):
         arr = (ctypes.c_int * 4)()

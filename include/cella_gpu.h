@@ -73,8 +73,17 @@ int cg_create(int n, int C, int K, const uint32_t* c0, const uint32_t* c1,
 int cg_destroy(cg_sim* sim);
 
 /* GpuMaceLenia::set_kernel, mod.rs:207-214: kernel k's full n*n complex
- * spectrum, interleaved (re, im) f32, row-major, origin at [0,0]. */
+ * spectrum, interleaved (re, im) f32, row-major, origin at [0,0].
+ * The step only uses the spectrum's Hermitian part (the state is real and
+ * growth reads the real part of each convolution).  When that part is real
+ * to rounding for every kernel (point-symmetric kernels, h(x) = h(-x), as
+ * every radially symmetric Lenia ring is), the column pass reads only the
+ * real parts, half the bytes; the results agree with the complex form to
+ * rounding.  cg_kernels_real reports which form is in use (1 real, 0
+ * complex); spectra from cg_set_kernel_device or cg_build_ring_kernels
+ * keep the complex form. */
 int cg_set_kernel(cg_sim* sim, int k, const float* spec_interleaved);
+int cg_kernels_real(cg_sim* sim, int* real);
 
 /* set_kernel from DEVICE memory: kernel k's full n*n complex spectrum,
  * interleaved (re, im) f32, already on the GPU (no host round trip). */

@@ -304,3 +304,45 @@ def test_fifty_steps_within_one_grey_level(n):
         drift = float(np.abs(sim.state() - x64).max())
     assert worst <= 1, worst
     assert drift <= 1e-4, drift
+
+
+@pytest.mark.parametrize("n", [64, 512, 2048])
+def test_real_kernel_spectra_path(n):
+    """Point-symmetric kernels (every ring kernel here) take the column
+    pass's real-spectrum form; a kernel shifted off the origin has a complex
+    Hermitian part and keeps the complex form.  Both step like the FP64
+    oracle, and the real form agrees with the complex one to rounding."""
+    import torch
+    cr = make_creature(n, 3, seed=500 + n, radius=(max(2.0, n / 40), max(4.0, n / 16)),
+                       seed_box=n // 2)
+    a = (cr.kspec.astype(np.complex128), cr.c0, cr.c1, cr.mu.astype(np.float64),
+         cr.sigma.astype(np.float64), cr.weights.astype(np.float64), cr.temp)
+    with GpuMaceLenia.from_creature(cr) as sim, GpuMaceLenia.from_creature(cr) as cpx:
+        assert sim.kernels_real()
+        # the same spectra through the device upload keep the complex form
+        specs = [torch.tensor(np.stack([cr.kspec[k].real, cr.kspec[k].imag], -1)
+                              .astype(np.float32), device="cuda") for k in range(cr.K)]
+        torch.cuda.synchronize()        # the uploads, on torch's stream, before cpx reads them
+        for k in range(cr.K):
+            cpx.set_kernel_device(specs[k].data_ptr(), k)
+        cpx.synchronize()
+        del specs
+        assert not cpx.kernels_real()
+        for _ in range(2):
+            x = sim.state()
+            sim.iterate()
+            cpx.iterate()
+            ref, _, _ = O.step_c(x.astype(np.float64), *a, nthreads=os.cpu_count() or 1)
+            assert np.abs(sim.state() - ref).max() <= STEP_TOL
+            # two f32 roundings of the same step (each within the bar above)
+            assert np.abs(sim.state() - cpx.state()).max() <= STEP_TOL
+    # an asymmetric kernel: kernel 0 shifted by (3, 5) pixels
+    shift = np.exp(-2j * np.pi * (3 * np.fft.fftfreq(n)[:, None] + 5 * np.fft.fftfreq(n)[None, :]))
+    cr.kspec[0] = (cr.kspec[0] * shift).astype(np.complex64)
+    a = (cr.kspec.astype(np.complex128),) + a[1:]
+    with GpuMaceLenia.from_creature(cr) as sim:
+        assert not sim.kernels_real()
+        x = sim.state()
+        sim.iterate()
+        ref, _, _ = O.step_c(x.astype(np.float64), *a, nthreads=os.cpu_count() or 1)
+        assert np.abs(sim.state() - ref).max() <= STEP_TOL

@@ -50,3 +50,24 @@ def test_noalloc_mass_rejects_too_many_channels():
     rc = _noalloc(lib, x.data_ptr(), 16, 17, out.data_ptr(), 0)
     assert rc == -1
     assert "at most 16" in lib.cg_last_error().decode()
+
+
+def test_noalloc_mass_leaves_free_device_memory_unchanged():
+    """The property the entry point exists for, as far as the runtime shows
+    it: after the first call on the device (which looks the scratch address
+    up), further calls leave the device's free memory exactly as it was (no
+    allocation outlives a call)."""
+    import torch
+    lib = _abi.load()
+    x = torch.rand((4, 512, 512), dtype=torch.float32, device="cuda")
+    out = torch.zeros(4, dtype=torch.float64, device="cuda")
+    _abi.check(_noalloc(lib, x.data_ptr(), 512, 4, out.data_ptr(), 0))
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    for _ in range(3):
+        _abi.check(_noalloc(lib, x.data_ptr(), 512, 4, out.data_ptr(), 0))
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0, (free0, free1)
+    np.testing.assert_allclose(out.cpu().numpy(), x.double().sum(dim=(1, 2)).cpu().numpy(),
+                               rtol=1e-12)
