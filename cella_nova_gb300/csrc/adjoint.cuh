@@ -117,6 +117,8 @@ __global__ void __launch_bounds__(256) k_diffusion_bwd(const float* __restrict__
                                                         float* __restrict__ xbar,
                                                         float* __restrict__ abar, float temp) {
     extern __shared__ __align__(128) float sm_dbwd[];
+    pdl_wait();
+    pdl_launch_dependents();
     diffusion_bwd_body<LOGN, V>(A, x, ybar, xbar, abar, temp, blockIdx.z, blockIdx.x * Geo<LOGN, V>::TX,
                              blockIdx.y * Geo<LOGN, V>::TY, sm_dbwd);
 }
@@ -224,6 +226,8 @@ __global__ void __launch_bounds__(Geo<LOGN, V>::RT, 512 / Geo<LOGN, V>::RT) k_gr
                                                      double* __restrict__ pgrad, int K) {
     extern __shared__ __align__(128) float2 sm_gbwd[];
     __shared__ double red[16];
+    pdl_wait();
+    pdl_launch_dependents();
     const int k = blockIdx.y;
     growth_bwd_body<LOGN, V>(U, abar, tw, *app, k, app->cout[k], blockIdx.x * Geo<LOGN, V>::RB, pgrad, K,
                           sm_gbwd, red);
@@ -379,6 +383,8 @@ __global__ void __launch_bounds__(Geo<LOGN, V>::CT, 512 / Geo<LOGN, V>::CT) k_co
                                                           int* err) {
     extern __shared__ __align__(128) float2 sm_cadj[];
     __shared__ __align__(8) uint64_t bar;
+    pdl_wait();
+    pdl_launch_dependents();
     init_tile_barrier(&bar);
     uint32_t phase = 0;
     col_conv_adj_body<LOGN, V>(rowspec, kspec, U, kgrad, tw, groups, blockIdx.y,
@@ -396,6 +402,8 @@ __global__ void __launch_bounds__(Geo<LOGN, V>::RT, 512 / Geo<LOGN, V>::RT) k_ro
                                                       int accumulate) {
     using G = Geo<LOGN, V>;
     extern __shared__ __align__(128) float2 sm_c2ra[];
+    pdl_wait();
+    pdl_launch_dependents();
     const int c = blockIdx.y, y0 = blockIdx.x * G::RB;
     gather_rows<LOGN, V>(src + size_t(c) * G::M * G::N + y0, sm_c2ra);
     float* d = dst + (size_t(c) * G::N + y0) * G::N;
@@ -464,30 +472,32 @@ cudaError_t prepare_backward() {
 // the three tiles measured within 1 % of each other in the backward.
 constexpr int kDiffBwdVariant = 1;
 
+// The backward step's kernels, launched like the forward ones
+// (launch_pdl: each may start while the one before it drains).
 template <int LOGN, int V>
-void launch_diff_bwd(const BwdArgs& a, cudaStream_t st) {
+cudaError_t launch_diff_bwd(const BwdArgs& a, cudaStream_t st) {
     using G = Geo<LOGN, V>;
-    k_diffusion_bwd<LOGN, V><<<dim3(G::N / G::TX, G::N / G::TY, a.C), 256,
-                               DiffBwdGeo<LOGN, V>::SMEM, st>>>(a.A, a.x, a.ybar, a.xbar, a.abar,
-                                                                a.temp);
+    return launch_pdl(k_diffusion_bwd<LOGN, V>, dim3(G::N / G::TX, G::N / G::TY, a.C), 256,
+                      DiffBwdGeo<LOGN, V>::SMEM, st, a.A, a.x, a.ybar, a.xbar, a.abar, a.temp);
 }
 template <int LOGN, int V>
-void launch_growth_bwd(const BwdArgs& a, cudaStream_t st) {
+cudaError_t launch_growth_bwd(const BwdArgs& a, cudaStream_t st) {
     using G = Geo<LOGN, V>;
-    k_growth_bwd<LOGN, V><<<dim3(G::N / G::RB, a.K), G::RT, G::R2C_SMEM, st>>>(a.U, a.abar, a.tw,
-                                                                              a.ap, a.pgrad, a.K);
+    return launch_pdl(k_growth_bwd<LOGN, V>, dim3(G::N / G::RB, a.K), G::RT, G::R2C_SMEM, st,
+                      a.U, a.abar, a.tw, a.ap, a.pgrad, a.K);
 }
 template <int LOGN, int V>
-void launch_col_adj(const BwdArgs& a, cudaStream_t st) {
+cudaError_t launch_col_adj(const BwdArgs& a, cudaStream_t st) {
     using G = Geo<LOGN, V>;
-    k_col_conv_adj<LOGN, V><<<dim3(G::M / G::TW, a.C), G::CT, AdjColGeo<LOGN, V>::SMEM, st>>>(
-        a.rowspec, a.kspec, a.U, a.kgrad, a.tw, a.groups, a.err);
+    return launch_pdl(k_col_conv_adj<LOGN, V>, dim3(G::M / G::TW, a.C), G::CT,
+                      AdjColGeo<LOGN, V>::SMEM, st, a.rowspec, a.kspec, a.U, a.kgrad, a.tw,
+                      a.groups, a.err);
 }
 template <int LOGN, int V>
-void launch_c2r_add(const BwdArgs& a, cudaStream_t st) {
+cudaError_t launch_c2r_add(const BwdArgs& a, cudaStream_t st) {
     using G = Geo<LOGN, V>;
-    k_row_c2r_add<LOGN, V><<<dim3(G::N / G::RB, a.C), G::RT, G::R2C_SMEM, st>>>(a.rowspec, a.xbar,
-                                                                               a.tw, 1.f, 1);
+    return launch_pdl(k_row_c2r_add<LOGN, V>, dim3(G::N / G::RB, a.C), G::RT, G::R2C_SMEM, st,
+                      static_cast<const float2*>(a.rowspec), a.xbar, a.tw, 1.f, 1);
 }
 
 template <int LOGN>
@@ -513,15 +523,19 @@ cudaError_t launch_backward(const BwdArgs& a, cudaStream_t st) {
         const cudaError_t e = launch_step<LOGN>(f, kPhaseRowFwd | kPhaseColConv | kPhaseGrowth, st);
         if (e != cudaSuccess) return e;
     }
-    launch_diff_bwd<LOGN, kDiffBwdVariant>(a, st);
+    cudaError_t e = launch_diff_bwd<LOGN, kDiffBwdVariant>(a, st);
+    if (e != cudaSuccess) return e;
     // the adjoint kernels exist in the CTA shapes of variants 0-2: the plan
     // variants take the shape they share (row passes: two rows per CTA as
     // in variant 2; column pass: Geo::CVS)
     const int vrow = a.var.c2r > 2 ? 2 : a.var.c2r;
     const int vcol = a.var.col == 3 ? 1 : (a.var.col == 4 ? 0 : a.var.col);
-    CG_VARIANT_SWITCH(vrow, launch_growth_bwd, a, st)
-    CG_VARIANT_SWITCH(vcol, launch_col_adj, a, st)
-    CG_VARIANT_SWITCH(vrow, launch_c2r_add, a, st)
+    CG_VARIANT_SWITCH(vrow, e = launch_growth_bwd, a, st)
+    if (e != cudaSuccess) return e;
+    CG_VARIANT_SWITCH(vcol, e = launch_col_adj, a, st)
+    if (e != cudaSuccess) return e;
+    CG_VARIANT_SWITCH(vrow, e = launch_c2r_add, a, st)
+    if (e != cudaSuccess) return e;
     return cudaGetLastError();
 }
 

@@ -83,6 +83,8 @@ __global__ void __launch_bounds__(R2CShape<LOGN, V>::RT, R2CShape<LOGN, V>::MINB
     kb_row_r2c(const WorldDesc* __restrict__ worlds, const WorkItem* __restrict__ items, int count,
                int parity) {
     extern __shared__ __align__(128) float2 smb_r2c[];
+    pdl_wait();
+    pdl_launch_dependents();
     for (int i = blockIdx.x; i < count; i += gridDim.x) {
         __syncthreads();
         const WorkItem it = items[i];
@@ -97,6 +99,8 @@ __global__ void __launch_bounds__(Geo<LOGN, V>::CT, 512 / Geo<LOGN, V>::CT)
                 int* err) {
     extern __shared__ __align__(128) float2 smb_col[];
     __shared__ __align__(8) uint64_t bar;
+    pdl_wait();
+    pdl_launch_dependents();
     init_tile_barrier(&bar);
     uint32_t phase = 0;
     for (int i = blockIdx.x; i < count; i += gridDim.x) {
@@ -115,6 +119,8 @@ __global__ void __launch_bounds__(C2RShape<LOGN, V>::RT, C2RShape<LOGN, V>::MINB
                       int count, int* err) {
     extern __shared__ __align__(128) float2 smb_c2r[];
     __shared__ __align__(8) uint64_t bar;
+    pdl_wait();
+    pdl_launch_dependents();
     init_tile_barrier(&bar);
     uint32_t phase = 0;
     for (int i = blockIdx.x; i < count; i += gridDim.x) {
@@ -133,6 +139,8 @@ __global__ void __launch_bounds__(DiffTile<LOGN, V>::THREADS)
     kb_diffusion(const WorldDesc* __restrict__ worlds, const WorkItem* __restrict__ items,
                  int count, int parity) {
     extern __shared__ __align__(128) float smb_diff[];
+    pdl_wait();
+    pdl_launch_dependents();
     for (int i = blockIdx.x; i < count; i += gridDim.x) {
         __syncthreads();
         const WorkItem it = items[i];
@@ -284,7 +292,19 @@ cudaError_t launch_class_phase(cg_batch* b, const cg_batch::SizeClass& sc, int p
     if (phase == 1 || phase == 2) args[3] = &b->err;   // the bulk-copy phases
     else args[3] = &parity;
     const void* fn = (b->kreal_all && pv.fn_real) ? pv.fn_real : pv.fn;
-    return cudaLaunchKernel(fn, dim3(sc.grid[phase][v]), dim3(pv.threads), args, pv.smem, st);
+    // programmatic stream serialization, as the single-world kernels: the
+    // next phase's CTAs are dispatched while this one drains
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(sc.grid[phase][v]);
+    cfg.blockDim = dim3(pv.threads);
+    cfg.dynamicSmemBytes = pv.smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelExC(&cfg, fn, args);
 }
 
 // One phase: a persistent launch per size class (largest first).
