@@ -110,8 +110,10 @@ def peaks():
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled every 100 ms."""
-    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+    """nvidia-smi clocks and throttle reasons sampled every 100 ms.  Each
+    sample carries nvidia-smi's own timestamp: its output reaches the pipe in
+    bursts, so the arrival time would misplace short windows."""
+    Q = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
@@ -134,8 +136,17 @@ class ClockSampler:
         self.thread.start()
 
     def _read(self):
+        import datetime
+        # nvidia-smi prints local wall-clock time; map it to perf_counter
+        offset = time.time() - time.perf_counter()
         for line in self.proc.stdout:
-            self.rows.append((time.perf_counter(), [x.strip() for x in line.split(",")]))
+            f = [x.strip() for x in line.split(",")]
+            t = time.perf_counter()
+            try:
+                t = datetime.datetime.strptime(f[0], "%Y/%m/%d %H:%M:%S.%f").timestamp() - offset
+            except (ValueError, IndexError):
+                pass
+            self.rows.append((t, f[1:]))
 
     def stop(self):
         if self.proc:
