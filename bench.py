@@ -637,6 +637,7 @@ def measure_batched(dev, sampler, steps=500, warmup=3, autotune=True, check=True
     clocks = sampler.summary(tw0, tw1)
     phase_ms = b.profile(min(max(steps, 4), 32))
     items, grid = b.info()
+    modes = {str(side): b.mode(side) for side in sorted({cr.n for cr in crs})}
     # one teacher-forced step of one world of each grid side against FP64
     checks = {}
     if check:
@@ -676,10 +677,17 @@ def measure_batched(dev, sampler, steps=500, warmup=3, autotune=True, check=True
         "phase_ms": {"row_r2c": phase_ms[0], "col_conv": phase_ms[1],
                      "row_c2r_growth": phase_ms[2], "diffusion": phase_ms[3]},
         "work_items": items, "persistent_grid": grid, "autotune": tuned,
+        # per grid side: 0 = one persistent launch per phase over its worlds,
+        # 1 = each world's own step kernels as parallel graph branches
+        "modes": modes,
         "mass_drift": {"max_rel": drift, "steps": max(warmup, 3) + steps + 32 + len(checks),
                        "reduction": "FP64 on the GPU, every world"},
-        # one persistent launch per phase per grid size
-        "gpu_launches": 4 * len({cr.n for cr in crs}) * steps, "clocks": clocks,
+        # mode 0: one persistent launch per phase per grid side; mode 1: per
+        # world one launch per phase and channel
+        "gpu_launches": steps * sum(4 if modes[str(side)] == 0 else
+                                    4 * sum(cr.C for cr in crs if cr.n == side)
+                                    for side in {cr.n for cr in crs}),
+        "clocks": clocks,
         "setup_s": {"generate": gen_s},
     }
     if checks:

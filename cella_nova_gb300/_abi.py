@@ -120,6 +120,8 @@ SIGNATURES = {
     "cg_batch_info": ([_P, ctypes.POINTER(_I), ctypes.POINTER(_I)], _I),
     "cg_batch_autotune": ([_P, _I, ctypes.POINTER(_I), _DP], _I),
     "cg_batch_set_variants": ([_P, _I, ctypes.POINTER(_I)], _I),
+    "cg_batch_set_mode": ([_P, _I, _I], _I),
+    "cg_batch_get_mode": ([_P, _I, ctypes.POINTER(_I)], _I),
     "cg_load_config_json": ([ctypes.c_char_p, ctypes.POINTER(cg_config)], _I),
     "cg_free_config": ([ctypes.POINTER(cg_config)], None),
     "cg_load_config_bin": ([ctypes.c_char_p, ctypes.POINTER(cg_config)], _I),

@@ -219,9 +219,15 @@ struct cg_batch {
         GrowthParams gp{};
     };
     // All worlds of one grid side: per phase and CTA-shape variant a work
-    // list and a persistent grid; var[] names the variant in use.
+    // list and a persistent grid; var[] names the variant in use.  mode 0
+    // steps the side with one persistent launch per phase over all its
+    // worlds; mode 1 runs each world's own step kernels (the single-world
+    // kernels, per channel, as in a single world's step graph) with the
+    // worlds as parallel branches of the step graph.  The tuner picks the
+    // faster; both compute the same bits.
     struct SizeClass {
         int logn = 0;
+        int mode = 0;
         PhaseVariant pv[4][kVariants]{};
         WorkItem* d_items[4][kVariants] = {};
         int count[4][kVariants] = {};
@@ -316,6 +322,127 @@ cudaError_t launch_phase(cg_batch* b, int phase, int parity, cudaStream_t st) {
     return cudaGetLastError();
 }
 
+// Arguments of the single-world step kernels for batched world w (mode 1).
+StepArgs world_step_args(const cg_batch* b, int w, int parity, const Variants& var) {
+    const auto& W = b->worlds[size_t(w)];
+    StepArgs a{};
+    a.C = W.C;
+    a.K = W.K;
+    a.temp = W.temp;
+    a.x_in = W.state[parity];
+    a.x_out = W.state[parity ^ 1];
+    a.rowspec = W.rowspec;
+    a.kspec = W.kspec;
+    bool real = true;
+    for (uint8_t r : W.kreal) real = real && r != 0;
+    a.kre = real ? W.kspec_re : nullptr;
+    a.U = W.U;
+    a.A = W.A;
+    a.tw = b->tw_by_logn[W.logn];
+    a.udbg = nullptr;
+    a.err = b->err;
+    a.render = nullptr;
+    a.groups = W.groups;
+    a.gp = &b->d_worlds[w].gp;   // the descriptor's copy, in device memory
+    a.var = var;
+    return a;
+}
+
+// Streams and events one class step in mode 1 uses: kLanes lane groups of
+// C_max streams (world i of the class runs on lane group i % kLanes, channel
+// c on its stream c), a join event per lane stream and, per world and
+// channel, the event after its column pass.
+constexpr int kLanes = 8;
+struct LanePool {
+    std::vector<cudaStream_t> streams;   // [kLanes][cmax]
+    std::vector<cudaEvent_t> events;
+    int cmax = 0;
+    LanePool() = default;
+    LanePool(const LanePool&) = delete;
+    LanePool& operator=(const LanePool&) = delete;
+    cudaError_t make(int cmax_, int nevents) {
+        cmax = cmax_;
+        streams.assign(size_t(kLanes) * cmax, nullptr);
+        events.assign(size_t(nevents), nullptr);
+        cudaError_t e = cudaSuccess;
+        for (auto& st : streams)
+            if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+        for (auto& ev : events)
+            if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+        return e;
+    }
+    ~LanePool() {
+        for (auto st : streams)
+            if (st) cudaStreamDestroy(st);
+        for (auto ev : events)
+            if (ev) cudaEventDestroy(ev);
+    }
+};
+
+int class_cmax(const cg_batch* b, const cg_batch::SizeClass& sc) {
+    int c = 1;
+    for (const auto& W : b->worlds)
+        if (W.logn == sc.logn) c = std::max(c, W.C);
+    return c;
+}
+int class_events(const cg_batch* b, const cg_batch::SizeClass& sc) {
+    int n = 1 + kLanes * class_cmax(b, sc);
+    for (const auto& W : b->worlds)
+        if (W.logn == sc.logn) n += W.C;
+    return n;
+}
+
+// One step of one class on stream st, after what st holds and before what
+// it gets next (the lanes fork from st and join back into it).
+cudaError_t enqueue_class_step(cg_batch* b, const cg_batch::SizeClass& sc, int parity,
+                               cudaStream_t st, LanePool* pool) {
+    if (sc.mode == 0) {
+        for (int ph = 0; ph < 4; ++ph) {
+            cudaError_t e = launch_class_phase(b, sc, ph, sc.var[ph], parity, st);
+            if (e != cudaSuccess) return e;
+        }
+        return cudaSuccess;
+    }
+    Variants var;
+    var.r2c = sc.var[0];
+    var.col = sc.var[1];
+    var.c2r = sc.var[2];
+    var.diff = sc.var[3];
+    const SizeOps* ops = size_ops(sc.logn);
+    size_t ev = 0;
+    cudaEvent_t fork = pool->events[ev++];
+    cudaError_t e = cudaEventRecord(fork, st);
+    for (auto lane : pool->streams)
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(lane, fork, 0);
+    int i = 0;
+    for (int w = 0; w < int(b->worlds.size()) && e == cudaSuccess; ++w) {
+        const auto& W = b->worlds[size_t(w)];
+        if (W.logn != sc.logn) continue;
+        const StepArgs a = world_step_args(b, w, parity, var);
+        cudaStream_t* ls = &pool->streams[size_t(i % kLanes) * pool->cmax];
+        ++i;
+        const size_t ev0 = ev;
+        for (int c = 0; c < W.C && e == cudaSuccess; ++c) {
+            e = ops->step_channel(a, kPhaseRowFwd | kPhaseColConv, c, ls[c]);
+            if (e == cudaSuccess) e = cudaEventRecord(pool->events[ev0 + c], ls[c]);
+        }
+        ev += size_t(W.C);
+        // a channel's inverse row pass reads U of every input channel
+        for (int c = 0; c < W.C && e == cudaSuccess; ++c) {
+            for (int o = 0; o < W.C && e == cudaSuccess; ++o)
+                if (o != c) e = cudaStreamWaitEvent(ls[c], pool->events[ev0 + o], 0);
+            if (e == cudaSuccess) e = ops->step_channel(a, kPhaseGrowth | kPhaseDiffusion, c, ls[c]);
+        }
+    }
+    for (auto lane : pool->streams) {
+        if (e != cudaSuccess) break;
+        cudaEvent_t j = pool->events[ev++];
+        e = cudaEventRecord(j, lane);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(st, j, 0);
+    }
+    return e;
+}
+
 // One graph per ping-pong parity, (re)captured from the current variants.
 // The size classes share no data, so each runs its four phases on a forked
 // stream of its own: one class's phase tails overlap the other's work.
@@ -328,11 +455,14 @@ cudaError_t capture_batch_graphs(cg_batch* b) {
     const size_t nc = b->classes.size();
     std::vector<cudaStream_t> st(nc, nullptr);
     std::vector<cudaEvent_t> done(nc, nullptr);
+    std::vector<LanePool> pools(nc);
     cudaEvent_t fork = nullptr;
     cudaError_t e = cudaEventCreateWithFlags(&fork, cudaEventDisableTiming);
     for (size_t i = 0; i < nc && e == cudaSuccess; ++i) {
         e = cudaStreamCreateWithFlags(&st[i], cudaStreamNonBlocking);
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&done[i], cudaEventDisableTiming);
+        if (e == cudaSuccess && b->classes[i].mode == 1)
+            e = pools[i].make(class_cmax(b, b->classes[i]), class_events(b, b->classes[i]));
     }
     for (int p = 0; p < 2 && e == cudaSuccess; ++p) {
         cudaGraph_t g = nullptr;
@@ -342,8 +472,7 @@ cudaError_t capture_batch_graphs(cg_batch* b) {
             for (size_t i = 1; i < nc && le == cudaSuccess; ++i)
                 le = cudaStreamWaitEvent(st[i], fork, 0);
             for (size_t i = 0; i < nc && le == cudaSuccess; ++i)
-                for (int ph = 0; ph < 4 && le == cudaSuccess; ++ph)
-                    le = launch_class_phase(b, b->classes[i], ph, b->classes[i].var[ph], p, st[i]);
+                le = enqueue_class_step(b, b->classes[i], p, st[i], &pools[i]);
             for (size_t i = 1; i < nc && le == cudaSuccess; ++i) {
                 le = cudaEventRecord(done[i], st[i]);
                 if (le == cudaSuccess) le = cudaStreamWaitEvent(st[0], done[i], 0);
@@ -361,6 +490,37 @@ cudaError_t capture_batch_graphs(cg_batch* b) {
     }
     if (fork) cudaEventDestroy(fork);
     return e;
+}
+
+// Device ms of one step of class sc alone (its current mode and variants),
+// averaged over reps launches of a captured one-step graph.
+int time_class_step(cg_batch* b, const cg_batch::SizeClass& sc, int reps, double* ms) {
+    cudaStream_t ts = nullptr;
+    cudaGraph_t g = nullptr;
+    cudaGraphExec_t ge = nullptr;
+    LanePool pool;
+    cudaError_t e = cudaStreamCreateWithFlags(&ts, cudaStreamNonBlocking);
+    if (e == cudaSuccess && sc.mode == 1) e = pool.make(class_cmax(b, sc), class_events(b, sc));
+    if (e == cudaSuccess) e = cudaStreamBeginCapture(ts, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+        const cudaError_t le = enqueue_class_step(b, sc, b->cur, ts, &pool);
+        e = cudaStreamEndCapture(ts, &g);
+        if (le != cudaSuccess) e = le;
+    }
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&ge, g, 0);
+    if (e == cudaSuccess) e = cudaGraphLaunch(ge, ts);   // warm-up
+    if (e == cudaSuccess) e = cudaEventRecord(b->ev[0], ts);
+    for (int r = 0; r < reps && e == cudaSuccess; ++r) e = cudaGraphLaunch(ge, ts);
+    if (e == cudaSuccess) e = cudaEventRecord(b->ev[1], ts);
+    if (e == cudaSuccess) e = cudaEventSynchronize(b->ev[1]);
+    float f = 0.f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&f, b->ev[0], b->ev[1]);
+    if (ge) cudaGraphExecDestroy(ge);
+    if (g) cudaGraphDestroy(g);
+    if (ts) cudaStreamDestroy(ts);
+    if (e != cudaSuccess) return cuda_fail(e, "timing a batched step");
+    *ms = double(f) / reps;
+    return CG_OK;
 }
 
 int batch_sync_check(cg_batch* b) {
@@ -729,6 +889,29 @@ int cg_batch_set_variants(cg_batch* b, int n, const int v[4]) {
     return fail(CG_ERR_ARG, "the batch has no world of grid side %d", n);
 }
 
+int cg_batch_set_mode(cg_batch* b, int n, int mode) {
+    if (!b) return fail(CG_ERR_ARG, "cg_batch_set_mode: NULL handle");
+    if (mode < 0 || mode > 1) return fail(CG_ERR_ARG, "batch mode %d outside [0, 1]", mode);
+    for (auto& sc : b->classes) {
+        if ((1 << sc.logn) != n) continue;
+        BCHECK(cudaStreamSynchronize(b->stream), "cudaStreamSynchronize");
+        sc.mode = mode;
+        BCHECK(capture_batch_graphs(b), "re-capturing the batched step graph");
+        return CG_OK;
+    }
+    return fail(CG_ERR_ARG, "the batch has no world of grid side %d", n);
+}
+
+int cg_batch_get_mode(cg_batch* b, int n, int* mode) {
+    if (!b || !mode) return fail(CG_ERR_ARG, "cg_batch_get_mode: NULL argument");
+    for (const auto& sc : b->classes)
+        if ((1 << sc.logn) == n) {
+            *mode = sc.mode;
+            return CG_OK;
+        }
+    return fail(CG_ERR_ARG, "the batch has no world of grid side %d", n);
+}
+
 int cg_batch_autotune(cg_batch* b, int reps, int* chosen, double* ms_out) {
     if (!b) return fail(CG_ERR_ARG, "cg_batch_autotune: NULL handle");
     if (reps < 1 || reps > 1000)
@@ -766,6 +949,22 @@ int cg_batch_autotune(cg_batch* b, int reps, int* chosen, double* ms_out) {
             sc.var[p] = best;
             if (chosen) chosen[slot * 4 + p] = best;
         }
+        // then the two ways of stepping the side (mode 0 and 1), each as a
+        // captured one-step graph of this side alone, in the parity of the
+        // current state (diffusion writes the spare buffer: nothing steps)
+        double best_t = 0.0;
+        int best_mode = 0;
+        for (int m = 0; m < 2; ++m) {
+            sc.mode = m;
+            double t = 0.0;
+            const int rc = time_class_step(b, sc, reps, &t);
+            if (rc != CG_OK) return rc;
+            if (m == 0 || t < best_t) {
+                best_t = t;
+                best_mode = m;
+            }
+        }
+        sc.mode = best_mode;
     }
     int rc = batch_sync_check(b);
     if (rc != CG_OK) return rc;

@@ -499,6 +499,16 @@ class GpuMaceLeniaBatch:
         arr = (ctypes.c_int * 4)(*[int(x) for x in v])
         check(self._lib.cg_batch_set_variants(self._h, int(n), arr))
 
+    def set_mode(self, n, mode):
+        """Step the worlds of grid side n with one persistent launch per phase
+        (0) or as parallel branches of single-world step kernels (1)."""
+        check(self._lib.cg_batch_set_mode(self._h, int(n), int(mode)))
+
+    def mode(self, n) -> int:
+        v = ctypes.c_int()
+        check(self._lib.cg_batch_get_mode(self._h, int(n), ctypes.byref(v)))
+        return v.value
+
     def autotune(self, reps=5):
         """Per grid side present: time every variant of every phase and keep
         the fastest.  Returns {side: (chosen[4], ms[4][5])}, ms -1 where a

@@ -375,14 +375,22 @@ int cg_batch_info(cg_batch* b, int* items4, int* grid4);
 
 /* Autotuner of the batch: per grid side present and per phase, times the
  * variants that phase has at that side (those of cg_autotune) on the live
- * batch without stepping it, keeps the fastest and re-captures the step
- * graphs.  chosen[6*4] and ms[6*4*CG_MAX_VARIANTS] (either may be NULL) are
+ * batch without stepping it, keeps the fastest, then times a step of the
+ * side in each mode (cg_batch_set_mode), keeps the faster and re-captures
+ * the step graphs.  chosen[6*4] and ms[6*4*CG_MAX_VARIANTS] (either may be NULL) are
  * indexed by grid side 64, 128, ..., 2048, then phase, then variant; sides
  * the batch lacks give -1, variants a phase lacks give ms -1. */
 int cg_batch_autotune(cg_batch* b, int reps, int* chosen, double* ms);
 /* Set the variants of the batch's worlds of grid side n (as cg_set_variants
  * does for one world); re-captures the step graphs. */
 int cg_batch_set_variants(cg_batch* b, int n, const int v[4]);
+/* How the worlds of grid side n are stepped: mode 0, one persistent launch
+ * per phase over all of them; mode 1, each world's own step kernels (those
+ * of a single world, per channel) with the worlds as parallel branches of
+ * the step graph.  Both give the same bits; cg_batch_autotune times both and
+ * keeps the faster.  Setting re-captures the step graphs. */
+int cg_batch_set_mode(cg_batch* b, int n, int mode);
+int cg_batch_get_mode(cg_batch* b, int n, int* mode);
 
 /* ---------------------------------------------------------------------------
  * Gradient-search helpers (the optimisation loop of train/, on the device).

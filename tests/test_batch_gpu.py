@@ -104,3 +104,25 @@ def test_batched_plan_variants_match_single_worlds():
                     s.set_variants(var)
                     s.run_steps(3)
                     np.testing.assert_array_equal(b.state(i), s.state(), err_msg=f"{var} {i}")
+
+
+def test_batch_world_branch_mode_equals_single_worlds():
+    """Mode 1 (each world's own step kernels, the worlds as parallel graph
+    branches) steps every world exactly like a single world with the same
+    variants, as mode 0 does."""
+    crs = mixed_creatures()
+    with GpuMaceLeniaBatch(crs) as b:
+        for side in sorted({cr.n for cr in crs}):
+            b.set_mode(side, 1)
+            assert b.mode(side) == 1
+        b.run_steps(3)
+        for i, cr in enumerate(crs):
+            with GpuMaceLenia.from_creature(cr) as s:
+                s.run_steps(3)
+                np.testing.assert_array_equal(b.state(i), s.state(), err_msg=f"world {i}")
+        # back to persistent launches, mid-run
+        b.set_mode(512, 0)
+        b.run_steps(2)
+        with GpuMaceLenia.from_creature(crs[5]) as s:
+            s.run_steps(5)
+            np.testing.assert_array_equal(b.state(5), s.state())
