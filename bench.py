@@ -388,7 +388,8 @@ def run_ours(args):
         tuned = {"variants": sim.variants(), "ms": None, "how": "--variants"}
     elif not args.no_autotune:
         chosen, tms = sim.autotune(reps=10)
-        tuned = {"variants": chosen, "ms": np.round(tms, 4).tolist()}
+        tuned = {"variants": chosen, "ms": np.round(tms, 4).tolist(),
+                 "graph_layout": sim.graph_layout()}
     stream = torch.cuda.ExternalStream(sim.stream())
 
     # warm-up, then K timed graph launches between barriers + syncs
@@ -593,11 +594,12 @@ def measure_plain_1024(dev, sampler, steps=200, check=True):
     m1 = sim.mass_f64()
     tb1 = time.perf_counter()
     variants = sim.variants()
+    layout = sim.graph_layout()
     sim.close()
     px = n * n
     out = {"metric": "cell-updates/s (DiffusionLenia fwd step, 1024^2, C=3, K=9)",
            "value": px * steps / (ms / 1e3), "unit": UNIT, "steps": steps,
-           "ms_per_step": ms / steps, "variants": variants,
+           "ms_per_step": ms / steps, "variants": variants, "graph_layout": layout,
            "kernel_spectra": "real (point-symmetric kernels)" if real else "complex",
            "hbm_frac_as_built": bytes_per_px_as_built(3, 9, real) * px / (ms / 1e3 / steps) / 1e9
            / peaks()[0],

@@ -100,6 +100,8 @@ SIGNATURES = {
     "cg_autotune": ([_P, _I, _DP, ctypes.POINTER(_I)], _I),
     "cg_set_variants": ([_P, ctypes.POINTER(_I)], _I),
     "cg_kernels_real": ([_P, ctypes.POINTER(_I)], _I),
+    "cg_set_graph_layout": ([_P, _I], _I),
+    "cg_get_graph_layout": ([_P, ctypes.POINTER(_I)], _I),
     "cg_get_variants": ([_P, ctypes.POINTER(_I)], _I),
     "cg_mass_f64": ([_P, _DP], _I),
     "cg_mass_f64_noalloc": ([_P, _I, _I, _P, _P], _I),

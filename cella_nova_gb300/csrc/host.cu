@@ -242,6 +242,10 @@ struct cg_sim {
     AdjointParams ap{};
     DeviceParams* dparams = nullptr;   // the copies the kernels read
     Variants var{};
+    // graph layout: 0, each channel's launches on a forked stream of its own
+    // (the channels' phases overlap); 1, one stream, one launch per phase
+    // over all channels (fewer, larger launches); the tuner picks
+    int layout = 0;
     float* abar = nullptr;          // backward scratch, allocated on first use
     float* utmp[2] = {nullptr, nullptr};   // cg_unroll scratch states
     // cg_unroll_backward: each segment step's row spectra, U and A, kept from
@@ -335,8 +339,36 @@ constexpr int kStepsPerGraph = 8;
 // stream order.
 // nsteps steps from parity p0 into one graph; with render, the last step's
 // diffusion kernels also write the render buffer.
-cudaError_t capture_steps(cg_sim* s, int p0, int nsteps, bool render, cudaGraphExec_t* out) {
+// fixed_parity: every captured step reads the same state (p0) and writes the
+// other buffer (U still alternates, so the dependencies are a real run's),
+// so replaying the graph does not advance the world (the tuner's timing)
+cudaError_t capture_steps(cg_sim* s, int p0, int nsteps, bool render, cudaGraphExec_t* out,
+                          bool fixed_parity = false) {
     const int C = s->C;
+    if (s->layout == 1) {   // one stream, one launch per phase over all channels
+        cudaStream_t st0 = nullptr;
+        cudaError_t e = cudaStreamCreateWithFlags(&st0, cudaStreamNonBlocking);
+        cudaGraph_t g = nullptr;
+        if (e == cudaSuccess) e = cudaStreamBeginCapture(st0, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) {
+            cudaError_t le = cudaSuccess;
+            for (int t = 0; t < nsteps && le == cudaSuccess; ++t) {
+                StepArgs a = s->args(p0 ^ (t & 1), nullptr);
+                if (fixed_parity) {
+                    a.x_in = s->state[p0];
+                    a.x_out = s->state[p0 ^ 1];
+                }
+                if (render && t == nsteps - 1) a.render = reinterpret_cast<unsigned char*>(s->render);
+                le = s->ops->step(a, kPhaseAll, st0);
+            }
+            e = cudaStreamEndCapture(st0, &g);
+            if (le != cudaSuccess) e = le;
+        }
+        if (e == cudaSuccess) e = cudaGraphInstantiate(out, g, 0);
+        if (g) cudaGraphDestroy(g);
+        if (st0) cudaStreamDestroy(st0);
+        return e;
+    }
     std::vector<cudaStream_t> st(C, nullptr);
     std::vector<cudaEvent_t> ecol(C, nullptr);
     std::vector<cudaEvent_t> ec2r[2] = {std::vector<cudaEvent_t>(C, nullptr),
@@ -356,6 +388,10 @@ cudaError_t capture_steps(cg_sim* s, int p0, int nsteps, bool render, cudaGraphE
         for (int c = 1; c < C && le == cudaSuccess; ++c) le = cudaStreamWaitEvent(st[c], fork, 0);
         for (int t = 0; t < nsteps && le == cudaSuccess; ++t) {
             StepArgs a = s->args(p0 ^ (t & 1), nullptr);
+            if (fixed_parity) {   // the state stays put; U alternates as in a real run
+                a.x_in = s->state[p0];
+                a.x_out = s->state[p0 ^ 1];
+            }
             if (render && t == nsteps - 1) a.render = reinterpret_cast<unsigned char*>(s->render);
             for (int c = 0; c < C && le == cudaSuccess; ++c) {
                 le = s->ops->step_channel(a, kPhaseRowFwd, c, st[c]);
@@ -1295,7 +1331,46 @@ int cg_autotune(cg_sim* s, int reps, double ms_out[4 * CG_MAX_VARIANTS], int cho
             for (int v = 0; v < kMaxVariants; ++v) ms_out[p * kMaxVariants + v] = ms[p][v];
     if (chosen)
         for (int p = 0; p < 4; ++p) chosen[p] = best[p];
-    return cg_set_variants(s, best);
+    s->var.r2c = best[0];
+    s->var.col = best[1];
+    s->var.c2r = best[2];
+    s->var.diff = best[3];
+    // then the graph layout: each layout's graph of kStepsPerGraph steps,
+    // all reading the current state (nothing steps), replayed reps times
+    double lay_ms[2] = {0.0, 0.0};
+    for (int l = 0; l < 2; ++l) {
+        s->layout = l;
+        cudaGraphExec_t ge = nullptr;
+        cudaError_t e = capture_steps(s, s->cur, kStepsPerGraph, false, &ge, true);
+        if (e == cudaSuccess) e = cudaGraphLaunch(ge, s->stream);   // warm-up
+        if (e == cudaSuccess) e = cudaEventRecord(s->ev[0], s->stream);
+        for (int r = 0; r < reps && e == cudaSuccess; ++r) e = cudaGraphLaunch(ge, s->stream);
+        if (e == cudaSuccess) e = cudaEventRecord(s->ev[1], s->stream);
+        if (e == cudaSuccess) e = cudaEventSynchronize(s->ev[1]);
+        float t = 0.f;
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&t, s->ev[0], s->ev[1]);
+        if (ge) cudaGraphExecDestroy(ge);
+        if (e != cudaSuccess) return cuda_fail(e, "timing a graph layout");
+        lay_ms[l] = double(t) / reps / kStepsPerGraph;
+    }
+    s->layout = lay_ms[1] < lay_ms[0] ? 1 : 0;
+    rc = check_device_error(s);
+    if (rc != CG_OK) return rc;
+    return recapture(s);
+}
+
+int cg_set_graph_layout(cg_sim* s, int layout) {
+    if (!s) return fail(CG_ERR_ARG, "cg_set_graph_layout: NULL handle");
+    if (layout < 0 || layout > 1) return fail(CG_ERR_ARG, "graph layout %d outside [0, 1]", layout);
+    CG_CHECK(cudaStreamSynchronize(s->stream), "cudaStreamSynchronize");
+    s->layout = layout;
+    return recapture(s);
+}
+
+int cg_get_graph_layout(cg_sim* s, int* layout) {
+    if (!s || !layout) return fail(CG_ERR_ARG, "cg_get_graph_layout: NULL argument");
+    *layout = s->layout;
+    return CG_OK;
 }
 
 int cg_synchronize(cg_sim* s) {

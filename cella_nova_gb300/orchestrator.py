@@ -235,6 +235,16 @@ class GpuMaceLenia:
         arr = (ctypes.c_int * 4)(*[int(x) for x in v])
         check(self._lib.cg_set_variants(self._h, arr))
 
+    def set_graph_layout(self, layout: int):
+        """0: each channel on a forked stream; 1: one launch per phase over
+        all channels (cg_set_graph_layout)."""
+        check(self._lib.cg_set_graph_layout(self._h, int(layout)))
+
+    def graph_layout(self) -> int:
+        v = ctypes.c_int()
+        check(self._lib.cg_get_graph_layout(self._h, ctypes.byref(v)))
+        return v.value
+
     def kernels_real(self) -> bool:
         """Whether the column pass uses the real form of the kernel spectra
         (every kernel point-symmetric; see cg_set_kernel)."""

@@ -197,8 +197,9 @@ int cg_timed_iterate(cg_sim* sim, double ms[4]);
  *        against FP64), not bit for bit.
  * Diffusion, and every phase below side 512, has variants 0-2 only.
  * cg_autotune times every variant of every phase `reps` times on the live
- * handle (the state is not advanced), keeps the fastest per phase and
- * re-captures the step graphs.  ms_out[4 * CG_MAX_VARIANTS] (phase-major:
+ * handle (the state is not advanced), keeps the fastest per phase, then
+ * picks the graph layout (cg_set_graph_layout) and re-captures the step
+ * graphs.  ms_out[4 * CG_MAX_VARIANTS] (phase-major:
  * [row FFT v0..v4, column v0..v4, inverse row + growth v0..v4, diffusion
  * v0..v4], -1 where a variant does not exist) and chosen[4] may be NULL. */
 #define CG_MAX_VARIANTS 5
@@ -207,6 +208,14 @@ int cg_autotune(cg_sim* sim, int reps, double ms_out[4 * CG_MAX_VARIANTS], int c
  * growth, diffusion]); a variant the phase lacks at this grid side is
  * CG_ERR_ARG.  Setting re-captures the graphs. */
 int cg_set_variants(cg_sim* sim, const int v[4]);
+/* Layout of the step graphs: 0, each channel's launches on a forked stream of
+ * its own, so the channels' phases overlap; 1, one stream with one launch
+ * per phase over all channels.  Both compute the same bits; after the
+ * variants, cg_autotune times both (graphs of steps that all read the
+ * current state, so the world does not advance) and keeps the faster.
+ * Setting re-captures the graphs. */
+int cg_set_graph_layout(cg_sim* sim, int layout);
+int cg_get_graph_layout(cg_sim* sim, int* layout);
 int cg_get_variants(cg_sim* sim, int v[4]);
 
 /* Per-kernel device time, averaged over nsteps steps (1..1024) launched
