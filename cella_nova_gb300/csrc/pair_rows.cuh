@@ -56,11 +56,14 @@ struct PairGeo {
 
 // Row phases' shapes per variant: 0-2 are Geo's half-length row kernels,
 // 3 and 4 the paired ones.
+// The forward row pass of variants 0-2 is bound by the latency of its first
+// pass's global loads: a register cap of 64 (MINB = 1024 / RT, no spills)
+// lets a third more warps share an SM.
 template <int LOGN, int V>
 struct R2CShape {
     static constexpr bool PAIR = false;
     using G = Geo<LOGN, V>;
-    static constexpr int RT = G::RT, RB = G::RB, MINB = 512 / G::RT;
+    static constexpr int RT = G::RT, RB = G::RB, MINB = 1024 / G::RT;
     static constexpr size_t SMEM = G::R2C_SMEM;
 };
 template <int LOGN>
