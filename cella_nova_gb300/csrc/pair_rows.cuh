@@ -92,7 +92,7 @@ template <int LOGN>
 struct C2RShape<LOGN, 3> {
     static constexpr bool PAIR = true;
     using P = PairGeo<LOGN, 128, 16>;
-    static constexpr int RT = P::RT, RB = P::RB, MINB = 4;
+    static constexpr int RT = P::RT, RB = P::RB, MINB = 5;
     static constexpr size_t SMEM = P::C2R_SMEM;
 };
 template <int LOGN>
