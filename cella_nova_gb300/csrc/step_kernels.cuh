@@ -86,10 +86,11 @@ struct Geo {
     // Resident CTAs per SM the compiler must allow for (the register cap) in
     // the single-world column pass: the small-CTA variant asks for five, which
     // ptxas meets without spills (96 registers at n = 2048; 66.0 against
-    // 67.6 us).  Caps on the inverse row pass did not pay: three CTAs of 256
-    // threads (80 registers) ran at 121 against 92 us, and five CTAs of the
-    // 128-thread variant (96 registers) at 63.5 against 63.7 us, so that pass
-    // keeps its default.
+    // 67.6 us).  Six CTAs of the swapped-plan variant 3 (80 registers, no
+    // spills) ran at 62.1 against 61.1 us, so it keeps five.  On the inverse
+    // row pass, three CTAs of 256 threads (80 registers) ran at 121 against
+    // 92 us and five of the 128-thread variant at 63.5 against 63.7 us; only
+    // the paired variant 3 takes a cap there (pair_rows.cuh).
     static constexpr int COL_MINB = (CVS == 1) ? 5 : 512 / CT;
     static constexpr int CP = padded_len(N) + 1;
     // the staging tile is a bulk-copy (TMA) destination: 16-byte aligned
