@@ -27,7 +27,7 @@ namespace cg {
 constexpr int kBatchMinLogN = 6;   // 64^2 .. 2048^2 in one batch
 constexpr int kBatchMaxLogN = 11;
 
-constexpr int kVariants = 5;   // per phase; diffusion and sides below 512 have 3
+constexpr int kVariants = 5;   // per phase at most (phase_variant_count)
 
 struct WorldDesc {
     // tensor maps of U for the inverse row pass's tile copies, one per
@@ -81,15 +81,32 @@ struct WorkItem {
 template <int LOGN, int V>
 __global__ void __launch_bounds__(R2CShape<LOGN, V>::RT, R2CShape<LOGN, V>::MINB)
     kb_row_r2c(const WorldDesc* __restrict__ worlds, const WorkItem* __restrict__ items, int count,
-               int parity) {
+               int parity, int* err) {
     extern __shared__ __align__(128) float2 smb_r2c[];
+    using Sh = R2CShape<LOGN, V>;
     pdl_wait();
     pdl_launch_dependents();
-    for (int i = blockIdx.x; i < count; i += gridDim.x) {
-        __syncthreads();
-        const WorkItem it = items[i];
-        const WorldDesc& w = worlds[it.world];
-        row_r2c_variant<LOGN, V>(w.state[parity], w.rowspec, w.tw, it.c, it.a, smb_r2c);
+    if constexpr (Sh::STREAM) {
+        constexpr int N = 1 << LOGN;
+        __shared__ __align__(8) uint64_t bar;
+        init_tile_barrier(&bar);
+        uint32_t phase = 0;
+        auto item = [&](int i, const float*& src, float2*& dst) {
+            const WorkItem it = items[i];
+            const WorldDesc& w = worlds[it.world];
+            src = w.state[parity] + (size_t(it.c) * N + it.a) * N;
+            dst = w.rowspec + size_t(it.c) * (N / 2) * N + it.a;
+        };
+        // every world of this size class shares the size's twiddle table
+        const float2* tw = int(blockIdx.x) < count ? worlds[items[blockIdx.x].world].tw : nullptr;
+        row_r2c_stream<LOGN>(item, count, tw, smb_r2c, &bar, phase, err);
+    } else {
+        for (int i = blockIdx.x; i < count; i += gridDim.x) {
+            __syncthreads();
+            const WorkItem it = items[i];
+            const WorldDesc& w = worlds[it.world];
+            row_r2c_variant<LOGN, V>(w.state[parity], w.rowspec, w.tw, it.c, it.a, smb_r2c);
+        }
     }
 }
 
@@ -173,11 +190,12 @@ void fill_variant(PhaseVariant (&pv)[4][kVariants]) {
                 0};
     pv[2][V] = {reinterpret_cast<const void*>(kb_row_c2r_growth<LOGN, V>), nullptr, Q::RT, Q::SMEM,
                 Q::RB, 0};
-    if constexpr (V <= 2) {
-        using D = DiffTile<LOGN, V>;
-        pv[3][V] = {reinterpret_cast<const void*>(kb_diffusion<LOGN, V>), nullptr, D::THREADS,
-                    D::SMEM, D::TX, D::TY};
-    }
+}
+template <int LOGN, int V>
+void fill_diffusion(PhaseVariant (&pv)[4][kVariants]) {
+    using D = DiffTile<LOGN, V>;
+    pv[3][V] = {reinterpret_cast<const void*>(kb_diffusion<LOGN, V>), nullptr, D::THREADS, D::SMEM,
+                D::TX, D::TY};
 }
 template <int LOGN>
 void fill_size(PhaseVariant (&pv)[4][kVariants]) {
@@ -188,6 +206,10 @@ void fill_size(PhaseVariant (&pv)[4][kVariants]) {
         fill_variant<LOGN, 3>(pv);
         fill_variant<LOGN, 4>(pv);
     }
+    fill_diffusion<LOGN, 0>(pv);
+    fill_diffusion<LOGN, 1>(pv);
+    fill_diffusion<LOGN, 2>(pv);
+    fill_diffusion<LOGN, 3>(pv);
 }
 static void phase_variants_for(int logn, PhaseVariant (&pv)[4][kVariants]) {
     switch (logn) {
@@ -291,12 +313,16 @@ cudaError_t launch_class_phase(cg_batch* b, const cg_batch::SizeClass& sc, int p
     const WorldDesc* worlds = b->d_worlds;
     const WorkItem* items = sc.d_items[phase][v];
     int count = sc.count[phase][v];
-    void* args[4];
+    void* args[5];
     args[0] = &worlds;
     args[1] = &items;
     args[2] = &count;
-    if (phase == 1 || phase == 2) args[3] = &b->err;   // the bulk-copy phases
-    else args[3] = &parity;
+    if (phase == 1 || phase == 2) {   // the bulk-copy phases
+        args[3] = &b->err;
+    } else {
+        args[3] = &parity;
+        args[4] = &b->err;   // the forward row pass (its streaming variant copies)
+    }
     const void* fn = (b->kreal_all && pv.fn_real) ? pv.fn_real : pv.fn;
     // programmatic stream serialization, as the single-world kernels: the
     // next phase's CTAs are dispatched while this one drains

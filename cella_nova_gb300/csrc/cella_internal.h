@@ -38,9 +38,11 @@ struct Variants {
 };
 constexpr int kMinPairLogN = 9;
 constexpr int kMaxVariants = 5;
-// Variants phase p (0 r2c, 1 col, 2 c2r, 3 diffusion) has at side 2^logn.
+// Variants phase p (0 r2c, 1 col, 2 c2r, 3 diffusion) has at side 2^logn:
+// diffusion four at every side, the FFT phases five from kMinPairLogN on
+// (the plan variants) and three below.
 __host__ __device__ constexpr int phase_variant_count(int logn, int phase) {
-    return (phase == 3 || logn < kMinPairLogN) ? 3 : kMaxVariants;
+    return phase == 3 ? 4 : (logn < kMinPairLogN ? 3 : kMaxVariants);
 }
 
 // Everything one step's launches need.  Planar layouts, all device pointers:

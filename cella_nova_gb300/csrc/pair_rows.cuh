@@ -56,26 +56,40 @@ struct PairGeo {
 
 // Row phases' shapes per variant: 0-2 are Geo's half-length row kernels,
 // 3 and 4 the paired ones.
-// The forward row pass of variants 0-2 is bound by the latency of its first
-// pass's global loads: a register cap of 64 (MINB = 1024 / RT, no spills)
-// lets a third more warps share an SM.
+// The forward row pass of variants 0 and 1 is bound by the latency of its
+// first pass's global loads: a register cap of 64 (MINB = 1024 / RT, no
+// spills) lets a third more warps share an SM.  Variant 2 (STREAM) runs
+// variant 1's tile in a persistent grid whose CTAs bring each block's rows
+// into a staging tile with one bulk copy, the next block's while the
+// current one is transformed (row_r2c_stream); STG is the staging tile's
+// offset in float2 (128-byte aligned, after the work rows).
 template <int LOGN, int V>
 struct R2CShape {
-    static constexpr bool PAIR = false;
+    static constexpr bool PAIR = false, STREAM = false;
     using G = Geo<LOGN, V>;
     static constexpr int RT = G::RT, RB = G::RB, MINB = 1024 / G::RT;
     static constexpr size_t SMEM = G::R2C_SMEM;
 };
 template <int LOGN>
+struct R2CShape<LOGN, 2> {
+    static constexpr bool PAIR = false, STREAM = true;
+    using G = Geo<LOGN, 1>;
+    static constexpr int RT = G::RT, RB = G::RB, MINB = 3;
+    static constexpr int STG = int((G::R2C_SMEM / sizeof(float2) + 15) & ~size_t(15));
+    static constexpr uint32_t kBlockBytes = uint32_t(RB) * G::N * sizeof(float);
+    static constexpr size_t SMEM = size_t(STG) * sizeof(float2) + kBlockBytes;
+    static_assert(kBlockBytes % 16 == 0, "bulk-copy size");
+};
+template <int LOGN>
 struct R2CShape<LOGN, 3> {
-    static constexpr bool PAIR = true;
+    static constexpr bool PAIR = true, STREAM = false;
     using P = PairGeo<LOGN, 256, 16>;
     static constexpr int RT = P::RT, RB = P::RB, MINB = 2;
     static constexpr size_t SMEM = P::R2C_SMEM;
 };
 template <int LOGN>
 struct R2CShape<LOGN, 4> {
-    static constexpr bool PAIR = true;
+    static constexpr bool PAIR = true, STREAM = false;
     using P = PairGeo<LOGN, 512, 8>;
     static constexpr int RT = P::RT, RB = P::RB, MINB = 2;
     static constexpr size_t SMEM = P::R2C_SMEM;

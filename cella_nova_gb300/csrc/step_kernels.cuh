@@ -29,7 +29,8 @@ namespace cg {
 
 // Geometry of one grid size.  V selects a variant (the autotuner times
 // them): row kernels V=1 / V=2 halve / quarter the rows per CTA and the
-// threads; the column kernel V=1 halves and V=2 doubles the columns and the
+// threads (the forward row pass's variant 2 streams variant 1's tile
+// instead, R2CShape); the column kernel V=1 halves and V=2 doubles the columns and the
 // threads per CTA (work per thread is unchanged); diffusion V=1 keeps its
 // sums in registers (DiffGeoReg) and V=2 uses 64 tile rows with two columns
 // per thread instead of 32 rows (the diffusion adjoint takes V=1 as 16 tile
@@ -204,15 +205,96 @@ __device__ __forceinline__ void row_r2c_variant(const float* __restrict__ state,
         row_r2c_body<LOGN, V>(state, rowspec, tw, c, y0, sm);
 }
 
+__device__ __forceinline__ void init_tile_barrier(uint64_t* bar) {
+    if (threadIdx.x == 0) {
+        mbar_init(bar, 1);
+        fence_barrier_init();
+    }
+    __syncthreads();
+}
+
+// The streaming form of the forward row pass (R2CShape<LOGN, 2>): this CTA
+// takes blocks blockIdx.x, blockIdx.x + gridDim.x, ... of `count`;
+// item(i, src, dst) names block i's RB state rows (contiguous) and its
+// destination in the kx-major row spectra.  The rows arrive by one bulk copy
+// into the staging tile; the next block's copy is issued once the first FFT
+// pass has read the tile, so it lands while the remaining passes and the
+// stores run.  Same arithmetic as variant 1, so the same bits.  Returns
+// false if a bounded wait timed out (the error word is set).  `bar` is an
+// initialised mbarrier; `phase` counts its completed phases.
+template <int LOGN, class ITEM>
+__device__ __forceinline__ bool row_r2c_stream(ITEM item, int count,
+                                               const float2* __restrict__ tw, float2* sm,
+                                               uint64_t* barp, uint32_t& phase, int* err) {
+    using Sh = R2CShape<LOGN, 2>;
+    using G = typename Sh::G;
+    const float2* stg = sm + Sh::STG;
+    uint64_t& bar = *barp;
+    auto issue = [&](int i) {   // all threads call; thread 0 copies
+        const float* src;
+        float2* dst;
+        item(i, src, dst);
+        fence_proxy_async_smem();
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            mbar_arrive_expect_tx(&bar, Sh::kBlockBytes);
+            bulk_g2s(const_cast<float2*>(stg), src, Sh::kBlockBytes, &bar);
+        }
+    };
+    if (int(blockIdx.x) < count) issue(blockIdx.x);
+    for (int i = blockIdx.x; i < count; i += gridDim.x) {
+        const bool ok = mbar_wait(&bar, phase & 1u, err);
+        if (__syncthreads_or(!ok)) {
+            // one more bounded chance for the copy in flight to land before
+            // this CTA's shared memory is released
+            mbar_wait(&bar, phase & 1u, nullptr);
+            return false;
+        }
+        ++phase;
+        const float* src;
+        float2* dst;
+        item(i, src, dst);
+        auto ld0 = [&](int s, int j, int, int) { return stg[s * G::M + j]; };
+        SmemRows rows{sm, G::RP};
+        // the first pass reads the staging tile and writes the work rows: no
+        // load-store barrier (the wait above ordered the previous block's
+        // reads of the work rows)
+        fft_with_hook<G::M, false, G::RT, G::RB, false, G::ROW_MR, false, false, true>(
+            ld0, rows, rows, rows, tw + G::TW_ROW, [&]() {
+                if (i + int(gridDim.x) < count) issue(i + gridDim.x);
+            });
+        r2c_finish<LOGN, 1>(sm, tw, dst);
+        __syncthreads();
+    }
+    return true;
+}
+
+// grid (N/RB, C) for the block variants; for the streaming variant a
+// persistent grid over the nc * N/RB blocks of channels cbase.. (gridDim.x
+// CTAs, gridDim.y = 1).
 template <int LOGN, int V = 0>
 __global__ void __launch_bounds__(R2CShape<LOGN, V>::RT, R2CShape<LOGN, V>::MINB)
     k_row_r2c(const float* __restrict__ state, float2* __restrict__ rowspec,
-              const float2* __restrict__ tw, int cbase) {
+              const float2* __restrict__ tw, int cbase, int nc, int* err) {
     extern __shared__ __align__(128) float2 sm_r2c[];
+    using Sh = R2CShape<LOGN, V>;
     pdl_wait();
     pdl_launch_dependents();
-    row_r2c_variant<LOGN, V>(state, rowspec, tw, blockIdx.y + cbase,
-                             blockIdx.x * R2CShape<LOGN, V>::RB, sm_r2c);
+    if constexpr (Sh::STREAM) {
+        constexpr int N = 1 << LOGN, NB = N / Sh::RB;
+        __shared__ __align__(8) uint64_t bar;
+        init_tile_barrier(&bar);
+        uint32_t phase = 0;
+        auto item = [&](int i, const float*& src, float2*& dst) {
+            const int c = cbase + i / NB, y0 = (i % NB) * Sh::RB;
+            src = state + (size_t(c) * N + y0) * N;
+            dst = rowspec + size_t(c) * (N / 2) * N + y0;
+        };
+        row_r2c_stream<LOGN>(item, nc * NB, tw, sm_r2c, &bar, phase, err);
+    } else {
+        row_r2c_variant<LOGN, V>(state, rowspec, tw, blockIdx.y + cbase, blockIdx.x * Sh::RB,
+                                 sm_r2c);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -361,14 +443,6 @@ __device__ __forceinline__ bool col_conv_body(const float2* __restrict__ rowspec
         });
     }
     return true;
-}
-
-__device__ __forceinline__ void init_tile_barrier(uint64_t* bar) {
-    if (threadIdx.x == 0) {
-        mbar_init(bar, 1);
-        fence_barrier_init();
-    }
-    __syncthreads();
 }
 
 template <int LOGN, int V = 0, bool KRE = false>
@@ -863,24 +937,26 @@ __device__ __forceinline__ void diffusion_pair_body(const float* __restrict__ A,
 // horizontal 3-sums of the last three rows (heads, tails, q) in registers;
 // the vertical sums come from those slots.  Every sum keeps the order of
 // diffusion2_body, so the bits are the same.  A CTA is RS strips of TX/4
-// threads: TX columns by RS * TYR rows.
-template <int LOGN>
+// threads: TX columns by RS * TYR rows.  Strips of STRIP rows (variant 1:
+// 16, variant 3: 8; fewer at small sides) trade the four halo rows each
+// strip re-reads against twice the CTAs and half the unrolled body.
+template <int LOGN, int STRIP = 16>
 struct DiffGeoReg {
     static constexpr int N = 1 << LOGN;
     static constexpr int TX = N < 128 ? N : 128;
-    static constexpr int TYR = N / 4 < 16 ? N / 4 : 16;
+    static constexpr int TYR = N / 4 < STRIP ? N / 4 : STRIP;
     static constexpr int RS = 4;
     static constexpr int TY = RS * TYR;
     static constexpr int THREADS = TX / 4 * RS;
     static_assert(TX % 4 == 0 && N % TY == 0, "tile shape");
 };
 
-template <int LOGN>
+template <int LOGN, int STRIP>
 __device__ __forceinline__ void diffusion_reg_body(const float* __restrict__ A,
                                                    const float* __restrict__ x,
                                                    float* __restrict__ out, int c, int x0, int y0,
                                                    unsigned char* render, int nch) {
-    using D = DiffGeoReg<LOGN>;
+    using D = DiffGeoReg<LOGN, STRIP>;
     constexpr int N = D::N, MASK = N * N - 1;
     const int col = x0 + 4 * (threadIdx.x % (D::TX / 4));   // first of this thread's columns
     const int ys = y0 + (threadIdx.x / (D::TX / 4)) * D::TYR;
@@ -961,18 +1037,33 @@ __device__ __forceinline__ void diffusion_reg_body(const float* __restrict__ A,
     }
 }
 
-// Variant 1 of the diffusion phase is the register body, variant 2 the
-// column-pair body.  TX x TY is the tile of one CTA (one work item).
+// The diffusion phase's variants: 0 the shared-memory tile body, 1 and 3
+// the register body in 16- and 8-row strips, 2 the column-pair body.  All
+// four give the same bits.  TX x TY is the tile of one CTA (one work item).
+constexpr int kDiffVariants = 4;
+template <int LOGN, int V, int KIND = (V == 1 || V == 3) ? 1 : (V == 2 ? 2 : 0)>
+struct DiffTile;
 template <int LOGN, int V>
-struct DiffTile {
-    static constexpr bool PAIR = (V == 2);
-    static constexpr bool REG = (V == 1);
-    static constexpr int THREADS = REG ? DiffGeoReg<LOGN>::THREADS
-                                 : (PAIR ? DiffGeoPair<LOGN, V>::THREADS : DiffGeo2<LOGN, V>::THREADS);
-    static constexpr size_t SMEM =
-        REG ? 0 : (PAIR ? DiffGeoPair<LOGN, V>::SMEM : DiffGeo2<LOGN, V>::SMEM);
-    static constexpr int TX = REG ? DiffGeoReg<LOGN>::TX : Geo<LOGN, V>::TX;
-    static constexpr int TY = REG ? DiffGeoReg<LOGN>::TY : Geo<LOGN, V>::TY;
+struct DiffTile<LOGN, V, 1> {
+    static constexpr bool REG = true, PAIR = false;
+    static constexpr int STRIP = (V == 3) ? 8 : 16;
+    using D = DiffGeoReg<LOGN, STRIP>;
+    static constexpr int THREADS = D::THREADS, TX = D::TX, TY = D::TY;
+    static constexpr size_t SMEM = 0;
+};
+template <int LOGN, int V>
+struct DiffTile<LOGN, V, 2> {
+    static constexpr bool REG = false, PAIR = true;
+    using D = DiffGeoPair<LOGN, V>;
+    static constexpr int THREADS = D::THREADS, TX = D::TX, TY = D::TY;
+    static constexpr size_t SMEM = D::SMEM;
+};
+template <int LOGN, int V>
+struct DiffTile<LOGN, V, 0> {
+    static constexpr bool REG = false, PAIR = false;
+    using D = DiffGeo2<LOGN, V>;
+    static constexpr int THREADS = D::THREADS, TX = D::TX, TY = D::TY;
+    static constexpr size_t SMEM = D::SMEM;
 };
 
 template <int LOGN, int V>
@@ -980,9 +1071,10 @@ __device__ __forceinline__ void diffusion_tile(const float* __restrict__ A,
                                                const float* __restrict__ x,
                                                float* __restrict__ out, int c, int x0, int y0,
                                                float* smf, unsigned char* render, int nch) {
-    if constexpr (DiffTile<LOGN, V>::REG)
-        diffusion_reg_body<LOGN>(A, x, out, c, x0, y0, render, nch);
-    else if constexpr (DiffTile<LOGN, V>::PAIR)
+    using T = DiffTile<LOGN, V>;
+    if constexpr (T::REG)
+        diffusion_reg_body<LOGN, T::STRIP>(A, x, out, c, x0, y0, render, nch);
+    else if constexpr (T::PAIR)
         diffusion_pair_body<LOGN, V>(A, x, out, c, x0, y0, smf, render, nch);
     else
         diffusion2_body<LOGN, V>(A, x, out, c, x0, y0, smf, render, nch);
@@ -1040,18 +1132,18 @@ cudaError_t prepare_variant() {
                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   int(C2RShape<LOGN, V>::SMEM))) != cudaSuccess)
         return e;
-    if constexpr (V <= 2) {
-        if ((e = cudaFuncSetAttribute(k_diffusion<LOGN, V>,
-                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      int(DiffTile<LOGN, V>::SMEM))) != cudaSuccess)
-            return e;
-    }
     if ((e = cudaFuncSetAttribute(k_col_conv<LOGN, V, true>,
                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   int(G::COL_SMEM))) != cudaSuccess)
         return e;
     return cudaFuncSetAttribute(k_col_conv<LOGN, V>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 int(G::COL_SMEM));
+}
+
+template <int LOGN, int V>
+cudaError_t prepare_diffusion() {
+    return cudaFuncSetAttribute(k_diffusion<LOGN, V>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                int(DiffTile<LOGN, V>::SMEM));
 }
 
 template <int LOGN>
@@ -1063,6 +1155,10 @@ cudaError_t prepare_size() {
         if (e == cudaSuccess) e = prepare_variant<LOGN, 3>();
         if (e == cudaSuccess) e = prepare_variant<LOGN, 4>();
     }
+    if (e == cudaSuccess) e = prepare_diffusion<LOGN, 0>();
+    if (e == cudaSuccess) e = prepare_diffusion<LOGN, 1>();
+    if (e == cudaSuccess) e = prepare_diffusion<LOGN, 2>();
+    if (e == cudaSuccess) e = prepare_diffusion<LOGN, 3>();
     return e;
 }
 
@@ -1090,8 +1186,21 @@ cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, int threads, size_t 
 template <int LOGN, int V>
 cudaError_t launch_r2c(const StepArgs& a, int c_lo, int nc, cudaStream_t st) {
     using R = R2CShape<LOGN, V>;
-    return launch_pdl(k_row_r2c<LOGN, V>, dim3((1 << LOGN) / R::RB, nc), R::RT, R::SMEM, st,
-                      a.x_in, a.rowspec, a.tw, c_lo);
+    constexpr int NB = (1 << LOGN) / R::RB;
+    dim3 grid(NB, nc);
+    if constexpr (R::STREAM) {   // persistent: the CTAs that fit at once
+        int dev = 0, sms = 0, per_sm = 0;
+        cudaError_t e = cudaGetDevice(&dev);
+        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (e == cudaSuccess)
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_row_r2c<LOGN, V>, R::RT,
+                                                              R::SMEM);
+        if (e != cudaSuccess) return e;
+        const int ctas = (per_sm > 0 ? per_sm : 1) * sms;
+        grid = dim3(NB * nc < ctas ? NB * nc : ctas, 1);
+    }
+    return launch_pdl(k_row_r2c<LOGN, V>, grid, R::RT, R::SMEM, st, a.x_in, a.rowspec, a.tw, c_lo,
+                      nc, a.err);
 }
 template <int LOGN, int V>
 cudaError_t launch_col(const StepArgs& a, int c_lo, int nc, cudaStream_t st) {
@@ -1116,9 +1225,9 @@ cudaError_t launch_c2r(const StepArgs& a, int c_lo, int nc, cudaStream_t st) {
 }
 template <int LOGN, int V>
 cudaError_t launch_diff(const StepArgs& a, int c_lo, int nc, cudaStream_t st) {
-    using G = Geo<LOGN, V>;
+    constexpr int N = 1 << LOGN;
     using D = DiffTile<LOGN, V>;
-    return launch_pdl(k_diffusion<LOGN, V>, dim3(G::N / D::TX, G::N / D::TY, nc), D::THREADS,
+    return launch_pdl(k_diffusion<LOGN, V>, dim3(N / D::TX, N / D::TY, nc), D::THREADS,
                       D::SMEM, st, a.A, a.x_in, a.x_out, c_lo, a.render, a.C);
 }
 
@@ -1145,6 +1254,15 @@ cudaError_t launch_diff(const StepArgs& a, int c_lo, int nc, cudaStream_t st) {
         CG_VARIANT_SWITCH(v, FN, __VA_ARGS__)                               \
     }
 
+// The diffusion phase's four variants (every size).
+#define CG_DIFF_SWITCH(v, FN, ...)               \
+    switch (v) {                                  \
+        case 1: FN<LOGN, 1>(__VA_ARGS__); break;  \
+        case 2: FN<LOGN, 2>(__VA_ARGS__); break;  \
+        case 3: FN<LOGN, 3>(__VA_ARGS__); break;  \
+        default: FN<LOGN, 0>(__VA_ARGS__); break; \
+    }
+
 // The given phases for channels [c_lo, c_hi), each in the variant a.var
 // names.
 template <int LOGN>
@@ -1160,7 +1278,7 @@ cudaError_t launch_step_range(const StepArgs& a, int phases, int c_lo, int c_hi,
     if (phases & kPhaseGrowth) { CG_VARIANT_SWITCH5(a.var.c2r, e = launch_c2r, a, c_lo, nc, st) }
     if (e != cudaSuccess) return e;
     if (phases & kPhaseDiffusion) {
-        CG_VARIANT_SWITCH(a.var.diff, e = launch_diff, a, c_lo, nc, st)
+        CG_DIFF_SWITCH(a.var.diff, e = launch_diff, a, c_lo, nc, st)
     }
     if (e != cudaSuccess) return e;
     return cudaGetLastError();

@@ -188,6 +188,11 @@ int cg_timed_iterate(cg_sim* sim, double ms[4]);
  *   0-2  CTA shapes (rows per CTA and threads for the row FFTs, columns per
  *        CTA and threads for the column pass, tile rows and columns per
  *        thread for diffusion), radix-16 plans; bit-identical results.
+ *        The forward row FFT's variant 2 is variant 1's tile in a
+ *        persistent grid whose CTAs bring each block of rows in with one
+ *        bulk copy, the next block's during the current one's transform.
+ *   3    for diffusion, at every grid side: variant 1's register tiles in
+ *        strips of 8 rows instead of 16; bit-identical results.
  *   3, 4 FFT plans, for the row and column phases at grid sides >= 512:
  *        row FFTs over two real rows as one complex sequence of length n
  *        with radix-16 (3) or radix-8 (4) passes; the column pass with its
@@ -195,7 +200,7 @@ int cg_timed_iterate(cg_sim* sim, double ms[4]);
  *        first forward) in the CTA shape of variant 1 (3) or 0 (4).  These
  *        agree with variants 0-2 to rounding (the same step error bar
  *        against FP64), not bit for bit.
- * Diffusion, and every phase below side 512, has variants 0-2 only.
+ * Diffusion has variants 0-3; the other phases below side 512 have 0-2.
  * cg_autotune times every variant of every phase `reps` times on the live
  * handle (the state is not advanced), keeps the fastest per phase, then
  * picks the graph layout (cg_set_graph_layout) and re-captures the step

@@ -180,9 +180,9 @@ def test_kernel_reupload_and_zero_kernel():
 
 @pytest.mark.parametrize("n", [16, 32, 64, 256, 1024, 2048])
 def test_variants_agree_and_autotune(n):
-    """Every CTA-shape variant (0-2) computes the same bits; the autotuner
-    keeps a variant of each phase that exists at this size and does not
-    step the world."""
+    """Every CTA-shape variant (0-2, and diffusion's 3) computes the same
+    bits; the autotuner keeps a variant of each phase that exists at this
+    size and does not step the world."""
     cr = make_creature(n, 3, seed=70 + n, radius=(max(2.0, n / 16), max(4.0, n / 6)),
                        seed_box=n // 2)
     with GpuMaceLenia.from_creature(cr) as sim:
@@ -190,14 +190,14 @@ def test_variants_agree_and_autotune(n):
         sim.run_steps(3)
         ref = sim.state()
     for p in range(4):
-        for v in (1, 2):
+        for v in ((1, 2, 3) if p == 3 else (1, 2)):
             var = [0, 0, 0, 0]
             var[p] = v
             with GpuMaceLenia.from_creature(cr) as sim:
                 sim.set_variants(var)
                 sim.run_steps(3)
                 np.testing.assert_array_equal(sim.state(), ref, err_msg=str(var))
-    counts = [5 if n >= 512 and p < 3 else 3 for p in range(4)]
+    counts = [4 if p == 3 else (5 if n >= 512 else 3) for p in range(4)]
     with GpuMaceLenia.from_creature(cr) as sim:
         x0 = sim.state()
         chosen, ms = sim.autotune(reps=3)
@@ -369,3 +369,27 @@ def test_graph_layouts_agree(n):
         b.autotune(reps=2)
         assert b.graph_layout() in (0, 1)
         np.testing.assert_array_equal(b.state(), x)
+
+
+@pytest.mark.parametrize("var", [[3, 3, 3, 3], [4, 4, 4, 2]])
+def test_plan_variants_irregular_and_maximal_maps(var):
+    """The FFT-plan variants on the maps that stress the kernel grouping:
+    an irregular map at 512^2 (the reference's slot copy mishandles it) and
+    the largest world the ABI accepts in channels and kernels (C = 16,
+    K = 64), each step against the FP64 oracle."""
+    cases = [make_creature(512, 3, seed=61, c0=[1, 0, 2, 1, 2], c1=[0, 1, 1, 2, 0],
+                           radius=(8, 30), seed_box=256)]
+    C, K = 16, 64
+    cases.append(make_creature(512, C, seed=62, c0=np.arange(K) % C, c1=(np.arange(K) * 5 + 3) % C,
+                               radius=(8, 24), seed_box=128))
+    for cr in cases:
+        a = (cr.kspec.astype(np.complex128), cr.c0, cr.c1, cr.mu.astype(np.float64),
+             cr.sigma.astype(np.float64), cr.weights.astype(np.float64), cr.temp)
+        with GpuMaceLenia.from_creature(cr) as sim:
+            sim.set_variants(var)
+            for _ in range(2):
+                x = sim.state()
+                sim.iterate()
+                ref, _, _ = O.step_c(x.astype(np.float64), *a, nthreads=os.cpu_count() or 1)
+                err = float(np.abs(sim.state() - ref).max())
+                assert err <= STEP_TOL, (cr.C, cr.K, err)
