@@ -66,6 +66,7 @@ SIGNATURES = {
     "cg_set_kernel": ([_P, _I, _FP], _I),
     "cg_upload_channel": ([_P, _I, _DP], _I),
     "cg_set_kernel_device": ([_P, _I, _P], _I),
+    "cg_set_kernels_spatial_device": ([_P, _P], _I),
     "cg_set_params": ([_P, _FP, _FP, _FP, _F], _I),
     "cg_set_params_device": ([_P, _P, _P, _P], _I),
     "cg_build_ring_kernels": ([_P, _P, _P], _I),

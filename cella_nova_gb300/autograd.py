@@ -92,32 +92,25 @@ class LeniaWorld:
         check(self.lib.cg_build_ring_kernels(self.h, ctypes.cast(specs, ctypes.c_void_p),
                                              _p(rings)))
 
-    def load(self, mu, sigma, weights, spec):
-        """Growth parameters (host arrays) and kernel spectra (K, n, n, 2) f32
-        on the device."""
+    def load(self, mu, sigma, weights, h: torch.Tensor):
+        """Growth parameters (host arrays) and the spatial kernels h (K, n, n)
+        f32 on the device, whose spectra the library takes with its own
+        FFTs (cg_set_kernels_spatial_device)."""
         mu = np.ascontiguousarray(mu, np.float32)
         sg = np.ascontiguousarray(sigma, np.float32)
         w = np.ascontiguousarray(weights, np.float32)
         check(self.lib.cg_set_params(self.h, fptr(mu), fptr(sg), fptr(w),
                                      ctypes.c_float(self.temp)))
-        for k in range(self.K):
-            check(self.lib.cg_set_kernel_device(self.h, k, _p(spec[k])))
-
-
-def kernel_spectra(h: torch.Tensor) -> torch.Tensor:
-    """(K, n, n) real spatial kernels -> (K, n, n, 2) f32 interleaved spectra,
-    transformed in float64 and rounded once (the .bin format's precision)."""
-    s = torch.fft.fft2(h.detach().to(torch.float64)).to(torch.complex64)
-    return torch.view_as_real(s).contiguous()
+        check(self.lib.cg_set_kernels_spatial_device(self.h, _p(h)))
 
 
 class _Unroll(torch.autograd.Function):
     @staticmethod
     def forward(ctx, world, T, every, seed, mu, sigma, weights, h):
         lib = world.lib
-        spec = kernel_spectra(h)
+        hk = h.detach().float().contiguous()
         host = [t.detach().float().cpu().numpy() for t in (mu, sigma, weights)]
-        world.load(*host, spec)
+        world.load(*host, hk)
         x0 = seed.detach().float().contiguous()
         nck = (T - 1) // every + 1
         ckpt = torch.empty((nck,) + tuple(x0.shape), dtype=torch.float32, device=x0.device)
@@ -125,7 +118,7 @@ class _Unroll(torch.autograd.Function):
         check(lib.cg_unroll(world.h, _p(x0), int(T), int(every), _p(ckpt), _p(xT)))
         ctx.world, ctx.T, ctx.every = world, int(T), int(every)
         ctx.dtypes = (seed.dtype, mu.dtype, sigma.dtype, weights.dtype, h.dtype)
-        ctx.host, ctx.spec = host, spec
+        ctx.host, ctx.h = host, hk
         ctx.save_for_backward(ckpt)
         return xT
 
@@ -134,7 +127,7 @@ class _Unroll(torch.autograd.Function):
         world = ctx.world
         lib = world.lib
         (ckpt,) = ctx.saved_tensors
-        world.load(*ctx.host, ctx.spec)   # another unroll may have run since
+        world.load(*ctx.host, ctx.h)   # another unroll may have run since
         gT = gT.contiguous().float()
         g0 = torch.empty_like(gT)
         gtmp = torch.empty_like(gT)

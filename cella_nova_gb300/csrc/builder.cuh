@@ -12,7 +12,8 @@ namespace cg {
 
 // grid (M/TW, K), CT threads.  rows: [K][M][N] (rowspec layout: 2x the row
 // DFT, X[0] + i X[M] packed in column 0); zsum[k] = sum of kernel k's spatial
-// values.  kspec: [K][M+1][N] packed as k_pack_kernel writes it.
+// values, or zsum = nullptr for no normaliser (the spectra of the kernels as
+// given).  kspec: [K][M+1][N] packed as k_pack_kernel writes it.
 template <int LOGN>
 __global__ void __launch_bounds__(256) k_kspec_cols(const float2* __restrict__ rows,
                                                      float2* __restrict__ kspec,
@@ -28,7 +29,7 @@ __global__ void __launch_bounds__(256) k_kspec_cols(const float2* __restrict__ r
     FftPasses<N, 1, false, T, TW, false>::run(ld, cols, cols, cols, tw + G::TW_COL_FWD);
     __syncthreads();
     // P = 2 K^ (column kx >= 1); kspec holds K^ / (2 N^2 sum h)
-    const double z = zsum[k];
+    const double z = zsum ? zsum[k] : 1.0;
     const float scale = z != 0.0 ? float(1.0 / (4.0 * double(N) * double(N) * z)) : 0.f;
     float2* out = kspec + size_t(k) * (M + 1) * N;
     for (int e = threadIdx.x; e < TW * N; e += T) {

@@ -62,6 +62,14 @@ int cuda_fail(cudaError_t e, const char* what) {
     return fail(CG_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
 }
 
+// Device buffers given to the library feed 16-byte vector loads and bulk
+// copies (TMA), so each must start on a 16-byte boundary (every cudaMalloc
+// and PyTorch allocation does; a view at an odd element offset may not).
+bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
+int misaligned(const char* fn) {
+    return fail(CG_ERR_ARG, "%s: device buffers must be 16-byte aligned", fn);
+}
+
 #define CG_CHECK(call, what)                                \
     do {                                                    \
         cudaError_t e_ = (call);                            \
@@ -704,6 +712,7 @@ int cg_kernels_real(cg_sim* s, int* real) {
 
 int cg_set_kernel_device(cg_sim* s, int k, const float* dev_spec) {
     if (!s || !dev_spec) return fail(CG_ERR_ARG, "cg_set_kernel_device: NULL argument");
+    if (!aligned16(dev_spec)) return misaligned("cg_set_kernel_device");
     if (k < 0 || k >= s->K) return fail(CG_ERR_ARG, "kernel index %d outside [0, %d)", k, s->K);
     const size_t half = size_t(s->n / 2) * s->n;
     CG_CHECK(s->ops->pack(reinterpret_cast<const float2*>(dev_spec),
@@ -1107,10 +1116,31 @@ int cg_build_ring_kernels(cg_sim* s, const cg_ring_spec* specs, const float* dev
     return set_kernel_realness(s, -1, false);
 }
 
+int cg_set_kernels_spatial_device(cg_sim* s, const float* dev_h) {
+    if (!s || !dev_h) return fail(CG_ERR_ARG, "cg_set_kernels_spatial_device: NULL argument");
+    // the builder's scratch (the second half of U) holds an aligned copy for
+    // the row transform, as cg_build_ring_kernels' builder output does
+    const size_t half = size_t(s->n / 2) * s->n;
+    float2* rows = s->U;
+    float* h = reinterpret_cast<float*>(s->U + size_t(s->K) * half);
+    CG_CHECK(cudaMemcpyAsync(h, dev_h, sizeof(float) * size_t(s->K) * s->px(),
+                             cudaMemcpyDeviceToDevice, s->stream),
+             "copying the spatial kernels");
+    StepArgs a = s->args(s->cur, nullptr);
+    a.C = s->K;   // the kernels pass through the row transform as channels
+    a.x_in = h;
+    a.rowspec = rows;
+    CG_CHECK(s->ops->step(a, kPhaseRowFwd, s->stream), "launching the builder's row transform");
+    CG_CHECK(s->ops->kspec_cols(rows, s->kspec, s->tw, nullptr, s->K, s->stream),
+             "launching the builder's column transform");
+    return set_kernel_realness(s, -1, false);
+}
+
 int cg_ring_weight_grad(cg_sim* s, const cg_ring_spec* specs, const float* dev_ring_weights,
                         const float* dev_hbar, float* dev_grad) {
     if (!s || !specs || !dev_hbar || !dev_grad)
         return fail(CG_ERR_ARG, "cg_ring_weight_grad: NULL argument");
+    if (!aligned16(dev_hbar)) return misaligned("cg_ring_weight_grad");
     RingSet rs;
     int rc = ring_set(s, specs, &rs, "cg_ring_weight_grad");
     if (rc != CG_OK) return rc;
@@ -1133,6 +1163,7 @@ int cg_set_params_device(cg_sim* s, const float* dev_mu, const float* dev_sigma,
 int cg_step_from(cg_sim* s, const float* x_in, float* x_out) {
     if (!s || !x_in || !x_out) return fail(CG_ERR_ARG, "cg_step_from: NULL argument");
     if (x_in == x_out) return fail(CG_ERR_ARG, "cg_step_from: input and output must differ");
+    if (!aligned16(x_in) || !aligned16(x_out)) return misaligned("cg_step_from");
     StepArgs a = s->args(s->cur, nullptr);
     a.x_in = x_in;
     a.x_out = x_out;
@@ -1146,6 +1177,8 @@ int cg_step_backward(cg_sim* s, const float* x, const float* ybar, float* xbar, 
         return fail(CG_ERR_ARG, "cg_step_backward: NULL argument");
     if (xbar == ybar || xbar == x)
         return fail(CG_ERR_ARG, "cg_step_backward: xbar must not alias x or ybar");
+    if (!aligned16(x) || !aligned16(ybar) || !aligned16(xbar) || !aligned16(kgrad))
+        return misaligned("cg_step_backward");
     int rc = ensure_backward(s);
     if (rc != CG_OK) return rc;
     CG_CHECK(s->ops->backward(bwd_args(s, x, ybar, xbar, pgrad, reinterpret_cast<float2*>(kgrad)),
@@ -1175,6 +1208,7 @@ int cg_zero_grads(cg_sim* s, double* pgrad, float* kgrad) {
 
 int cg_kernel_grad_spatial(cg_sim* s, float* kgrad, float* hbar) {
     if (!s || !kgrad || !hbar) return fail(CG_ERR_ARG, "cg_kernel_grad_spatial: NULL argument");
+    if (!aligned16(kgrad) || !aligned16(hbar)) return misaligned("cg_kernel_grad_spatial");
     int rc = ensure_backward(s);
     if (rc != CG_OK) return rc;
     CG_CHECK(s->ops->kgrad_final(reinterpret_cast<float2*>(kgrad), hbar, s->K, s->tw, s->stream),
@@ -1185,6 +1219,7 @@ int cg_kernel_grad_spatial(cg_sim* s, float* kgrad, float* hbar) {
 int cg_unroll(cg_sim* s, const float* x0, int T, int every, float* ckpt, float* xT) {
     if (!s || !x0 || !ckpt || !xT) return fail(CG_ERR_ARG, "cg_unroll: NULL argument");
     if (T < 1 || every < 1) return fail(CG_ERR_ARG, "cg_unroll: T=%d, every=%d", T, every);
+    if (!aligned16(x0) || !aligned16(ckpt) || !aligned16(xT)) return misaligned("cg_unroll");
     const size_t bytes = sizeof(float) * s->C * s->px();
     const size_t plane = size_t(s->C) * s->px();
     for (auto& p : s->utmp)
@@ -1209,6 +1244,9 @@ int cg_unroll_backward(cg_sim* s, const float* ckpt, int T, int every, const flo
     if (!s || !ckpt || !gT || !g0 || !pgrad || !seg || !gtmp)
         return fail(CG_ERR_ARG, "cg_unroll_backward: NULL argument");
     if (T < 1 || every < 1) return fail(CG_ERR_ARG, "cg_unroll_backward: T=%d, every=%d", T, every);
+    if (!aligned16(ckpt) || !aligned16(gT) || !aligned16(g0) || !aligned16(kgrad) ||
+        !aligned16(seg) || !aligned16(gtmp))
+        return misaligned("cg_unroll_backward");
     int rc = ensure_backward(s);
     if (rc != CG_OK) return rc;
     const size_t bytes = sizeof(float) * s->C * s->px();

@@ -95,6 +95,12 @@ class GpuMaceLenia:
         interleaved f32 pairs), enqueued on the handle's stream."""
         check(self._lib.cg_set_kernel_device(self._h, int(kernel_idx), ctypes.c_void_p(dev_ptr)))
 
+    def set_kernels_spatial_device(self, dev_ptr: int):
+        """All K kernels from their spatial form: K*n*n f32 on the device
+        (origin at [0][0]); the library takes the spectra with its own FFTs
+        (cg_set_kernels_spatial_device)."""
+        check(self._lib.cg_set_kernels_spatial_device(self._h, ctypes.c_void_p(dev_ptr)))
+
     def upload_channel(self, data, channel):
         """Channel ``channel`` from n*n f64 values (mod.rs:217-226)."""
         a = np.ascontiguousarray(data, dtype=np.float64).reshape(-1)

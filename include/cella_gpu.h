@@ -86,8 +86,17 @@ int cg_set_kernel(cg_sim* sim, int k, const float* spec_interleaved);
 int cg_kernels_real(cg_sim* sim, int* real);
 
 /* set_kernel from DEVICE memory: kernel k's full n*n complex spectrum,
- * interleaved (re, im) f32, already on the GPU (no host round trip). */
+ * interleaved (re, im) f32, already on the GPU (no host round trip); the
+ * buffer must be 16-byte aligned (CG_ERR_ARG otherwise). */
 int cg_set_kernel_device(cg_sim* sim, int k, const float* dev_spec_interleaved);
+
+/* All K kernels from their SPATIAL form: dev_h holds K*n*n f32 (kernel k's
+ * n x n values, origin at [0][0], as the .bin spectra's inverse FFT), in
+ * device memory.  The spectra are taken on the GPU with the step's own row
+ * and column FFTs (no normaliser: the kernels as given) and stored as
+ * cg_set_kernel would store their fft2; the column pass keeps the complex
+ * form.  Uses the handle's spectrum scratch: enqueue it between steps. */
+int cg_set_kernels_spatial_device(cg_sim* sim, const float* dev_h);
 
 /* GpuMaceLenia::upload_channel, mod.rs:217-226: channel c from n*n doubles,
  * rounded to f32 (mod.rs:220 casts with `as f32`, round-to-nearest). */
@@ -271,7 +280,11 @@ int cg_synchronize(cg_sim* sim);
  * Differentiation (no counterpart in the Rust orchestrator; the reference
  * differentiates its PyTorch model, train/diff_lenia_org.py, with autograd).
  * Array arguments here are DEVICE pointers on the handle's device, except
- * those of cg_set_params; work is enqueued on the handle's stream.
+ * those of cg_set_params; work is enqueued on the handle's stream.  The
+ * state- and spectrum-sized ones (x, ybar, xbar, kgrad, hbar, x0, ckpt, xT,
+ * gT, g0, seg, gtmp, x_in, x_out) must be 16-byte aligned, as every
+ * cudaMalloc and PyTorch allocation is (CG_ERR_ARG otherwise): the kernels
+ * read them with 16-byte vector loads and bulk copies.
  * ------------------------------------------------------------------------- */
 
 /* Replace mu/sigma/weights (K each, HOST arrays) and temp.  Same checks as

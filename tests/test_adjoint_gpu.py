@@ -8,7 +8,7 @@ import pytest
 torch = pytest.importorskip("torch")
 
 from cella_nova_gb300 import GpuMaceLenia  # noqa: E402
-from cella_nova_gb300.autograd import DiffusionLeniaGPU, LeniaWorld, kernel_spectra  # noqa: E402
+from cella_nova_gb300.autograd import DiffusionLeniaGPU, LeniaWorld  # noqa: E402
 from cella_nova_gb300.creature import make_creature, ring_kernel  # noqa: E402
 from oracle import autograd_ref as AR  # noqa: E402
 
@@ -32,7 +32,7 @@ def test_single_step_vjp_matches_fp64():
     x = torch.tensor(cr.seed, dtype=torch.float32, device=dev)
     ybar = torch.tensor(rng.standard_normal(cr.seed.shape), dtype=torch.float32, device=dev)
     w = LeniaWorld(cr.n, cr.C, cr.c0, cr.c1, cr.temp)
-    w.load(cr.mu, cr.sigma, cr.weights, kernel_spectra(torch.tensor(h64, device=dev)))
+    w.load(cr.mu, cr.sigma, cr.weights, torch.tensor(h64, dtype=torch.float32, device=dev))
     xbar = torch.empty_like(x)
     pgrad = torch.zeros(3 * cr.K, dtype=torch.float64, device=dev)
     kgrad = torch.zeros((cr.K, cr.n // 2, cr.n, 2), dtype=torch.float32, device=dev)
@@ -101,7 +101,8 @@ def test_unroll_forward_equals_graph_steps():
 
 def test_unroll_with_spatial_kernels_matches_fp64():
     """The kernel-agnostic path: spatial kernels h as a tensor (here the
-    ring kernels, spectra taken by torch), gradients against FP64 autograd."""
+    ring kernels; the library takes their spectra with its own FFTs),
+    gradients against FP64 autograd."""
     from cella_nova_gb300.autograd import unroll
     n, C, T, every = 64, 2, 6, 4
     cr = make_creature(n, C, seed=77, radius=(4, 12), seed_box=32)

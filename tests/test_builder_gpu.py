@@ -99,3 +99,28 @@ def test_ring_weight_grad_matches_torch_autograd():
         B = len(ref)
         np.testing.assert_allclose(got[k, :B], ref, rtol=1e-4, atol=1e-4 * np.abs(ref).max())
         assert (got[k, B:] == 0).all()
+
+
+@pytest.mark.parametrize("n,C,seed", [(64, 3, 11), (512, 2, 12)])
+def test_spatial_kernels_on_the_gpu_match_oracle(n, C, seed):
+    """cg_set_kernels_spatial_device: the spectra of spatial kernels (the
+    creature's rings, with no normaliser applied) taken by the library's own
+    FFTs step within the bar of the FP64 oracle run on their FP64 fft2, and
+    the convolutions agree with those of cg_set_kernel's host spectra."""
+    import torch
+    from cella_nova_gb300.creature import ring_kernel
+    cr = make_creature(n, C, seed=seed, radius=(max(2.0, n / 16), max(4.0, n / 6)),
+                       seed_box=n // 2)
+    h64 = np.stack([ring_kernel(n, R, b) for R, b in zip(cr.ring_radius, cr.ring_weights)])
+    hd = torch.tensor(h64, dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()
+    with GpuMaceLenia.from_creature(cr) as a, GpuMaceLenia.from_creature(cr) as b:
+        b.set_kernels_spatial_device(hd.data_ptr())
+        ua, ub = conv_of(a, cr.K, n), conv_of(b, cr.K, n)
+        assert np.abs(ua - ub).max() <= 2e-6 * np.abs(ua).max()
+        x = b.state()
+        b.iterate()
+        ref, _, _ = (O.step_c if n <= 256 else O.step_np)(
+            x.astype(np.float64), np.fft.fft2(h64), cr.c0, cr.c1, cr.mu.astype(np.float64),
+            cr.sigma.astype(np.float64), cr.weights.astype(np.float64), cr.temp)
+        assert np.abs(b.state() - ref).max() <= 1e-5

@@ -75,6 +75,31 @@ def test_unroll_argument_errors():
     w.close()
 
 
+def test_misaligned_device_buffers_are_rejected():
+    """Device buffers start on 16-byte boundaries (the kernels read them with
+    16-byte loads and bulk copies): a pointer 4 bytes in is refused on the
+    host, before anything is launched, and the world still steps."""
+    import ctypes
+    torch = pytest.importorskip("torch")
+    from cella_nova_gb300.autograd import LeniaWorld
+    cr = make_creature(64, 2, seed=6, radius=(4, 12), seed_box=32)
+    w = LeniaWorld(cr.n, cr.C, cr.c0, cr.c1, cr.temp)
+    plane = cr.C * 64 * 64
+    buf = torch.zeros(2 * plane + 8, device="cuda")
+    x, y = buf[:plane], buf[plane + 4:2 * plane + 4]
+    odd = ctypes.c_void_p(buf.data_ptr() + 4)
+    P = lambda t: ctypes.c_void_p(t.data_ptr())
+    assert w.lib.cg_step_from(w.h, odd, P(y)) == ARG
+    assert b"16-byte aligned" in w.lib.cg_last_error()
+    assert w.lib.cg_step_from(w.h, P(x), odd) == ARG
+    assert w.lib.cg_unroll(w.h, odd, 4, 4, P(y), P(x)) == ARG
+    assert w.lib.cg_set_kernel_device(w.h, 0, odd) == ARG
+    assert w.lib.cg_step_from(w.h, P(x), P(y)) == 0
+    torch.cuda.synchronize()
+    assert torch.isfinite(y).all()
+    w.close()
+
+
 def test_bounded_wait_gives_up_and_reports_timeout():
     """A device-side wait that nothing completes (an mbarrier no thread or
     copy arrives on) ends at its limit with the timeout status; the context
