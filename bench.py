@@ -581,7 +581,7 @@ def measure_plain_1024(dev, sampler, steps=200, check=True):
     real = sim.kernels_real()
     m0 = sim.mass_f64()
     checks = {"step 1": sample_step(sim)}
-    sim.autotune(reps=10)
+    _, tune_ms = sim.autotune(reps=10)
     sim.run_steps(3)
     sim.synchronize()
     stream = torch.cuda.ExternalStream(sim.stream())
@@ -600,6 +600,7 @@ def measure_plain_1024(dev, sampler, steps=200, check=True):
     out = {"metric": "cell-updates/s (DiffusionLenia fwd step, 1024^2, C=3, K=9)",
            "value": px * steps / (ms / 1e3), "unit": UNIT, "steps": steps,
            "ms_per_step": ms / steps, "variants": variants, "graph_layout": layout,
+           "autotune_ms": [[round(float(t), 4) for t in row] for row in tune_ms],
            "kernel_spectra": "real (point-symmetric kernels)" if real else "complex",
            "hbm_frac_as_built": bytes_per_px_as_built(3, 9, real) * px / (ms / 1e3 / steps) / 1e9
            / peaks()[0],
