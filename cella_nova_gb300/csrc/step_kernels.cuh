@@ -30,11 +30,12 @@ namespace cg {
 // Geometry of one grid size.  V selects a variant (the autotuner times
 // them): row kernels V=1 / V=2 halve / quarter the rows per CTA and the
 // threads (the forward row pass's variant 2 streams variant 1's tile
-// instead, R2CShape); the column kernel V=1 halves and V=2 doubles the columns and the
-// threads per CTA (work per thread is unchanged); diffusion V=1 keeps its
-// sums in registers (DiffGeoReg) and V=2 uses 64 tile rows with two columns
-// per thread instead of 32 rows (the diffusion adjoint takes V=1 as 16 tile
-// rows).  Variants 0-2 compute the same bits.
+// instead, R2CShape); the column kernel V=1 halves and V=2 doubles the
+// columns and the threads per CTA (work per thread is unchanged); diffusion
+// V=1 keeps its sums in registers (DiffGeoReg, 16-row strips; V=3 the same
+// in 8-row strips, DiffTile) and V=2 uses 64 tile rows with two columns per
+// thread instead of 32 rows (the diffusion adjoint takes V=1 as 16 tile
+// rows).  Variants 0-2, and diffusion's 3, compute the same bits.
 //
 // Variants 3 and 4 (grid sides of at least kMinPairLogN) change the FFT
 // plans instead of only the shapes, and agree with the others to rounding:
