@@ -101,12 +101,15 @@ def test_ring_weight_grad_matches_torch_autograd():
         assert (got[k, B:] == 0).all()
 
 
-@pytest.mark.parametrize("n,C,seed", [(64, 3, 11), (512, 2, 12)])
-def test_spatial_kernels_on_the_gpu_match_oracle(n, C, seed):
+@pytest.mark.parametrize("n,C,seed,var", [(64, 3, 11, None), (512, 2, 12, None),
+                                          (512, 2, 13, [2, 3, 3, 3]), (512, 3, 14, [3, 4, 4, 1])])
+def test_spatial_kernels_on_the_gpu_match_oracle(n, C, seed, var):
     """cg_set_kernels_spatial_device: the spectra of spatial kernels (the
     creature's rings, with no normaliser applied) taken by the library's own
     FFTs step within the bar of the FP64 oracle run on their FP64 fft2, and
-    the convolutions agree with those of cg_set_kernel's host spectra."""
+    the convolutions agree with those of cg_set_kernel's host spectra.  The
+    transform runs the handle's forward row pass in whatever variant it is
+    set to (here also the streamed and the paired-row forms)."""
     import torch
     from cella_nova_gb300.creature import ring_kernel
     cr = make_creature(n, C, seed=seed, radius=(max(2.0, n / 16), max(4.0, n / 6)),
@@ -115,6 +118,8 @@ def test_spatial_kernels_on_the_gpu_match_oracle(n, C, seed):
     hd = torch.tensor(h64, dtype=torch.float32, device="cuda")
     torch.cuda.synchronize()
     with GpuMaceLenia.from_creature(cr) as a, GpuMaceLenia.from_creature(cr) as b:
+        if var is not None:
+            b.set_variants(var)
         b.set_kernels_spatial_device(hd.data_ptr())
         ua, ub = conv_of(a, cr.K, n), conv_of(b, cr.K, n)
         assert np.abs(ua - ub).max() <= 2e-6 * np.abs(ua).max()
