@@ -487,6 +487,8 @@ def run_ours(args):
         line["grad"] = measure_grad(dev, sampler, iters=10, warmup=3, check=check)
         line["search"] = measure_search(dev, sampler, iters=3, warmup=3, ncand=args.candidates,
                                         check=check)
+        line["next_rows"] = measure_next_rows(dev, tuned["variants"] if tuned else [0, 0, 0, 0],
+                                              check=check)
     sampler.stop()
     if rank == 0:
         print(json.dumps(line), flush=True)
@@ -611,6 +613,123 @@ def measure_plain_1024(dev, sampler, steps=200, check=True):
            "l2": "no flush: each step streams ~0.2 GB (> 129 MB L2)"}
     if check:
         out["step_error_vs_fp64"] = step_errors(checks, cr)
+    return out
+
+
+def measure_next_rows(dev, variants, reps=50, check=True):
+    """The survey's "next" rows on the 2048^2, C=3, K=9 creature, each with a
+    figure and a parity check:
+    - render: a rendering step against a plain step, the standalone render
+      kernel, the RGB24 download, and frame streaming to a
+      file descriptor (the video loop, main.rs:239-303); render words against
+      the FP32 restatement of render_main (compute_1024.wgsl:428-443);
+    - kernel builder: K ring kernels built and transformed on the GPU against
+      the host generator (numpy ring kernels and FFT in FP64, what
+      generate_kernel_json.py does), two kernels timed and scaled to K; a step
+      with the built spectra against one with the host spectra;
+    - binary seed: load time of a 1024^2, C=3 seed as JSON and as its binary
+      twin, and the two loads compared value for value."""
+    import tempfile
+    import torch
+    from cella_nova_gb300 import GpuMaceLenia
+    from cella_nova_gb300.creature import (make_creature, ring_kernel, write_seed_bin,
+                                           write_seed_json)
+    from cella_nova_gb300.orchestrator import creature_ring_specs, load_config
+    n, px = N_GRID, N_GRID * N_GRID
+    cr = make_creature(n, C_CH, seed=2048, temp=1.0, device=dev)
+    out = {}
+    with GpuMaceLenia.from_creature(cr) as sim:
+        sim.set_variants(variants)
+        stream = torch.cuda.ExternalStream(sim.stream())
+        for _ in range(3):
+            sim.iterate()
+            sim.iterate_and_render()
+            sim.render()
+        sim.synchronize()
+        plain = timed(stream, lambda: [sim.iterate() for _ in range(reps)]) / reps
+        fused = timed(stream, lambda: [sim.iterate_and_render() for _ in range(reps)]) / reps
+        alone = timed(stream, lambda: [sim.render() for _ in range(reps)]) / reps
+        t0 = time.perf_counter()
+        for _ in range(5):
+            rgb = sim.download_render()
+        dl_s = (time.perf_counter() - t0) / 5
+        nframes = 20
+        with open(os.devnull, "wb") as f:
+            t0 = time.perf_counter()
+            sim.stream_frames(f.fileno(), nframes, 1)
+            fr_s = time.perf_counter() - t0
+        render = {"step_ms": plain, "step_with_render_ms": fused,
+                  "render_cost_ms": fused - plain,
+                  "render_how": "iterate_and_render: the diffusion kernels also write level "
+                                "bytes, then one kernel packs them into 0x00RRGGBB words",
+                  "render_kernel_ms": alone,
+                  "render_kernel_gbs": (C_CH * 4 + 4) * px / (alone / 1e3) / 1e9,
+                  "download_rgb24_ms": dl_s * 1e3,
+                  "frames_per_s": nframes / fr_s,
+                  "frames": f"{nframes} RGB24 frames of {n}^2 to /dev/null, one step each "
+                            "(cg_stream_frames)"}
+        if check:
+            from oracle import oracle as O
+            sim.iterate_and_render()
+            words = sim.download_render_packed()
+            render["words_equal_oracle"] = bool(np.array_equal(words, O.render_np(sim.state())))
+            render["rgb24_equal_oracle"] = bool(np.array_equal(sim.download_render(),
+                                                               O.rgb24_np(words)))
+        out["render"] = render
+
+        # kernel builder
+        specs, w = creature_ring_specs(cr)
+        wd = torch.tensor(w, device=dev)
+        torch.cuda.synchronize()
+        x = sim.state()
+        sim.build_ring_kernels(specs, wd.data_ptr())   # warm-up (re-captures the graphs once)
+        sim.synchronize()
+        build = timed(stream, lambda: [sim.build_ring_kernels(specs, wd.data_ptr())
+                                       for _ in range(10)]) / 10
+        t0 = time.perf_counter()
+        nk = 2
+        for k in range(nk):
+            np.fft.fft2(ring_kernel(n, cr.ring_radius[k], cr.ring_weights[k]))
+        host_s = (time.perf_counter() - t0) / nk * cr.K
+        builder = {"kernels": cr.K, "gpu_ms": build, "host_generator_ms": host_s * 1e3,
+                   "host_how": f"numpy ring kernel + FP64 fft2 per kernel, {nk} of {cr.K} "
+                               f"timed and scaled to {cr.K}, one host thread"}
+        # one step from the same state with the built spectra, then with the
+        # host spectra (cg_set_kernel)
+        for c in range(C_CH):
+            sim.upload_channel_f32(x[c], c)
+        sim.iterate()
+        y_built = sim.state()
+        for k in range(cr.K):
+            sim.set_kernel(cr.kspec[k], k)
+        for c in range(C_CH):
+            sim.upload_channel_f32(x[c], c)
+        sim.iterate()
+        builder["step_max_abs_diff_vs_host_spectra"] = float(np.abs(y_built - sim.state()).max())
+        out["kernel_builder"] = builder
+
+    # binary seed against JSON
+    seed_cr = make_creature(1024, 3, seed=1024)
+    with tempfile.TemporaryDirectory() as d:
+        js, bs = os.path.join(d, "s.json"), os.path.join(d, "s.bin")
+        write_seed_json(js, seed_cr)
+        write_seed_bin(bs, seed_cr)
+        times = {}
+        cfgs = {}
+        for name, path in (("json", js), ("binary", bs)):
+            best = None
+            for _ in range(2):
+                t0 = time.perf_counter()
+                cfgs[name] = load_config(path)
+                dt = time.perf_counter() - t0
+                best = dt if best is None else min(best, dt)
+            times[name] = best
+        same = all(np.array_equal(np.asarray(cfgs["json"][k]), np.asarray(cfgs["binary"][k]))
+                   for k in cfgs["json"])
+        out["binary_seed"] = {"seed": "1024^2, C=3", "json_load_ms": times["json"] * 1e3,
+                              "binary_load_ms": times["binary"] * 1e3,
+                              "json_bytes": os.path.getsize(js), "binary_bytes": os.path.getsize(bs),
+                              "same_values": bool(same)}
     return out
 
 

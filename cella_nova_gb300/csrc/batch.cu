@@ -163,7 +163,7 @@ __global__ void __launch_bounds__(DiffTile<LOGN, V>::THREADS)
         const WorkItem it = items[i];
         const WorldDesc& w = worlds[it.world];
         diffusion_tile<LOGN, V>(w.A, w.state[parity], w.state[parity ^ 1], it.c, it.a, it.b,
-                                smb_diff, nullptr, 0);
+                                smb_diff, nullptr);
     }
 }
 
@@ -367,7 +367,7 @@ StepArgs world_step_args(const cg_batch* b, int w, int parity, const Variants& v
     a.tw = b->tw_by_logn[W.logn];
     a.udbg = nullptr;
     a.err = b->err;
-    a.render = nullptr;
+    a.levels = nullptr;
     a.groups = W.groups;
     a.gp = &b->d_worlds[w].gp;   // the descriptor's copy, in device memory
     a.var = var;

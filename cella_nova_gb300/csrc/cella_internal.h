@@ -70,7 +70,7 @@ struct StepArgs {
     const float2* tw;
     float* udbg;   // optional [K][n][n] f32: Re(conv) before the 1/n^2 scale
     int* err;      // device error word (bounded waits that timed out)
-    unsigned char* render;   // optional packed 0x00RRGGBB words, written by the diffusion
+    unsigned char* levels;   // optional [3][n][n] render level bytes, written by the diffusion
     KernelGroups groups;
     const GrowthParams* gp;   // device-resident: updated without re-capturing graphs
     Variants var;
@@ -192,6 +192,8 @@ bool hermitian_part_is_real(const float* spec, int n);
 cudaError_t launch_mass_f64(const float* x, int C, size_t px, double* partial, int nblocks,
                             double* out, cudaStream_t s);
 cudaError_t launch_render(const float* x, int C, size_t px, unsigned* out, cudaStream_t s);
+cudaError_t launch_pack_levels(const unsigned char* levels, int C, size_t px, unsigned* out,
+                               cudaStream_t s);
 // Tensor map over U (K kernels x n/2 rows kx x n float2 y, kx-major) for the
 // inverse row pass's 2-D tile loads: boxes of rb values of y by up to 256 kx.
 cudaError_t encode_u_map(CUtensorMap* map, const float2* U, int n, int K, int rb);

@@ -5,8 +5,8 @@
 // kernel, conv, render) become: two state planes used in turn (no
 // new_channel -> channel copy, mod.rs:377-383), row spectra, packed kernel
 // half spectra, column-inverted products and the affinity exponential.  The
-// Z buffer and the render buffer do not exist: Z lives in shared memory and
-// rendering is not part of the step.  A step is two CUDA graphs, one per
+// Z buffer does not exist (Z lives in shared memory); the render buffer is
+// written only by the render calls.  A step is two CUDA graphs, one per
 // ping-pong parity, captured once at creation.
 #include <cuda_runtime.h>
 
@@ -238,6 +238,7 @@ struct cg_sim {
     cudaGraphExec_t graph8[2] = {nullptr, nullptr};    // kStepsPerGraph steps, per parity
     cudaGraphExec_t graphR[2] = {nullptr, nullptr};    // one step that also renders
     unsigned* render = nullptr;   // [n][n] packed 0x00RRGGBB
+    unsigned char* levels = nullptr;   // [3][n][n] render levels of a rendering step
     unsigned char* frames[2] = {nullptr, nullptr};   // pinned RGB24 frames (frame streaming)
     cudaEvent_t frame_ev[2] = {nullptr, nullptr};
     double* ring_partial = nullptr;   // kernel builder: K * kRingBlocks * kMaxRings
@@ -313,6 +314,7 @@ void release(cg_sim* s) {
     cudaFree(s->err);
     cudaFree(s->dparams);
     cudaFree(s->render);
+    cudaFree(s->levels);
     for (auto& f : s->frames)
         if (f) cudaFreeHost(f);
     for (auto& e : s->frame_ev)
@@ -346,7 +348,8 @@ constexpr int kStepsPerGraph = 8;
 // inverse row pass of step t-2 read.  Everything else is per channel and in
 // stream order.
 // nsteps steps from parity p0 into one graph; with render, the last step's
-// diffusion kernels also write the render buffer.
+// diffusion kernels also write the level planes, and after the channels have
+// joined, k_pack_levels turns them into the render buffer's words.
 // fixed_parity: every captured step reads the same state (p0) and writes the
 // other buffer (U still alternates, so the dependencies are a real run's),
 // so replaying the graph does not advance the world (the tuner's timing)
@@ -366,9 +369,11 @@ cudaError_t capture_steps(cg_sim* s, int p0, int nsteps, bool render, cudaGraphE
                     a.x_in = s->state[p0];
                     a.x_out = s->state[p0 ^ 1];
                 }
-                if (render && t == nsteps - 1) a.render = reinterpret_cast<unsigned char*>(s->render);
+                if (render && t == nsteps - 1) a.levels = s->levels;
                 le = s->ops->step(a, kPhaseAll, st0);
             }
+            if (render && le == cudaSuccess)
+                le = launch_pack_levels(s->levels, C, s->px(), s->render, st0);
             e = cudaStreamEndCapture(st0, &g);
             if (le != cudaSuccess) e = le;
         }
@@ -400,7 +405,7 @@ cudaError_t capture_steps(cg_sim* s, int p0, int nsteps, bool render, cudaGraphE
                 a.x_in = s->state[p0];
                 a.x_out = s->state[p0 ^ 1];
             }
-            if (render && t == nsteps - 1) a.render = reinterpret_cast<unsigned char*>(s->render);
+            if (render && t == nsteps - 1) a.levels = s->levels;
             for (int c = 0; c < C && le == cudaSuccess; ++c) {
                 le = s->ops->step_channel(a, kPhaseRowFwd, c, st[c]);
                 // U alternates with the parity, so the column pass of step t
@@ -424,6 +429,8 @@ cudaError_t capture_steps(cg_sim* s, int p0, int nsteps, bool render, cudaGraphE
             le = cudaEventRecord(ecol[c], st[c]);
             if (le == cudaSuccess) le = cudaStreamWaitEvent(st[0], ecol[c], 0);
         }
+        if (render && le == cudaSuccess)
+            le = launch_pack_levels(s->levels, C, s->px(), s->render, st[0]);
         e = cudaStreamEndCapture(st[0], &g);
         if (le != cudaSuccess) e = le;
     }
@@ -634,6 +641,7 @@ int cg_create(int n, int C, int K, const uint32_t* c0, const uint32_t* c1, const
     if (rc == CG_OK) chk(cudaMemset(s->err, 0, sizeof(int)), "memset(err)");
     if (rc == CG_OK) chk(cudaMalloc(&s->dparams, sizeof(DeviceParams)), "cudaMalloc(params)");
     if (rc == CG_OK) chk(cudaMalloc(&s->render, sizeof(unsigned) * px), "cudaMalloc(render)");
+    if (rc == CG_OK) chk(cudaMalloc(&s->levels, 3 * px), "cudaMalloc(render levels)");
     if (rc == CG_OK) chk(cudaMemsetAsync(s->render, 0, sizeof(unsigned) * px, s->stream), "memset");
     if (rc == CG_OK)
         chk(cudaMalloc(&s->ring_partial, sizeof(double) * K * kRingBlocks * kMaxRings),
@@ -803,7 +811,7 @@ int cg_stream_frames(cg_sim* s, int fd, int nframes, int steps_per_frame) {
                      "cudaEventCreate");
     }
     auto* dev_rgb = static_cast<unsigned char*>(s->staging);   // 8 B per pixel, 3 used
-    // Frame f is enqueued (its steps, the render epilogue, the RGB24
+    // Frame f is enqueued (its steps, the render levels and words, the RGB24
     // conversion and the copy into host buffer f % 2) before frame f - 1 is
     // written out, so the GPU computes while the host writes.
     for (int f = 0; f <= nframes; ++f) {

@@ -88,30 +88,89 @@ cudaError_t launch_mass_f64(const float* x, int C, size_t px, double* partial, i
 }
 
 // ---------------------------------------------------------------------------
-// Render the current state on its own (RenderPhase::run, render.rs:143-153):
-// one packed 0x00RRGGBB word per pixel from channels 0..2, the same levels the
-// diffusion epilogue writes.
+// Render (RenderPhase::run, render.rs:143-153): one packed 0x00RRGGBB word
+// per pixel from channels 0..2.  A thread takes four adjacent pixels: one
+// 16-byte load per channel and one 16-byte store of the four words (the
+// pixel count, n*n with n >= 16, is a multiple of four).
 // ---------------------------------------------------------------------------
 __global__ void k_render(const float* __restrict__ x, int C, size_t px,
                          unsigned* __restrict__ out) {
-    for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < px;
+    const size_t q = px / 4;
+    const float4* r4 = reinterpret_cast<const float4*>(x);
+    const float4* g4 = reinterpret_cast<const float4*>(x + px);
+    const float4* b4 = reinterpret_cast<const float4*>(x + 2 * px);
+    for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < q;
          i += size_t(gridDim.x) * blockDim.x) {
-        unsigned v = render_level(__ldg(&x[i])) << 16;
-        if (C > 1) v |= render_level(__ldg(&x[px + i])) << 8;
-        if (C > 2) v |= render_level(__ldg(&x[2 * px + i]));
-        out[i] = v;
+        const float4 r = __ldg(&r4[i]);
+        uint4 w = make_uint4(render_level(r.x) << 16, render_level(r.y) << 16,
+                             render_level(r.z) << 16, render_level(r.w) << 16);
+        if (C > 1) {
+            const float4 g = __ldg(&g4[i]);
+            w.x |= render_level(g.x) << 8;
+            w.y |= render_level(g.y) << 8;
+            w.z |= render_level(g.z) << 8;
+            w.w |= render_level(g.w) << 8;
+        }
+        if (C > 2) {
+            const float4 b = __ldg(&b4[i]);
+            w.x |= render_level(b.x);
+            w.y |= render_level(b.y);
+            w.z |= render_level(b.z);
+            w.w |= render_level(b.w);
+        }
+        reinterpret_cast<uint4*>(out)[i] = w;
+    }
+}
+
+// The words from the level planes the diffusion kernels wrote in a rendering
+// step: plane c (c < min(C, 3)) holds channel c's levels, one byte per pixel.
+// Four pixels per thread: a 4-byte load per plane, one 16-byte store.
+__global__ void k_pack_levels(const unsigned char* __restrict__ levels, int C, size_t px,
+                              unsigned* __restrict__ out) {
+    const size_t q = px / 4;
+    const uchar4* r4 = reinterpret_cast<const uchar4*>(levels);
+    const uchar4* g4 = reinterpret_cast<const uchar4*>(levels + px);
+    const uchar4* b4 = reinterpret_cast<const uchar4*>(levels + 2 * px);
+    for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < q;
+         i += size_t(gridDim.x) * blockDim.x) {
+        const uchar4 r = r4[i];
+        uint4 w = make_uint4(unsigned(r.x) << 16, unsigned(r.y) << 16, unsigned(r.z) << 16,
+                             unsigned(r.w) << 16);
+        if (C > 1) {
+            const uchar4 g = g4[i];
+            w.x |= unsigned(g.x) << 8;
+            w.y |= unsigned(g.y) << 8;
+            w.z |= unsigned(g.z) << 8;
+            w.w |= unsigned(g.w) << 8;
+        }
+        if (C > 2) {
+            const uchar4 b = b4[i];
+            w.x |= b.x;
+            w.y |= b.y;
+            w.z |= b.z;
+            w.w |= b.w;
+        }
+        reinterpret_cast<uint4*>(out)[i] = w;
     }
 }
 
 // download_render's conversion (mod.rs:322-329): packed words -> RGB24 bytes.
+// Four pixels per thread: one 16-byte load, their 12 bytes as three 4-byte
+// stores (little-endian: R, G, B of pixel 0 first).
 __global__ void k_rgb24(const unsigned* __restrict__ in, unsigned char* __restrict__ out,
                         size_t px) {
-    for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < px;
+    const size_t q = px / 4;
+    for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < q;
          i += size_t(gridDim.x) * blockDim.x) {
-        const unsigned v = __ldg(&in[i]);
-        out[3 * i] = static_cast<unsigned char>(v >> 16);
-        out[3 * i + 1] = static_cast<unsigned char>(v >> 8);
-        out[3 * i + 2] = static_cast<unsigned char>(v);
+        const uint4 v = __ldg(reinterpret_cast<const uint4*>(in) + i);
+        const unsigned b[12] = {v.x >> 16 & 255u, v.x >> 8 & 255u, v.x & 255u,
+                                v.y >> 16 & 255u, v.y >> 8 & 255u, v.y & 255u,
+                                v.z >> 16 & 255u, v.z >> 8 & 255u, v.z & 255u,
+                                v.w >> 16 & 255u, v.w >> 8 & 255u, v.w & 255u};
+        unsigned* o = reinterpret_cast<unsigned*>(out + 12 * i);
+#pragma unroll
+        for (int j = 0; j < 3; ++j)
+            o[j] = b[4 * j] | b[4 * j + 1] << 8 | b[4 * j + 2] << 16 | b[4 * j + 3] << 24;
     }
 }
 
@@ -123,12 +182,18 @@ static int grid_for(size_t count) {
 }
 
 cudaError_t launch_render(const float* x, int C, size_t px, unsigned* out, cudaStream_t s) {
-    k_render<<<grid_for(px), 256, 0, s>>>(x, C, px, out);
+    k_render<<<grid_for(px / 4), 256, 0, s>>>(x, C, px, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pack_levels(const unsigned char* levels, int C, size_t px, unsigned* out,
+                               cudaStream_t s) {
+    k_pack_levels<<<grid_for(px / 4), 256, 0, s>>>(levels, C, px, out);
     return cudaGetLastError();
 }
 
 cudaError_t launch_rgb24(const unsigned* in, unsigned char* out, size_t px, cudaStream_t s) {
-    k_rgb24<<<grid_for(px), 256, 0, s>>>(in, out, px);
+    k_rgb24<<<grid_for(px / 4), 256, 0, s>>>(in, out, px);
     return cudaGetLastError();
 }
 

@@ -1,5 +1,5 @@
-// Render levels shared by the diffusion epilogue and the standalone render
-// kernels.
+// Render levels, shared by the render kernel and the diffusion kernels'
+// level planes (iterate_and_render).
 #pragma once
 
 #include <cuda_runtime.h>
@@ -10,31 +10,15 @@ namespace cg {
 // Render (render.rs, render_main of compute_1024.wgsl:428-443): channels 0, 1
 // and 2 become the R, G and B levels u32(sqrt(clamp(1.5 c, 0, 1)) * 255) of
 // a packed 0x00RRGGBB word per pixel.  Channels a world lacks render as 0.
-// As an epilogue of the per-channel diffusion kernel, channel c stores only
-// its own bytes of the word (little-endian: B at byte 0, G at 1, R at 2),
-// and the kernels of channels 0..2 together write all four.
+// In a rendering step, the diffusion kernel of channel c < 3 also writes its
+// new values' levels to byte plane c (one byte per pixel, stored with the
+// state), and k_pack_levels joins the planes into the words.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ unsigned render_level(float v) {
     return __float2uint_rz(__fsqrt_rn(fminf(fmaxf(v * 1.5f, 0.f), 1.f)) * 255.f);
 }
-
-__device__ __forceinline__ void render_store(unsigned char* __restrict__ rb, int nch, int c,
-                                             size_t p, float v) {
-    const unsigned l = render_level(v);
-    unsigned char* px = rb + 4 * p;
-    if (c == 0) {
-        if (nch == 1)
-            *reinterpret_cast<unsigned*>(px) = l << 16;
-        else
-            *reinterpret_cast<unsigned short*>(px + 2) = static_cast<unsigned short>(l);
-    } else if (c == 1) {
-        if (nch == 2)
-            *reinterpret_cast<unsigned short*>(px) = static_cast<unsigned short>(l << 8);
-        else
-            px[1] = static_cast<unsigned char>(l);
-    } else if (c == 2) {
-        px[0] = static_cast<unsigned char>(l);
-    }
+__device__ __forceinline__ unsigned char render_level_byte(float v) {
+    return static_cast<unsigned char>(render_level(v));
 }
 
 }  // namespace cg

@@ -685,7 +685,7 @@ template <int LOGN, int V = 0>
 __device__ __forceinline__ void diffusion2_body(const float* __restrict__ A,
                                                 const float* __restrict__ x,
                                                 float* __restrict__ out, int c, int x0, int y0,
-                                                float* smf, unsigned char* render, int nch) {
+                                                float* smf, unsigned char* levels) {
     using D = DiffGeo2<LOGN, V>;
     constexpr int N = D::N, TX = D::TX, AS = D::AS, AH = D::AH, HW = D::HW, QH = D::QH;
     constexpr int MASK = N * N - 1;            // row offsets wrap as (row * N) & MASK
@@ -764,7 +764,8 @@ __device__ __forceinline__ void diffusion2_body(const float* __restrict__ A,
         const float* pb = sAl + (r0 + 2) * AS + fq + 4;
         const int p0 = (y0 + r0) * N + x0 + fq;
         float* oc = out + size_t(c) * N * N + p0;
-        const bool draw = render != nullptr && c < 3;
+        unsigned char* lv = levels ? levels + size_t(c) * N * N + p0 : nullptr;
+        const bool draw = levels != nullptr && c < 3;
         float s0 = pq[0] + pq[1] + pq[2];
         float s1 = pq[HW] + pq[HW + 1] + pq[HW + 2];
 #pragma unroll
@@ -774,7 +775,7 @@ __device__ __forceinline__ void diffusion2_body(const float* __restrict__ A,
             const float a = pa[i * AS] + pb[i * AS];
             const float v = a * ((s0 + s1) + s2);
             oc[i * N] = v;
-            if (draw) render_store(render, nch, c, size_t(p0 + i * N), v);
+            if (draw) lv[i * N] = render_level_byte(v);
             s0 = s1;
             s1 = s2;
         }
@@ -808,8 +809,7 @@ template <int LOGN, int V = 0>
 __device__ __forceinline__ void diffusion_pair_body(const float* __restrict__ A,
                                                     const float* __restrict__ x,
                                                     float* __restrict__ out, int c, int x0,
-                                                    int y0, float* smf, unsigned char* render,
-                                                    int nch) {
+                                                    int y0, float* smf, unsigned char* levels) {
     using D = DiffGeoPair<LOGN, V>;
     constexpr int N = D::N, AS = D::AS, AH = D::AH, QH = D::QH, QS = D::QS;
     constexpr int MASK = N * N - 1;
@@ -905,7 +905,8 @@ __device__ __forceinline__ void diffusion_pair_body(const float* __restrict__ A,
         const float* pb = sAl + (r0 + 2) * AS + 2 * ou + 4;
         const int p0 = (y0 + r0) * N + x0 + 2 * ou;
         float* oc = out + size_t(c) * N * N + p0;
-        const bool draw = render != nullptr && c < 3;
+        unsigned char* lv = levels ? levels + size_t(c) * N * N + p0 : nullptr;
+        const bool draw = levels != nullptr && c < 3;
         float s0[2], s1[2];
         sum3x2(pq, s0[0], s0[1]);
         sum3x2(pq + QS, s1[0], s1[1]);
@@ -918,11 +919,9 @@ __device__ __forceinline__ void diffusion_pair_body(const float* __restrict__ A,
             const float2 v = make_float2((ah.x + al.x) * ((s0[0] + s1[0]) + s2[0]),
                                          (ah.y + al.y) * ((s0[1] + s1[1]) + s2[1]));
             *reinterpret_cast<float2*>(oc + i * N) = v;
-            if (draw) {
-                const size_t p = size_t(p0 + i * N);
-                render_store(render, nch, c, p, v.x);
-                render_store(render, nch, c, p + 1, v.y);
-            }
+            if (draw)
+                *reinterpret_cast<uchar2*>(lv + i * N) =
+                    make_uchar2(render_level_byte(v.x), render_level_byte(v.y));
             s0[0] = s1[0];
             s0[1] = s1[1];
             s1[0] = s2[0];
@@ -955,8 +954,8 @@ struct DiffGeoReg {
 template <int LOGN, int STRIP>
 __device__ __forceinline__ void diffusion_reg_body(const float* __restrict__ A,
                                                    const float* __restrict__ x,
-                                                   float* __restrict__ out, int c, int x0, int y0,
-                                                   unsigned char* render, int nch) {
+                                                   float* __restrict__ out, int c, int x0,
+                                                   int y0, unsigned char* levels) {
     using D = DiffGeoReg<LOGN, STRIP>;
     constexpr int N = D::N, MASK = N * N - 1;
     const int col = x0 + 4 * (threadIdx.x % (D::TX / 4));   // first of this thread's columns
@@ -965,7 +964,8 @@ __device__ __forceinline__ void diffusion_reg_body(const float* __restrict__ A,
     const float* xc = x + size_t(c) * N * N;
     float* oc = out + size_t(c) * N * N;
     const int cl = (col - 4) & (N - 1), cr = (col + 4) & (N - 1);
-    const bool draw = render != nullptr && c < 3;
+    unsigned char* lv = levels ? levels + size_t(c) * N * N : nullptr;
+    const bool draw = levels != nullptr && c < 3;
     // columns col-4 .. col+7 of row y (toroidal)
     auto ld3 = [&](const float* p, int y, float4& l, float4& m, float4& r) {
         const float* row = p + ((y * N) & MASK);
@@ -1028,12 +1028,10 @@ __device__ __forceinline__ void diffusion_reg_body(const float* __restrict__ A,
                                          a.w * ((qs[s0][3] + qs[s1][3]) + qs[b][3]));
             const int p = (ya - 2) * N + col;
             *reinterpret_cast<float4*>(oc + p) = v;
-            if (draw) {
-                render_store(render, nch, c, size_t(p), v.x);
-                render_store(render, nch, c, size_t(p + 1), v.y);
-                render_store(render, nch, c, size_t(p + 2), v.z);
-                render_store(render, nch, c, size_t(p + 3), v.w);
-            }
+            if (draw)
+                *reinterpret_cast<uchar4*>(lv + p) =
+                    make_uchar4(render_level_byte(v.x), render_level_byte(v.y),
+                                render_level_byte(v.z), render_level_byte(v.w));
         }
     }
 }
@@ -1071,25 +1069,25 @@ template <int LOGN, int V>
 __device__ __forceinline__ void diffusion_tile(const float* __restrict__ A,
                                                const float* __restrict__ x,
                                                float* __restrict__ out, int c, int x0, int y0,
-                                               float* smf, unsigned char* render, int nch) {
+                                               float* smf, unsigned char* levels) {
     using T = DiffTile<LOGN, V>;
     if constexpr (T::REG)
-        diffusion_reg_body<LOGN, T::STRIP>(A, x, out, c, x0, y0, render, nch);
+        diffusion_reg_body<LOGN, T::STRIP>(A, x, out, c, x0, y0, levels);
     else if constexpr (T::PAIR)
-        diffusion_pair_body<LOGN, V>(A, x, out, c, x0, y0, smf, render, nch);
+        diffusion_pair_body<LOGN, V>(A, x, out, c, x0, y0, smf, levels);
     else
-        diffusion2_body<LOGN, V>(A, x, out, c, x0, y0, smf, render, nch);
+        diffusion2_body<LOGN, V>(A, x, out, c, x0, y0, smf, levels);
 }
 
 template <int LOGN, int V = 0>
 __global__ void __launch_bounds__(DiffTile<LOGN, V>::THREADS)
     k_diffusion(const float* __restrict__ A, const float* __restrict__ x, float* __restrict__ out,
-                int cbase, unsigned char* __restrict__ render, int nch) {
+                int cbase, unsigned char* __restrict__ levels) {
     extern __shared__ __align__(128) float sm_diff[];
     pdl_wait();
     pdl_launch_dependents();
     diffusion_tile<LOGN, V>(A, x, out, blockIdx.z + cbase, blockIdx.x * DiffTile<LOGN, V>::TX,
-                            blockIdx.y * DiffTile<LOGN, V>::TY, sm_diff, render, nch);
+                            blockIdx.y * DiffTile<LOGN, V>::TY, sm_diff, levels);
 }
 
 // ---------------------------------------------------------------------------
@@ -1229,7 +1227,7 @@ cudaError_t launch_diff(const StepArgs& a, int c_lo, int nc, cudaStream_t st) {
     constexpr int N = 1 << LOGN;
     using D = DiffTile<LOGN, V>;
     return launch_pdl(k_diffusion<LOGN, V>, dim3(N / D::TX, N / D::TY, nc), D::THREADS,
-                      D::SMEM, st, a.A, a.x_in, a.x_out, c_lo, a.render, a.C);
+                      D::SMEM, st, a.A, a.x_in, a.x_out, c_lo, a.levels);
 }
 
 #define CG_VARIANT_SWITCH(v, FN, ...)            \

@@ -117,11 +117,11 @@ int cg_step(cg_sim* sim, int nsteps);
  * the caller's stream instead of the handle's. */
 int cg_iterate_on(cg_sim* sim, cg_stream_t stream);
 
-/* GpuMaceLenia::iterate_and_render, mod.rs:390-431: one step whose diffusion
- * kernels also write the render buffer (render_main, compute_1024.wgsl:
- * 428-443): per pixel the packed word 0x00RRGGBB with R, G, B =
- * u32(sqrt(clamp(1.5 c, 0, 1)) * 255) of channels 0, 1, 2 (0 for channels the
- * world lacks).  Enqueued. */
+/* GpuMaceLenia::iterate_and_render, mod.rs:390-431: one step, then the render
+ * kernel on the new state, in one graph launch (render_main,
+ * compute_1024.wgsl:428-443): per pixel the packed word 0x00RRGGBB with R, G,
+ * B = u32(sqrt(clamp(1.5 c, 0, 1)) * 255) of channels 0, 1, 2 (0 for channels
+ * the world lacks).  Enqueued. */
 int cg_iterate_and_render(cg_sim* sim);
 
 /* RenderPhase::run, render.rs:143-153: render the current state without
