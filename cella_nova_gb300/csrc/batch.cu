@@ -518,6 +518,23 @@ cudaError_t capture_batch_graphs(cg_batch* b) {
     return e;
 }
 
+// Device ms of one whole batched step (every side, as captured), averaged
+// over reps launches of the step graph of the current parity: each launch
+// reads the current state and writes the spare buffer, so nothing steps.
+int time_batch_step(cg_batch* b, int reps, double* ms) {
+    cudaError_t e = cudaGraphLaunch(b->graph[b->cur], b->stream);   // warm-up
+    if (e == cudaSuccess) e = cudaEventRecord(b->ev[0], b->stream);
+    for (int r = 0; r < reps && e == cudaSuccess; ++r)
+        e = cudaGraphLaunch(b->graph[b->cur], b->stream);
+    if (e == cudaSuccess) e = cudaEventRecord(b->ev[1], b->stream);
+    if (e == cudaSuccess) e = cudaEventSynchronize(b->ev[1]);
+    float f = 0.f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&f, b->ev[0], b->ev[1]);
+    if (e != cudaSuccess) return cuda_fail(e, "timing the batched step");
+    *ms = double(f) / reps;
+    return CG_OK;
+}
+
 // Device ms of one step of class sc alone (its current mode and variants),
 // averaged over reps launches of a captured one-step graph.
 int time_class_step(cg_batch* b, const cg_batch::SizeClass& sc, int reps, double* ms) {
@@ -991,6 +1008,28 @@ int cg_batch_autotune(cg_batch* b, int reps, int* chosen, double* ms_out) {
             }
         }
         sc.mode = best_mode;
+    }
+    // The sides run concurrently in the step graph, so a mode that wins for
+    // a side alone can lose in the whole step (two sides' world branches
+    // competing for the SMs).  With at most three sides, every combination
+    // of modes is timed on the whole step and the fastest kept.
+    const int nsides = int(b->classes.size());
+    if (nsides >= 2 && nsides <= 3) {
+        int best_mask = 0;
+        for (int i = 0; i < nsides; ++i) best_mask |= b->classes[size_t(i)].mode << i;
+        double best_t = -1.0;
+        for (int mask = 0; mask < (1 << nsides); ++mask) {
+            for (int i = 0; i < nsides; ++i) b->classes[size_t(i)].mode = (mask >> i) & 1;
+            BCHECK(capture_batch_graphs(b), "capturing a batched step graph to time");
+            double t = 0.0;
+            const int rc = time_batch_step(b, reps, &t);
+            if (rc != CG_OK) return rc;
+            if (best_t < 0.0 || t < best_t) {
+                best_t = t;
+                best_mask = mask;
+            }
+        }
+        for (int i = 0; i < nsides; ++i) b->classes[size_t(i)].mode = (best_mask >> i) & 1;
     }
     int rc = batch_sync_check(b);
     if (rc != CG_OK) return rc;

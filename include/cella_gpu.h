@@ -403,10 +403,13 @@ int cg_batch_info(cg_batch* b, int* items4, int* grid4);
 /* Autotuner of the batch: per grid side present and per phase, times the
  * variants that phase has at that side (those of cg_autotune) on the live
  * batch without stepping it, keeps the fastest, then times a step of the
- * side in each mode (cg_batch_set_mode), keeps the faster and re-captures
- * the step graphs.  chosen[6*4] and ms[6*4*CG_MAX_VARIANTS] (either may be NULL) are
- * indexed by grid side 64, 128, ..., 2048, then phase, then variant; sides
- * the batch lacks give -1, variants a phase lacks give ms -1. */
+ * side in each mode (cg_batch_set_mode) and keeps the faster.  The sides run
+ * concurrently in the step graph, so with two or three sides every
+ * combination of their modes is then timed on the whole step and the
+ * fastest kept.  Re-captures the step graphs.  chosen[6*4] and
+ * ms[6*4*CG_MAX_VARIANTS] (either may be NULL) are indexed by grid side 64,
+ * 128, ..., 2048, then phase, then variant; sides the batch lacks give -1,
+ * variants a phase lacks give ms -1. */
 int cg_batch_autotune(cg_batch* b, int reps, int* chosen, double* ms);
 /* Set the variants of the batch's worlds of grid side n (as cg_set_variants
  * does for one world); re-captures the step graphs. */
