@@ -32,6 +32,26 @@ def test_iterate_and_render_matches_oracle_render(n, C):
         np.testing.assert_array_equal(a.download_render_packed(), packed)
 
 
+@pytest.mark.parametrize("n,C", [(64, 3), (256, 2), (512, 3)])
+def test_render_levels_in_every_diffusion_variant(n, C):
+    """A rendering step's level bytes come from whichever diffusion body the
+    world runs (one byte, two or four per store): every variant gives the
+    oracle's words and the same state as a plain step."""
+    cr = make_creature(n, C, seed=60 + n, radius=(max(2.0, n / 16), max(4.0, n / 6)),
+                       seed_box=n // 2)
+    for v in range(4):
+        with GpuMaceLenia.from_creature(cr) as a, GpuMaceLenia.from_creature(cr) as b:
+            a.set_variants([0, 0, 0, v])
+            b.set_variants([0, 0, 0, v])
+            for _ in range(2):
+                a.iterate_and_render()
+                b.iterate()
+            x = a.state()
+            np.testing.assert_array_equal(x, b.state(), err_msg=f"diffusion variant {v}")
+            np.testing.assert_array_equal(a.download_render_packed(), O.render_np(x),
+                                          err_msg=f"diffusion variant {v}")
+
+
 def test_render_saturates_and_clamps():
     n, C = 64, 3
     cr = make_creature(n, C, seed=5, radius=(4, 10), seed_box=32)
