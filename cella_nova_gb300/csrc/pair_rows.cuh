@@ -165,7 +165,7 @@ __device__ __forceinline__ void pair_r2c_body(const float* __restrict__ state,
 // at kx * RB + row), the next kernel's tile is issued as soon as the first
 // pass has read the current one.  Returns false if a bounded wait timed out.
 // ---------------------------------------------------------------------------
-template <class P>
+template <class P, bool DBG = false>
 __device__ __forceinline__ bool pair_c2r_growth_body(const CUtensorMap* umap, bool umap_global,
                                                      float* __restrict__ A,
                                                      const float2* __restrict__ tw,
@@ -237,12 +237,12 @@ __device__ __forceinline__ bool pair_c2r_growth_body(const CUtensorMap* umap, bo
         };
         const int k = groups.out_idx[base + gi];
         const float mu = gp.mu[k], c2 = gp.c2[k], w2 = gp.w2[k];
-        float* ud = udbg ? udbg + (size_t(k) * N + y0) * N : nullptr;
+        float* ud = DBG ? udbg + (size_t(k) * N + y0) * N : nullptr;
         auto gst = [&](int s, int i, float2 v, int it, int r) {
             const float dx = v.x - mu, dy = v.y - mu;
             acc[it][r].x = fmaf(w2, ex2_approx(dx * dx * c2), acc[it][r].x);
             acc[it][r].y = fmaf(w2, ex2_approx(dy * dy * c2), acc[it][r].y);
-            if (ud) {
+            if constexpr (DBG) {
                 ud[size_t(2 * s) * N + i] = v.x * udbg_scale;
                 ud[size_t(2 * s + 1) * N + i] = v.y * udbg_scale;
             }

@@ -491,7 +491,7 @@ __global__ void __launch_bounds__(Geo<LOGN, V>::CT, Geo<LOGN, V>::COL_MINB)
 // completed phases, so one CTA can run many tiles back to back.
 // grid (N/RB, C), block RT.
 // ---------------------------------------------------------------------------
-template <int LOGN, int V = 0>
+template <int LOGN, int V = 0, bool DBG = false>
 __device__ __forceinline__ bool row_c2r_growth_body(const CUtensorMap* umap, bool umap_global,
                                                     float* __restrict__ A,
                                                     const float2* __restrict__ tw,
@@ -562,17 +562,16 @@ __device__ __forceinline__ bool row_c2r_growth_body(const CUtensorMap* umap, boo
         };
         const int k = groups.out_idx[base + gi];
         const float mu = gp.mu[k], c2 = gp.c2[k], w2 = gp.w2[k];
-        float* ud = udbg ? udbg + (size_t(k) * G::N + y0) * G::N : nullptr;
+        float* ud = DBG ? udbg + (size_t(k) * G::N + y0) * G::N : nullptr;
         // w G = w (2 e - 1) with e = exp(-(u-mu)^2 / (2 sigma^2)) = 2^(d^2 c2):
         // accumulate 2 w e here, subtract sum(w) once per channel below.
         auto gst = [&](int s, int i, float2 v, int it, int r) {
             const float dx = v.x - mu, dy = v.y - mu;
             acc[it][r].x = fmaf(w2, ex2_approx(dx * dx * c2), acc[it][r].x);
             acc[it][r].y = fmaf(w2, ex2_approx(dy * dy * c2), acc[it][r].y);
-            if (ud) {
+            if constexpr (DBG)
                 reinterpret_cast<float2*>(ud + size_t(s) * G::N)[i] =
                     make_float2(v.x * udbg_scale, v.y * udbg_scale);
-            }
         };
         // the first pass reads the landing tile and the last one keeps its
         // values in registers: neither needs its load-store barrier
@@ -604,23 +603,25 @@ __device__ __forceinline__ bool row_c2r_growth_body(const CUtensorMap* umap, boo
 }
 
 // The inverse row pass + growth of variant V on the RB rows from y0
-// (C2RShape).
-template <int LOGN, int V>
+// (C2RShape).  DBG: also write each kernel's u (scaled by udbg_scale) to
+// udbg, for the debug read of the convolution buffer; the step's own
+// kernels are built without it, so the per-value store costs them nothing.
+template <int LOGN, int V, bool DBG = false>
 __device__ __forceinline__ bool row_c2r_growth_variant(
     const CUtensorMap* umap, bool umap_global, float* __restrict__ A,
     const float2* __restrict__ tw, const KernelGroups& groups, const GrowthParams& gp, float temp,
     float* __restrict__ udbg, float udbg_scale, int c, int y0, float2* sm, uint64_t* barp,
     uint32_t& phase, int* err) {
     if constexpr (C2RShape<LOGN, V>::PAIR)
-        return pair_c2r_growth_body<typename C2RShape<LOGN, V>::P>(
+        return pair_c2r_growth_body<typename C2RShape<LOGN, V>::P, DBG>(
             umap, umap_global, A, tw, groups, gp, temp, udbg, udbg_scale, c, y0, sm, barp, phase,
             err);
     else
-        return row_c2r_growth_body<LOGN, V>(umap, umap_global, A, tw, groups, gp, temp, udbg,
-                                            udbg_scale, c, y0, sm, barp, phase, err);
+        return row_c2r_growth_body<LOGN, V, DBG>(umap, umap_global, A, tw, groups, gp, temp,
+                                                 udbg, udbg_scale, c, y0, sm, barp, phase, err);
 }
 
-template <int LOGN, int V = 0>
+template <int LOGN, int V = 0, bool DBG = false>
 __global__ void __launch_bounds__(C2RShape<LOGN, V>::RT, C2RShape<LOGN, V>::MINB)
     k_row_c2r_growth(const __grid_constant__ CUtensorMap umap, float* __restrict__ A,
                      const float2* __restrict__ tw, const __grid_constant__ KernelGroups groups,
@@ -632,7 +633,7 @@ __global__ void __launch_bounds__(C2RShape<LOGN, V>::RT, C2RShape<LOGN, V>::MINB
     pdl_launch_dependents();
     init_tile_barrier(&bar);
     uint32_t phase = 0;
-    row_c2r_growth_variant<LOGN, V>(&umap, false, A, tw, groups, *gp, temp, udbg, udbg_scale,
+    row_c2r_growth_variant<LOGN, V, DBG>(&umap, false, A, tw, groups, *gp, temp, udbg, udbg_scale,
                                     blockIdx.y + cbase, blockIdx.x * C2RShape<LOGN, V>::RB,
                                     sm_c2r, &bar, phase, err);
 }
@@ -1139,6 +1140,13 @@ cudaError_t prepare_variant() {
                                 int(G::COL_SMEM));
 }
 
+template <int LOGN>
+cudaError_t prepare_c2r_debug() {
+    return cudaFuncSetAttribute(k_row_c2r_growth<LOGN, 0, true>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                int(C2RShape<LOGN, 0>::SMEM));
+}
+
 template <int LOGN, int V>
 cudaError_t prepare_diffusion() {
     return cudaFuncSetAttribute(k_diffusion<LOGN, V>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1154,6 +1162,7 @@ cudaError_t prepare_size() {
         if (e == cudaSuccess) e = prepare_variant<LOGN, 3>();
         if (e == cudaSuccess) e = prepare_variant<LOGN, 4>();
     }
+    if (e == cudaSuccess) e = prepare_c2r_debug<LOGN>();
     if (e == cudaSuccess) e = prepare_diffusion<LOGN, 0>();
     if (e == cudaSuccess) e = prepare_diffusion<LOGN, 1>();
     if (e == cudaSuccess) e = prepare_diffusion<LOGN, 2>();
@@ -1211,16 +1220,23 @@ cudaError_t launch_col(const StepArgs& a, int c_lo, int nc, cudaStream_t st) {
     return launch_pdl(k_col_conv<LOGN, V>, grid, G::CT, G::COL_SMEM, st, a.rowspec, a.kspec,
                       static_cast<const float*>(nullptr), a.U, a.tw, a.groups, a.err, c_lo);
 }
-template <int LOGN, int V>
-cudaError_t launch_c2r(const StepArgs& a, int c_lo, int nc, cudaStream_t st) {
+template <int LOGN, int V, bool DBG>
+cudaError_t launch_c2r_shape(const StepArgs& a, int c_lo, int nc, cudaStream_t st) {
     using R = C2RShape<LOGN, V>;
     constexpr int N = 1 << LOGN;
     CUtensorMap umap;   // passed by value: a graph capture keeps its own copy
     const cudaError_t e = encode_u_map(&umap, a.U, N, a.K, R::RB);
     if (e != cudaSuccess) return e;
-    return launch_pdl(k_row_c2r_growth<LOGN, V>, dim3(N / R::RB, nc), R::RT, R::SMEM, st, umap,
-                      a.A, a.tw, a.groups, a.gp, a.temp, a.udbg, float(N) * float(N), a.err,
+    return launch_pdl(k_row_c2r_growth<LOGN, V, DBG>, dim3(N / R::RB, nc), R::RT, R::SMEM, st,
+                      umap, a.A, a.tw, a.groups, a.gp, a.temp, a.udbg, float(N) * float(N), a.err,
                       c_lo);
+}
+// The inverse row pass in variant V; with a debug buffer (a.udbg, the debug
+// read of the convolution), variant 0's shape built with the debug store.
+template <int LOGN, int V>
+cudaError_t launch_c2r(const StepArgs& a, int c_lo, int nc, cudaStream_t st) {
+    if (a.udbg) return launch_c2r_shape<LOGN, 0, true>(a, c_lo, nc, st);
+    return launch_c2r_shape<LOGN, V, false>(a, c_lo, nc, st);
 }
 template <int LOGN, int V>
 cudaError_t launch_diff(const StepArgs& a, int c_lo, int nc, cudaStream_t st) {
