@@ -412,36 +412,47 @@ __device__ __forceinline__ bool col_conv_body(const float2* __restrict__ rowspec
         const int k = groups.in_idx[base + gi];
         const float2* kb = kspec + (size_t(k) * (M + 1) + M) * N;
         const float* kbr = KRE ? kre + (size_t(k) * (M + 1) + M) * N : nullptr;
-        auto ld_mul = [&](int s, int i, int it, int r) {
-            const float2 p = F[it][r];
-            if constexpr (KRE) {
-                // the roundings are pinned (no contraction left to the
-                // compiler), so that every CTA shape gives the same bits
-                const float kv = KR[s * N + i];
-                if (kx0 + s == 0) {   // p alpha + conj P(-ky) beta
-                    const float2 pm = cconj(W[pidx((N - i) & (N - 1))]);
-                    const float b = __ldg(&kbr[i]);
-                    return make_float2(__fmaf_rn(p.x, kv, __fmul_rn(pm.x, b)),
-                                       __fmaf_rn(p.y, kv, __fmul_rn(pm.y, b)));
-                }
-                return make_float2(__fmul_rn(p.x, kv), __fmul_rn(p.y, kv));
-            } else {
-                const float2 kv = KS[s * N + i];
-                if (kx0 + s == 0) {
-                    const float2 pm = cconj(W[pidx((N - i) & (N - 1))]);
-                    return cadd(cmul(p, kv), cmul(pm, __ldg(&kb[i])));
-                }
-                return cmul(p, kv);
-            }
-        };
         float2* dst = U + (size_t(k) * M + kx0) * N;
         auto gst = [&](int s, int i, float2 v, int, int) { dst[size_t(s) * N + i] = v; };
-        // inverse: the first pass reads W for column 0, so it keeps its
-        // barrier; the last one writes global memory
-        fft_with_hook<N, true, T, TW, !FREM, 16, false, true, false>(
-            ld_mul, wrows, wrows, gst, tw_inv, [&]() {
-            if (gi + 1 < cnt) issue_kernel(gi + 1);
-        });
+        // The inverse, in two forms chosen per CTA: the one holding column 0
+        // (kx0 == 0, its sequence 0) recombines p alpha + conj P(-ky) beta,
+        // reading another thread's P(-ky) from W, so its first pass keeps
+        // the load-store barrier; every other CTA multiplies only, with no
+        // per-value test and no barrier there.  The last pass writes global
+        // memory.
+        auto inverse = [&](auto col0) {
+            constexpr bool C0 = decltype(col0)::value;
+            auto ld_mul = [&](int s, int i, int it, int r) {
+                const float2 p = F[it][r];
+                if constexpr (KRE) {
+                    // the roundings are pinned (no contraction left to the
+                    // compiler), so that every CTA shape gives the same bits
+                    const float kv = KR[s * N + i];
+                    if (C0 && s == 0) {   // p alpha + conj P(-ky) beta
+                        const float2 pm = cconj(W[pidx((N - i) & (N - 1))]);
+                        const float b = __ldg(&kbr[i]);
+                        return make_float2(__fmaf_rn(p.x, kv, __fmul_rn(pm.x, b)),
+                                           __fmaf_rn(p.y, kv, __fmul_rn(pm.y, b)));
+                    }
+                    return make_float2(__fmul_rn(p.x, kv), __fmul_rn(p.y, kv));
+                } else {
+                    const float2 kv = KS[s * N + i];
+                    if (C0 && s == 0) {
+                        const float2 pm = cconj(W[pidx((N - i) & (N - 1))]);
+                        return cadd(cmul(p, kv), cmul(pm, __ldg(&kb[i])));
+                    }
+                    return cmul(p, kv);
+                }
+            };
+            fft_with_hook<N, true, T, TW, !FREM, 16, false, C0, false>(
+                ld_mul, wrows, wrows, gst, tw_inv, [&]() {
+                if (gi + 1 < cnt) issue_kernel(gi + 1);
+            });
+        };
+        if (kx0 == 0)
+            inverse(std::true_type{});
+        else
+            inverse(std::false_type{});
     }
     return true;
 }
