@@ -142,9 +142,10 @@ template <int LOGN, int V, class OUT>
 __device__ __forceinline__ void c2r_rows(float2* buf, const float2* __restrict__ tw, OUT& out) {
     using G = Geo<LOGN, V>;
     SmemRows rows{buf, G::RP};
-    auto ld0 = [&](int s, int m, int, int) -> float2 {
+    // m = j + q (M / R): m = 0 only in slot q = 0 (compile-time)
+    auto ld0 = [&](int s, int m, int, int q) -> float2 {
         const float2* row = buf + s * G::RP;
-        if (m == 0) {
+        if (q == 0 && m == 0) {
             const float2 x = row[0];
             return make_float2(x.x + x.y, x.x - x.y);
         }

@@ -221,14 +221,16 @@ __device__ __forceinline__ bool pair_c2r_growth_body(const CUtensorMap* umap, bo
     if (cnt > 0) issue(0);
     for (int gi = 0; gi < cnt; ++gi) {
         if (!wait_tile()) return false;
-        // Y[k], k = j + q (n / R1): q < R1/2 <=> k < M
+        // Y[k], k = j + q (n / R1): q < R1/2 <=> k < M; k = 0 and k = M need
+        // j = 0 and the slots q = 0 and q = R1/2 (compile-time after
+        // unrolling), so only those two slots test j
         auto ld0 = [&](int s, int k, int, int q) -> float2 {
             if (q < R1 / 2) {
                 const float4 t = lt[k * S + s];
-                if (k == 0) return make_float2(t.x, t.z);          // X_r0[0], X_r1[0] real
-                return make_float2(t.x - t.w, t.y + t.z);           // X_r0 + i X_r1
+                if (q == 0 && k == 0) return make_float2(t.x, t.z);   // X_r0[0], X_r1[0] real
+                return make_float2(t.x - t.w, t.y + t.z);             // X_r0 + i X_r1
             }
-            if (k == M) {
+            if (q == R1 / 2 && k == M) {
                 const float4 t = lt[s];
                 return make_float2(t.y, t.w);                       // X_r0[M], X_r1[M] real
             }

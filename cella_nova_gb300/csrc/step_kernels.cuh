@@ -560,8 +560,9 @@ __device__ __forceinline__ bool row_c2r_growth_body(const CUtensorMap* umap, boo
     for (int gi = 0; gi < cnt; ++gi) {
         if (!wait_tile()) return false;
         const float2* lt = land + srow;   // lt[kx * RB]
-        auto ld0 = [&](int, int m, int, int) -> float2 {
-            if (m == 0) {
+        // m = j + q (M / R): m = 0 only in slot q = 0 (compile-time)
+        auto ld0 = [&](int, int m, int, int q) -> float2 {
+            if (q == 0 && m == 0) {
                 const float2 x = lt[0];
                 return make_float2(x.x + x.y, x.x - x.y);
             }
