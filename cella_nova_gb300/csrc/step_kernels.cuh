@@ -175,22 +175,35 @@ template <int LOGN, int V>
 __device__ __forceinline__ void r2c_finish(float2* sm, const float2* __restrict__ tw,
                                            float2* __restrict__ dst) {
     using G = Geo<LOGN, V>;
-    constexpr int H = G::M / 2;
-    for (int item = threadIdx.x; item < G::RB * (H + 1); item += G::RT) {
-        const int s = item % G::RB, k = item / G::RB;
+    constexpr int H = G::M / 2, RB = G::RB;
+    auto split = [&](int s, int k, float2& lo, float2& hi) {   // X[k], conj X[M-k] for 0 < k <= H
         const float2* row = sm + s * G::RP;
-        if (k == 0) {
-            const float2 z = row[0];
-            dst[s] = make_float2(2.f * (z.x + z.y), 2.f * (z.x - z.y));
-        } else {
-            const float2 a = row[pidx(k)], b = row[pidx(G::M - k)];
-            const float2 E = make_float2(a.x + b.x, a.y - b.y);
-            const float2 D = make_float2(a.x - b.x, a.y + b.y);
-            const float2 O = make_float2(D.y, -D.x);
-            const float2 wo = cmul(__ldg(&tw[k]), O);
-            dst[size_t(k) * G::N + s] = cadd(E, wo);
-            if (k != H) dst[size_t(G::M - k) * G::N + s] = cconj(csub(E, wo));
-        }
+        const float2 a = row[pidx(k)], b = row[pidx(G::M - k)];
+        const float2 E = make_float2(a.x + b.x, a.y - b.y);
+        const float2 D = make_float2(a.x - b.x, a.y + b.y);
+        const float2 O = make_float2(D.y, -D.x);
+        const float2 wo = cmul(__ldg(&tw[k]), O);
+        lo = cadd(E, wo);
+        hi = cconj(csub(E, wo));
+    };
+    // k = 0 (slot 0 holds X[0] and X[M]) and k = H (its own mirror) take the
+    // first 2 RB threads, so the loop over 0 < k < H tests nothing per item
+    if (threadIdx.x < RB) {
+        const int s = threadIdx.x;
+        const float2 z = sm[s * G::RP];
+        dst[s] = make_float2(2.f * (z.x + z.y), 2.f * (z.x - z.y));
+    } else if (threadIdx.x < 2 * RB) {
+        const int s = threadIdx.x - RB;
+        float2 lo, hi;
+        split(s, H, lo, hi);
+        dst[size_t(H) * G::N + s] = lo;
+    }
+    for (int item = threadIdx.x + RB; item < RB * H; item += G::RT) {
+        const int s = item % RB, k = item / RB;
+        float2 lo, hi;
+        split(s, k, lo, hi);
+        dst[size_t(k) * G::N + s] = lo;
+        dst[size_t(G::M - k) * G::N + s] = hi;
     }
 }
 
